@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Benchmark of the mode-coupling hot path: coupling elements per second.
+
+Workload (default, --config all_spins_3071): every spin case of one (l1, l2)
+grid at lmax 3071 with nW = 6143 -- M00 (TT) on the temperature mask spectrum,
+M02 (TE) on the TxP cross-spectrum, M++ and M-- (EE/BB blocks) on the
+polarisation mask spectrum: 4 matrices of 3072 x 3072 FP64 per step.  One step
+is one pass of the hot path over that workload (one ps_mcm_multi_device call).
+
+  value     whole-job elements/s with the spectra resident in HBM
+  e2e       the same through the host-pointer C ABI call (ps_mcm_multi):
+            pinned host spectra in, pinned host matrices out, copies timed
+  roofline  the coupling kernel: algorithmic flops per launch / its CUDA-event
+            time, against this GPU's FMA-pipe peak measured live by the
+            library's probe kernel
+  cpu_baseline  the C/OpenMP oracle (the reference algorithm restated) on a
+            row sample of the same workload, on the host cores
+
+Multi-GPU (torchrun, one rank per GPU): every rank computes its own
+independent problem (weak scaling); no collective touches the data path.
+--impl reference times the CPU restatement of the reference algorithm.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "powerspectra.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "coupling elements/sec (l1,l2 pairs×spectra), chosen vs plain FP64 GPU, at ≤1e-6 rel err"
+UNIT = "elements/s"
+# Canonical algorithmic flops per l3-term (fixed accounting, sqrt and division count as one flop):
+FLOP_SPIN0 = 8 + 1          # two-term 00 recurrence
+FLOP_SPIN2 = 14 + 1 + 1     # three-term 22 recurrence
+FLOP_CONTRACT = 3           # per mask spectrum: product/square, (2 l3 + 1) weight, FMA
+L2_FLUSH_BYTES = 256 << 20  # > 126 MB L2
+
+
+def l3_terms(lmin, lmax, nW):
+    """l3-terms of one family summed over the pairs lmin <= l1 <= l2 <= lmax, l3 <= nW - 1."""
+    import numpy as np
+    tot = 0
+    for l1 in range(lmin, lmax + 1):
+        l2 = np.arange(l1, lmax + 1)
+        hi = np.minimum(l1 + l2, nW - 1)
+        tot += int(np.clip(hi - (l2 - l1) + 1, 0, None).sum())
+    return tot
+
+
+def workload(name, rank=0):
+    from powerspectra_gpu import synthetic as syn
+    if name == "all_spins_3071":
+        c = syn.all_spins(3071, seed=1 + 10 * rank)
+        Ws = {0: c["WT"], 1: c["WTP"], 2: c["WP"], 3: c["WP"]}
+        return {"name": name, "lmin": 0, "lmax": 3071, "nW": c["nW"], "Ws": Ws, "spectra": 3,
+                "cases": ["TT (M00, W_T)", "TE (M02, W_TxP)", "EE/BB diagonal (M++, W_P)", "EE/BB off-diagonal (M--, W_P)"]}
+    if name == "tt_767":
+        c = syn.tt_767(seed=rank)
+        return {"name": name, "lmin": 0, "lmax": 767, "nW": len(c["W"]), "Ws": {0: c["W"]}, "spectra": 1,
+                "cases": ["TT (M00)"]}
+    raise SystemExit("unknown --config %s" % name)
+
+
+def flops_per_launch(wl, terms):
+    spins = set(wl["Ws"])
+    f = 0
+    if spins & {0, 1}:
+        f += FLOP_SPIN0
+    if spins & {1, 2, 3}:
+        f += FLOP_SPIN2
+    f += FLOP_CONTRACT * wl["spectra"]
+    return f * terms
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(wl, budget_rows_stride, nthreads=0):
+    """Oracle (reference algorithm: one family fill + dot per pair and spin case, OpenMP
+    dynamic rows) on every stride-th l1 row; elements/s extrapolated by l3-term share."""
+    from oracle import oracle as o
+    lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
+    rows = list(range(lmin, lmax + 1, budget_rows_stride))
+    t0 = time.perf_counter()
+    for s, W in wl["Ws"].items():
+        o.inner_mcm(s, W, lmin, lmax, rows=rows, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    share = o.l3_terms(lmin, lmax, nW, rows) / o.l3_terms(lmin, lmax, nW)
+    n = lmax - lmin + 1
+    elements = len(wl["Ws"]) * n * n
+    threads = nthreads or o.max_threads()
+    return {"value": elements * share / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "every %d-th l1 row (%d rows, %.2f%% of the l3-terms), %d spin cases as separate passes, "
+                      "%.1f s, scaled by l3-term share" % (budget_rows_stride, len(rows), 100 * share,
+                                                            len(wl["Ws"]), dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    wl = workload(args.config)
+    stride = {"all_spins_3071": 48, "tt_767": 4}[args.config]
+    for _ in range(args.warmup):
+        cpu_baseline(wl, stride)
+    vals = [cpu_baseline(wl, stride) for _ in range(args.steps)]
+    value = statistics.median(v["value"] for v in vals)
+    n = wl["lmax"] - wl["lmin"] + 1
+    ms = len(wl["Ws"]) * n * n / value * 1e3
+    cb = dict(vals[-1])
+    cb["value"] = value
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["name"], "lmax": wl["lmax"], "nW": wl["nW"], "cases": wl["cases"],
+                       "implementation": "C/OpenMP restatement of the reference algorithm (Julia is not installed)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import powerspectra_gpu as pg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    wl = workload(args.config, rank)
+    lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
+    n = lmax - lmin + 1
+    spins = sorted(wl["Ws"])
+    mode = args.mode
+    ctx = pg.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    dW = {s: torch.tensor(wl["Ws"][s], device="cuda") for s in spins}
+    dM = {s: torch.empty((n, n), dtype=torch.float64, device="cuda") for s in spins}
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    wptr = {s: dW[s].data_ptr() for s in spins}
+    mptr = {s: dM[s].data_ptr() for s in spins}
+
+    def step():
+        ctx.mcm_multi_device(wptr, nW, lmin, lmax, mptr, n, mode=mode)
+
+    peak64 = ctx.fma_peak(fp64=True)
+    peak32 = ctx.fma_peak(fp64=False)
+    for _ in range(max(args.warmup, 3)):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    kernel_ms = []
+    n_launch0 = ctx.launch_count()
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        step()
+        kernel_ms.append(ctx.last_kernel_ms())  # coupling kernel only, events on this stream
+    t1.record(stream)
+    barrier()
+    launches = ctx.launch_count() - n_launch0
+    clk = clocks.stop()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    if dist is not None:
+        tt = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    elements = len(spins) * n * n
+    value = world * elements * args.steps / elapsed
+
+    # end to end through the host-pointer ABI: pinned spectra in, pinned matrices out
+    hW = {s: torch.from_numpy(np.ascontiguousarray(wl["Ws"][s])).pin_memory().numpy() for s in spins}
+    hM = {s: torch.empty((n, n), dtype=torch.float64).pin_memory().numpy().T for s in spins}  # F-ordered views
+    ctx.set_stream(0)
+    ctx.mcm_multi(hW, lmin, lmax, mode=mode, outs=hM)  # warm the host path
+    barrier()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.mcm_multi(hW, lmin, lmax, mode=mode, outs=hM)
+    barrier()
+    e_el = time.perf_counter() - e0
+    if dist is not None:
+        tt = torch.tensor([e_el], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e_el = float(tt.item())
+    e2e = {"value": world * elements * args.steps / e_el, "unit": UNIT,
+           "h2d_bytes_per_step": int(sum(min(len(hW[s]), 2 * lmax + 1) * 8 for s in spins)),
+           "d2h_bytes_per_step": int(elements * 8)}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    terms = l3_terms(lmin, lmax, nW)
+    fl = flops_per_launch(wl, terms)
+    kms = statistics.mean(kernel_ms)
+    peak = peak64 if mode in ("plain", "fp64") else peak32
+    achieved = fl / (kms * 1e-3)
+    roofline = {"bound": "fp64_fma_pipe" if mode in ("plain", "fp64") else "fp32_fma_pipe",
+                "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None,
+                "peak_source": "measured live by the library's FMA-chain probe kernel (MEASURED_PEAKS.json has no "
+                               "CUDA-core FP64/FP32 figure)",
+                "algorithmic_flops_per_launch": fl, "l3_terms_per_family": terms,
+                "kernel_ms_per_launch": kms}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if mode in ("plain", "fp64") else "f32",
+            "data": "synthetic",
+            "config": {"workload": wl["name"], "lmax": lmax, "nW": nW, "matrices_per_step": len(spins),
+                       "cases": wl["cases"], "mode": mode, "per_rank": "independent problem per GPU",
+                       "l2": "256 MiB buffer written between timed steps"},
+            "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+            "fma_peaks_tflops": {"fp64": peak64 / 1e12, "fp32": peak32 / 1e12}}
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(wl, {"all_spins_3071": 8, "tt_767": 1}[args.config])
+    print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", default="all_spins_3071")
+    ap.add_argument("--mode", default="plain", choices=("plain", "chosen"))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

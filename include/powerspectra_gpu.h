@@ -1,0 +1,133 @@
+/*
+ * powerspectra_gpu.h -- C ABI of the GB300 mode-coupling / covariance library.
+ *
+ * This is the drop-in boundary for the hot loops of PowerSpectra.jl.  A Julia
+ * `ccall` (or Python ctypes, or C) replaces the bodies of
+ *   inner_mcm00! / inner_mcm02! / inner_mcm++! / inner_mcm--!   (src/modecoupling.jl:78-159)
+ *   loop_covTTTT! ... loop_covTTEE!                            (src/covariance.jl:92-446)
+ * and keeps the callers (`mcm`, src/modecoupling.jl:192-256; `coupledcov`,
+ * src/covariance.jl:34-61) and their SpectralArray return types unchanged.
+ *
+ * Conventions shared by every entry point:
+ *   - Matrices are column-major (Julia's layout): element (l1, l2) of a result
+ *     with axes lmin:lmax lives at M[(l1 - lmin) + (l2 - lmin) * ld], with
+ *     ld >= lmax - lmin + 1.  This is `parent(M)` of a SpectralArray.
+ *   - Spectra are 0-indexed by l (`parent(V)` of a SpectralVector): W[l] for
+ *     l = 0..nW-1.  The l3 sum runs over the intersection of the 3j support and
+ *     0..nW-1, exactly like Xi_TT/Xi_EE/Xi_EB/Xi_TE (src/modecoupling.jl:3-66).
+ *   - Host-pointer entry points copy inputs in, compute, copy results out and
+ *     return when the output is filled (synchronous, like the Julia loops).
+ *     `_device` entry points take device pointers and enqueue on the context's
+ *     stream without synchronising.
+ *   - Every call returns PS_OK (0) or an error code; the message is kept per
+ *     context (ps_last_error).  The Julia shim maps non-zero to `error()`, the
+ *     way the reference raises on bad axes (@assert, src/modecoupling.jl:80)
+ *     and on an unknown spectrum (ArgumentError, src/modecoupling.jl:225).
+ *   - A context is not thread-safe: use one per host thread.
+ */
+#ifndef POWERSPECTRA_GPU_H
+#define POWERSPECTRA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ps_ctx ps_ctx;
+
+/* status codes */
+#define PS_OK 0
+#define PS_ERR_ARG 1          /* invalid argument (sizes, pointers, unknown case) */
+#define PS_ERR_CUDA 2         /* a CUDA runtime call or kernel failed */
+#define PS_ERR_OOM 3          /* device memory could not be allocated */
+#define PS_ERR_TIMEOUT 4      /* a bounded device wait gave up */
+#define PS_ERR_UNSUPPORTED 5  /* valid request this build does not provide */
+
+/* spin cases of the mode-coupling matrix (src/modecoupling.jl:192-224) */
+#define PS_SPIN_00 0 /* :TT, :M00                     -> inner_mcm00! */
+#define PS_SPIN_02 1 /* :TE, :ET, :TB, :BT, :M02, :M20 -> inner_mcm02! */
+#define PS_SPIN_PP 2 /* :M++ (EE/BB diagonal blocks)   -> inner_mcm++! */
+#define PS_SPIN_MM 3 /* :M-- (EE/BB off-diagonal)      -> inner_mcm--! */
+
+/* arithmetic of the 3j recurrence */
+#define PS_MODE_PLAIN_FP64 0 /* everything in FP64 */
+#define PS_MODE_CHOSEN 1     /* FP32-pipe recurrence with two-word compensation, FP64 anchors */
+
+/* family products / parities for ps_xi (Xi_TT = (00^2, ALL), Xi_EE = (22^2, EVEN),
+ * Xi_EB = (22^2, ODD), Xi_TE = (00x22, EVEN)) */
+#define PS_PROD_00_00 0
+#define PS_PROD_22_22 1
+#define PS_PROD_00_22 2
+#define PS_PARITY_ALL 0
+#define PS_PARITY_EVEN 1
+#define PS_PARITY_ODD 2
+
+/* covariance kinds (src/covariance.jl:47-60 dispatch; :305-333 planck flag) */
+#define PS_COV_TTTT 0
+#define PS_COV_EEEE 1
+#define PS_COV_TTTE 2
+#define PS_COV_TETE 3
+#define PS_COV_TEEE 4        /* planck=false: 00x22 family product */
+#define PS_COV_TEEE_PLANCK 5 /* planck=true (the reference default): 22^2 */
+#define PS_COV_TTEE 6
+
+/* Context lifetime.  Replaces get_thread_buffers (src/workspace.jl:216-223):
+ * device buffers are owned by the context and reused across calls. */
+int ps_create(int device, ps_ctx **out);
+void ps_destroy(ps_ctx *ctx);
+const char *ps_last_error(const ps_ctx *ctx);
+/* Use an external cudaStream_t (passed as void*) for all later work; NULL
+ * restores the context's own stream. */
+int ps_set_stream(ps_ctx *ctx, void *cuda_stream);
+int ps_synchronize(ps_ctx *ctx);
+
+/* One spin case: the body of inner_mcm00!/02!/++!/--! (src/modecoupling.jl:78-159).
+ * W: host, nW entries.  M: host, column-major, ld = ldm. */
+int ps_mcm(ps_ctx *ctx, int spin, const double *W, int64_t nW, int lmin, int lmax, int mode, double *M,
+           int64_t ldm);
+
+/* Several spin cases of one (l1, l2) grid in one pass: bit s of `cases` selects
+ * PS_SPIN_s, W[s] is its spectrum and M[s] its output.  The 00 and 22 families
+ * are generated once per pair and shared by every selected case; ++ and --
+ * come from one 22 family (the reference runs inner_mcm++! and inner_mcm--!
+ * separately for :EE_BB / :EB_BE, src/modecoupling.jl:210-223). */
+int ps_mcm_multi(ps_ctx *ctx, unsigned cases, const double *const W[4], int64_t nW, int lmin, int lmax, int mode,
+                 double *const M[4], int64_t ldm);
+/* Same with device pointers, enqueued on the context stream (no host copies). */
+int ps_mcm_multi_device(ps_ctx *ctx, unsigned cases, const double *const dW[4], int64_t nW, int lmin, int lmax,
+                        int mode, double *const dM[4], int64_t ldm);
+
+/* Symmetric Xi matrices (no (2l+1) weights) of K windows sharing one family
+ * product and parity: Xi_k[l1,l2] = sum_l3 (2 l3 + 1) x(l3) W_k[l3] / 4pi.
+ * The projectors of src/modecoupling.jl:3-66 over a whole (l1, l2) grid.
+ * K <= 8. */
+int ps_xi(ps_ctx *ctx, int product, int parity, const double *const *W, int K, int64_t nW, int lmin, int lmax,
+          int mode, double *const *Xi, int64_t ldx);
+
+/* Covariance block: the body of loop_cov<kind>! (src/covariance.jl:92-446).
+ * S[0..3], R[0..nr-1] and W[0..nw-1] follow the reference's argument order:
+ *   TTTT  S={TTip,TTjq,TTiq,TTjp} R={r_ip,r_jq,r_iq,r_jp} W1..W8
+ *   EEEE  S={EEip,EEjq,EEiq,EEjp} R={r_ip,r_jq,r_iq,r_jp} W1..W8
+ *   TTTE  S={TTip,TTjp,TEiq,TEjq} R={r_ip,r_jp}           W1..W4
+ *   TETE  S={TTip,EEjq,TEiq,TEjp} R={r_TT_ip,r_PP_jq}     W1..W5
+ *   TEEE, TEEE_PLANCK S={EEjq,EEjp,TEip,TEiq} R={r_EE_jq,r_EE_jp} W1..W4
+ *   TTEE  S={TEip,TEiq,TEjq,TEjp} R={}                    W1..W2
+ * S and R hold at least lmax+1 entries, each W holds nW.  C is symmetric. */
+int ps_coupledcov(ps_ctx *ctx, int kind, const double *const *S, const double *const *R, const double *const *W,
+                  int64_t nW, int lmin, int lmax, int mode, double *C, int64_t ldc);
+int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const double *const *dR,
+                         const double *const *dW, int64_t nW, int lmin, int lmax, int mode, double *dC, int64_t ldc);
+
+/* Instrumentation: device time of the last coupling kernel (CUDA events on the
+ * launching stream), number of kernels this context has launched, and a
+ * measured FMA-pipe peak (flop/s, FMA = 2 flops) of this GPU in FP64 (fp64=1)
+ * or FP32 (fp64=0). */
+double ps_last_kernel_ms(const ps_ctx *ctx);
+uint64_t ps_launch_count(const ps_ctx *ctx);
+int ps_probe_fma_peak(ps_ctx *ctx, int fp64, double *flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POWERSPECTRA_GPU_H */

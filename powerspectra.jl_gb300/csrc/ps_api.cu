@@ -1,0 +1,477 @@
+// ps_api.cu -- the C ABI (include/powerspectra_gpu.h): context, argument
+// checks, device buffers, host<->device copies and kernel dispatch.
+//
+// Every entry point validates its arguments on the host before any device
+// work, so a bad size or pointer is reported as PS_ERR_ARG and never reaches
+// a kernel.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ps_internal.cuh"
+
+// Largest lmax the kernels accept: the integer products in P(j) stay below 2^63
+// and every index stays in 32 bits.
+#define PS_MAX_LMAX 16383
+
+struct ps_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    char err[512] = {0};
+    // warp task list for the current (lmin, lmax)
+    int2* d_tasks = nullptr;
+    size_t tasks_cap = 0;
+    int ntasks = 0, task_lmin = -1, task_lmax = -1;
+    // padded windows, raw inputs, spectra, outputs (element counts)
+    double* d_win = nullptr;
+    size_t win_cap = 0;
+    double* d_raw = nullptr;
+    size_t raw_cap = 0;
+    double* d_spec = nullptr;
+    size_t spec_cap = 0;
+    double* d_out = nullptr;
+    size_t out_cap = 0;
+    double* d_probe = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    double last_ms = 0.0;
+    unsigned long long launches = 0;
+};
+
+static int set_err(ps_ctx* c, int code, const char* fmt, ...)
+{
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define PS_CUDA(ctx, call)                                                                                  \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess)                                                                              \
+            return set_err((ctx), e_ == cudaErrorMemoryAllocation ? PS_ERR_OOM : PS_ERR_CUDA, "%s: %s (%s:%d)", \
+                           #call, cudaGetErrorString(e_), __FILE__, __LINE__);                               \
+    } while (0)
+
+static int ensure(ps_ctx* c, double** p, size_t* cap, size_t need)
+{
+    if (need <= *cap) return PS_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, need * sizeof(double));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_err(c, PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", need * sizeof(double),
+                       cudaGetErrorString(e));
+    }
+    *cap = need;
+    return PS_OK;
+}
+
+static int ensure_tasks(ps_ctx* c, int lmin, int lmax)
+{
+    if (c->task_lmin == lmin && c->task_lmax == lmax && c->d_tasks) return PS_OK;
+    std::vector<int2> t;
+    t.reserve((size_t)(lmax - lmin + 1) * ((lmax - lmin) / 32 + 1));
+    for (int l1 = lmax; l1 >= lmin; --l1)  // heaviest rows (longest families) first
+        for (int l2 = l1; l2 <= lmax; l2 += 32) t.push_back(make_int2(l1, l2));
+    if (t.size() > c->tasks_cap) {
+        if (c->d_tasks) cudaFree(c->d_tasks);
+        c->d_tasks = nullptr;
+        c->tasks_cap = 0;
+        cudaError_t e = cudaMalloc((void**)&c->d_tasks, t.size() * sizeof(int2));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(c, PS_ERR_OOM, "cudaMalloc of the task list failed: %s", cudaGetErrorString(e));
+        }
+        c->tasks_cap = t.size();
+    }
+    PS_CUDA(c, cudaMemcpyAsync(c->d_tasks, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->ntasks = (int)t.size();
+    c->task_lmin = lmin;
+    c->task_lmax = lmax;
+    return PS_OK;
+}
+
+static int check_grid(ps_ctx* c, int lmin, int lmax, int64_t nW, int64_t ld)
+{
+    if (!c) return PS_ERR_ARG;
+    if (lmin < 0 || lmax < lmin) return set_err(c, PS_ERR_ARG, "need 0 <= lmin <= lmax (got %d, %d)", lmin, lmax);
+    if (lmax > PS_MAX_LMAX) return set_err(c, PS_ERR_ARG, "lmax %d exceeds the supported maximum %d", lmax, PS_MAX_LMAX);
+    if (nW < 1) return set_err(c, PS_ERR_ARG, "window length nW must be >= 1 (got %lld)", (long long)nW);
+    if (ld < (int64_t)(lmax - lmin + 1))
+        return set_err(c, PS_ERR_ARG, "leading dimension %lld < lmax - lmin + 1 = %d", (long long)ld, lmax - lmin + 1);
+    return PS_OK;
+}
+
+static int check_mode(ps_ctx* c, int mode)
+{
+    if (mode == PS_MODE_PLAIN_FP64) return PS_OK;
+    if (mode == PS_MODE_CHOSEN) return set_err(c, PS_ERR_UNSUPPORTED, "PS_MODE_CHOSEN is not built into this library");
+    return set_err(c, PS_ERR_ARG, "unknown mode %d", mode);
+}
+
+static void spin_window(int spin, int* product, int* parity)
+{
+    switch (spin) {
+    case PS_SPIN_00: *product = ps::PROD_00_00; *parity = ps::PAR_ALL; break;
+    case PS_SPIN_02: *product = ps::PROD_00_22; *parity = ps::PAR_EVEN; break;
+    case PS_SPIN_PP: *product = ps::PROD_22_22; *parity = ps::PAR_EVEN; break;
+    default: *product = ps::PROD_22_22; *parity = ps::PAR_ODD; break;
+    }
+}
+
+namespace ps {
+int cov_nwindows(int kind)
+{
+    static const int nw[7] = {8, 8, 4, 5, 4, 4, 2};
+    return (kind >= 0 && kind < 7) ? nw[kind] : -1;
+}
+int cov_nratios(int kind)
+{
+    static const int nr[7] = {4, 4, 2, 2, 2, 2, 0};
+    return (kind >= 0 && kind < 7) ? nr[kind] : -1;
+}
+// Family product and parity of window k of each covariance kind (src/covariance.jl:92-446).
+void cov_window_spec(int kind, int k, int* product, int* parity)
+{
+    switch (kind) {
+    case PS_COV_EEEE:
+    case PS_COV_TEEE_PLANCK: *product = PROD_22_22; *parity = PAR_EVEN; break;
+    case PS_COV_TEEE: *product = PROD_00_22; *parity = PAR_EVEN; break;
+    case PS_COV_TETE:
+        if (k == 1) { *product = PROD_00_00; *parity = PAR_ALL; }
+        else { *product = PROD_00_22; *parity = PAR_EVEN; }
+        break;
+    default: *product = PROD_00_00; *parity = PAR_ALL; break;
+    }
+}
+}  // namespace ps
+
+// Launch the coupling kernel with event timing on the context stream.
+static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode)
+{
+    (void)mode;
+    int st = ensure_tasks(c, p.lmin, p.lmax);
+    if (st) return st;
+    p.tasks = c->d_tasks;
+    p.ntasks = c->ntasks;
+    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    PS_CUDA(c, ps::launch_plain_fp64(p, c->stream));
+    c->launches++;
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->timed = true;
+    return PS_OK;
+}
+
+// Upload (if host) and pad K windows into ctx->d_win; fills p.win[k].wW.
+static int stage_windows(ps_ctx* c, ps::CouplingParams& p, const double* const* W, int K, int64_t nW, int lmax,
+                         bool host)
+{
+    int wlen = 2 * lmax + 2;
+    long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+    int st = ensure(c, &c->d_win, &c->win_cap, (size_t)K * wlen);
+    if (st) return st;
+    if (host) {
+        st = ensure(c, &c->d_raw, &c->raw_cap, (size_t)K * nuse);
+        if (st) return st;
+    }
+    for (int k = 0; k < K; ++k) {
+        if (!W[k]) return set_err(c, PS_ERR_ARG, "window %d is NULL", k);
+        const double* src = W[k];
+        if (host) {
+            PS_CUDA(c, cudaMemcpyAsync(c->d_raw + (size_t)k * nuse, W[k], nuse * sizeof(double),
+                                       cudaMemcpyHostToDevice, c->stream));
+            src = c->d_raw + (size_t)k * nuse;
+        }
+        PS_CUDA(c, ps::launch_pad_windows(c->d_win + (size_t)k * wlen, src, nuse, wlen, c->stream));
+        c->launches++;
+        p.win[k].wW = c->d_win + (size_t)k * wlen;
+    }
+    return PS_OK;
+}
+
+extern "C" {
+
+int ps_create(int device, ps_ctx** out)
+{
+    if (!out) return PS_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return PS_ERR_CUDA;
+    }
+    if (device < 0 || device >= n) return PS_ERR_ARG;
+    ps_ctx* c = new ps_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return PS_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return PS_OK;
+}
+
+void ps_destroy(ps_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_tasks);
+    cudaFree(c->d_win);
+    cudaFree(c->d_raw);
+    cudaFree(c->d_spec);
+    cudaFree(c->d_out);
+    cudaFree(c->d_probe);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+const char* ps_last_error(const ps_ctx* c) { return c ? c->err : "null context"; }
+
+int ps_set_stream(ps_ctx* c, void* s)
+{
+    if (!c) return PS_ERR_ARG;
+    c->stream = s ? (cudaStream_t)s : c->own_stream;
+    return PS_OK;
+}
+
+int ps_synchronize(ps_ctx* c)
+{
+    if (!c) return PS_ERR_ARG;
+    PS_CUDA(c, cudaSetDevice(c->device));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+double ps_last_kernel_ms(const ps_ctx* c)
+{
+    if (!c || !c->timed) return -1.0;
+    float ms = 0.f;
+    if (cudaEventSynchronize(c->ev1) != cudaSuccess || cudaEventElapsedTime(&ms, c->ev0, c->ev1) != cudaSuccess) {
+        cudaGetLastError();
+        return -1.0;
+    }
+    return (double)ms;
+}
+
+uint64_t ps_launch_count(const ps_ctx* c) { return c ? (uint64_t)c->launches : 0; }
+
+static int mcm_multi_impl(ps_ctx* c, unsigned cases, const double* const W[4], int64_t nW, int lmin, int lmax, int mode,
+                          double* const M[4], int64_t ldm, bool host)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldm);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    if (cases == 0 || (cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "cases mask 0x%x must select bits 0..3", cases);
+    if (!W || !M) return set_err(c, PS_ERR_ARG, "W and M arrays must not be NULL");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    ps::CouplingParams p;
+    memset(&p, 0, sizeof(p));
+    p.lmin = lmin;
+    p.lmax = lmax;
+    p.epilogue = ps::EPI_MCM;
+    const double* wsel[4];
+    int sel[4], K = 0;
+    for (int s = 0; s < 4; ++s) {
+        if (!(cases & (1u << s))) continue;
+        if (!W[s] || !M[s]) return set_err(c, PS_ERR_ARG, "spin case %d selected but its W or M pointer is NULL", s);
+        spin_window(s, &p.win[K].product, &p.win[K].parity);
+        wsel[K] = W[s];
+        sel[K] = s;
+        ++K;
+    }
+    p.nwin = K;
+    if ((st = stage_windows(c, p, wsel, K, nW, lmax, host))) return st;
+    const long long n = lmax - lmin + 1;
+    if (host) {
+        if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
+        for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
+        p.ldo = n;
+    } else {
+        for (int k = 0; k < K; ++k) p.out[k] = M[sel[k]];
+        p.ldo = ldm;
+    }
+    if ((st = run_coupling(c, p, mode))) return st;
+    if (host) {
+        for (int k = 0; k < K; ++k)
+            PS_CUDA(c, cudaMemcpy2DAsync(M[sel[k]], (size_t)ldm * sizeof(double), p.out[k], (size_t)n * sizeof(double),
+                                         (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return PS_OK;
+}
+
+int ps_mcm(ps_ctx* c, int spin, const double* W, int64_t nW, int lmin, int lmax, int mode, double* M, int64_t ldm)
+{
+    if (!c) return PS_ERR_ARG;
+    if (spin < 0 || spin > 3) return set_err(c, PS_ERR_ARG, "%d is not a valid spin case", spin);
+    const double* Ws[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* Ms[4] = {nullptr, nullptr, nullptr, nullptr};
+    Ws[spin] = W;
+    Ms[spin] = M;
+    return mcm_multi_impl(c, 1u << spin, Ws, nW, lmin, lmax, mode, Ms, ldm, true);
+}
+
+int ps_mcm_multi(ps_ctx* c, unsigned cases, const double* const W[4], int64_t nW, int lmin, int lmax, int mode,
+                 double* const M[4], int64_t ldm)
+{
+    return mcm_multi_impl(c, cases, W, nW, lmin, lmax, mode, M, ldm, true);
+}
+
+int ps_mcm_multi_device(ps_ctx* c, unsigned cases, const double* const dW[4], int64_t nW, int lmin, int lmax, int mode,
+                        double* const dM[4], int64_t ldm)
+{
+    return mcm_multi_impl(c, cases, dW, nW, lmin, lmax, mode, dM, ldm, false);
+}
+
+int ps_xi(ps_ctx* c, int product, int parity, const double* const* W, int K, int64_t nW, int lmin, int lmax, int mode,
+          double* const* Xi, int64_t ldx)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldx);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    if (product < 0 || product > 2 || parity < 0 || parity > 2)
+        return set_err(c, PS_ERR_ARG, "invalid product %d / parity %d", product, parity);
+    if (K < 1 || K > ps::kMaxWin) return set_err(c, PS_ERR_ARG, "K must be in 1..%d (got %d)", ps::kMaxWin, K);
+    if (!W || !Xi) return set_err(c, PS_ERR_ARG, "W and Xi arrays must not be NULL");
+    for (int k = 0; k < K; ++k)
+        if (!Xi[k]) return set_err(c, PS_ERR_ARG, "Xi[%d] is NULL", k);
+    PS_CUDA(c, cudaSetDevice(c->device));
+    ps::CouplingParams p;
+    memset(&p, 0, sizeof(p));
+    p.lmin = lmin;
+    p.lmax = lmax;
+    p.epilogue = ps::EPI_XI;
+    p.nwin = K;
+    for (int k = 0; k < K; ++k) {
+        p.win[k].product = product;
+        p.win[k].parity = parity;
+    }
+    if ((st = stage_windows(c, p, W, K, nW, lmax, true))) return st;
+    const long long n = lmax - lmin + 1;
+    if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
+    for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
+    p.ldo = n;
+    if ((st = run_coupling(c, p, mode))) return st;
+    for (int k = 0; k < K; ++k)
+        PS_CUDA(c, cudaMemcpy2DAsync(Xi[k], (size_t)ldx * sizeof(double), p.out[k], (size_t)n * sizeof(double),
+                                     (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* const* R, const double* const* W,
+                    int64_t nW, int lmin, int lmax, int mode, double* C, int64_t ldc, bool host)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldc);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    int K = ps::cov_nwindows(kind), NR = ps::cov_nratios(kind);
+    if (K < 0) return set_err(c, PS_ERR_ARG, "%d is not a covariance kind", kind);
+    if (!S || !W || !C || (NR > 0 && !R)) return set_err(c, PS_ERR_ARG, "S, R, W and C must not be NULL");
+    for (int i = 0; i < 4; ++i)
+        if (!S[i]) return set_err(c, PS_ERR_ARG, "spectrum S[%d] is NULL", i);
+    for (int i = 0; i < NR; ++i)
+        if (!R[i]) return set_err(c, PS_ERR_ARG, "noise ratio R[%d] is NULL", i);
+    PS_CUDA(c, cudaSetDevice(c->device));
+    ps::CouplingParams p;
+    memset(&p, 0, sizeof(p));
+    p.lmin = lmin;
+    p.lmax = lmax;
+    p.epilogue = ps::EPI_COV;
+    p.cov_kind = kind;
+    p.nwin = K;
+    for (int k = 0; k < K; ++k) ps::cov_window_spec(kind, k, &p.win[k].product, &p.win[k].parity);
+    if ((st = stage_windows(c, p, W, K, nW, lmax, host))) return st;
+    const size_t ns = (size_t)lmax + 1;
+    if (host) {
+        if ((st = ensure(c, &c->d_spec, &c->spec_cap, 8 * ns))) return st;
+        for (int i = 0; i < 4; ++i) {
+            PS_CUDA(c, cudaMemcpyAsync(c->d_spec + i * ns, S[i], ns * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+            p.S[i] = c->d_spec + i * ns;
+        }
+        for (int i = 0; i < NR; ++i) {
+            PS_CUDA(c, cudaMemcpyAsync(c->d_spec + (4 + i) * ns, R[i], ns * sizeof(double), cudaMemcpyHostToDevice,
+                                       c->stream));
+            p.R[i] = c->d_spec + (4 + i) * ns;
+        }
+    } else {
+        for (int i = 0; i < 4; ++i) p.S[i] = S[i];
+        for (int i = 0; i < NR; ++i) p.R[i] = R[i];
+    }
+    const long long n = lmax - lmin + 1;
+    if (host) {
+        if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)n * n))) return st;
+        p.out[0] = c->d_out;
+        p.ldo = n;
+    } else {
+        p.out[0] = C;
+        p.ldo = ldc;
+    }
+    if ((st = run_coupling(c, p, mode))) return st;
+    if (host) {
+        PS_CUDA(c, cudaMemcpy2DAsync(C, (size_t)ldc * sizeof(double), p.out[0], (size_t)n * sizeof(double),
+                                     (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return PS_OK;
+}
+
+int ps_coupledcov(ps_ctx* c, int kind, const double* const* S, const double* const* R, const double* const* W,
+                  int64_t nW, int lmin, int lmax, int mode, double* C, int64_t ldc)
+{
+    return cov_impl(c, kind, S, R, W, nW, lmin, lmax, mode, C, ldc, true);
+}
+
+int ps_coupledcov_device(ps_ctx* c, int kind, const double* const* dS, const double* const* dR,
+                         const double* const* dW, int64_t nW, int lmin, int lmax, int mode, double* dC, int64_t ldc)
+{
+    return cov_impl(c, kind, dS, dR, dW, nW, lmin, lmax, mode, dC, ldc, false);
+}
+
+int ps_probe_fma_peak(ps_ctx* c, int fp64, double* flops)
+{
+    if (!c || !flops) return PS_ERR_ARG;
+    PS_CUDA(c, cudaSetDevice(c->device));
+    int nsm = 0;
+    PS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    int blocks = nsm * 8;
+    size_t dummy = 0;
+    int st = ensure(c, &c->d_probe, &dummy, (size_t)blocks);
+    if (st) return st;
+    int iters = fp64 ? 4096 : 262144;
+    PS_CUDA(c, ps::launch_fma_probe(fp64, c->d_probe, blocks, 64, c->stream));  // warm-up
+    c->launches++;
+    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    PS_CUDA(c, ps::launch_fma_probe(fp64, c->d_probe, blocks, iters, c->stream));
+    c->launches++;
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    PS_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    PS_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    double fl = (double)blocks * 256.0 * (double)iters * 8.0 * 2.0;
+    *flops = fl / (ms * 1e-3);
+    c->timed = false;
+    cudaFree(c->d_probe);
+    c->d_probe = nullptr;
+    return PS_OK;
+}
+
+}  // extern "C"

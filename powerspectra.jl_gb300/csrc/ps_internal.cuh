@@ -1,0 +1,63 @@
+// ps_internal.cuh -- shared declarations of the powerspectra_gpu library.
+//
+// Data layout on the device (one context owns all of it, reused across calls):
+//   * windows:  K padded rows of length wlen = 2*lmax + 2 holding
+//               (2 l3 + 1) * W_k[l3] for l3 < nW and 0 beyond, so every family
+//               read (l3 <= l1 + l2 <= 2 lmax) stays in bounds without a branch.
+//   * tasks:    int2 (l1, l2_0) per warp, 32 consecutive l2 of one l1 row,
+//               sorted by decreasing l1 (the family length is 2 l1 + 1) so
+//               the heaviest warps start first.
+//   * outputs:  column-major (Julia) matrices, element (l1, l2) at
+//               (l1 - lmin) + (l2 - lmin) * ld.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/powerspectra_gpu.h"
+
+namespace ps {
+
+constexpr int kMaxWin = 8;       // windows per launch of the generic coupling kernel
+constexpr int kWarpsPerBlock = 4;
+constexpr double kInv4Pi = 0.079577471545947667884;  // 1 / (4 pi)
+
+// Family product a window is contracted with.
+enum Product : int { PROD_00_00 = 0, PROD_22_22 = 1, PROD_00_22 = 2 };
+// l3 parity filter relative to l1 + l2 + l3.
+enum Parity : int { PAR_ALL = 0, PAR_EVEN = 1, PAR_ODD = 2 };
+// What the kernel writes per pair.
+enum Epilogue : int { EPI_MCM = 0, EPI_XI = 1, EPI_COV = 2 };
+
+struct WinDesc {
+    const double* wW;  // padded (2 l3 + 1) W[l3], length >= 2 lmax + 1
+    int product;
+    int parity;
+};
+
+struct CouplingParams {
+    int lmin, lmax;
+    int nwin;
+    WinDesc win[kMaxWin];
+    const int2* tasks;
+    int ntasks;
+    int epilogue;
+    double* out[kMaxWin];  // EPI_MCM / EPI_XI: one matrix per window; EPI_COV: out[0]
+    long long ldo;
+    int cov_kind;
+    const double* S[4];  // covariance signal spectra (length >= lmax + 1), reference argument order
+    const double* R[4];  // covariance noise ratios
+};
+
+// Launchers (ps_plain_fp64.cu).
+cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
+cudaError_t launch_pad_windows(double* dst, const double* src, long long nW, int wlen, cudaStream_t s);
+cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cudaStream_t s);
+
+// Host-side covariance table (ps_api.cu).
+int cov_nwindows(int kind);
+int cov_nratios(int kind);
+void cov_window_spec(int kind, int k, int* product, int* parity);
+
+}  // namespace ps

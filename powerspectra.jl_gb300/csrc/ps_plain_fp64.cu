@@ -1,0 +1,315 @@
+// ps_plain_fp64.cu -- the plain FP64 coupling kernel.
+//
+// Replaces the per-pair work of inner_mcm00!/02!/++!/--! (src/modecoupling.jl:78-159)
+// and of loop_cov*! (src/covariance.jl:92-446): for every (l1 <= l2) pair the 3j
+// families (l1 l2 l3; 0 0 0) and (l1 l2 l3; -2 2 0) are generated in registers
+// and contracted with the windows on the fly.  No 3j value is ever stored.
+//
+// Mapping: one warp owns 32 consecutive l2 of one l1 row.  Every lane's family
+// has the same length 2 l1 + 1, so the lanes run in lockstep; lane i reads
+// l3 = (l2_0 + i) - l1 + t at step t, i.e. 32 consecutive window entries.
+//
+// Recurrence.  With m3 = 0 and c = m2 - m1 (0 for the 00 family, 4 for 22),
+// the Schulten-Gordon relation divided by j(j+1) reads
+//     a(j+1) f(j+1) + c (2j+1) f(j) + a(j) f(j-1) = 0,
+//     a(j)^2 = P(j) = (j^2 - (l1-l2)^2) ((l1+l2+1)^2 - j^2),
+// where a(jmin) = a(jmax+1) = 0 start and stop it.  The family is run forward
+// from jmin (f = 1) over l1 + 1 points and backward from jmax (f = 1) over l1
+// points, matched by least squares on the two points jm = jmin + l1, jm + 1,
+// normalised by sum (2 l3 + 1) f^2 = 1 and sign-fixed by sgn f(jmax) =
+// (-1)^(l1 - l2) (Luscombe & Luban, Phys. Rev. E 57, 7274 (1998)).  The 00
+// family shares a(j) with the 22 family: f00(j+2) = -a(j+1)/a(j+2) f00(j).
+//
+// Only the two normalisation sums and the window sums are kept per pair, so
+// normalisation, matching and sign are applied once at the end.
+#include "ps_internal.cuh"
+#include "ps_cov_epilogue.cuh"
+
+namespace ps {
+
+// P(j+1) at forward step t (j = jmin + t, jmin = d = l2 - l1), from exact integer factors:
+// (j+1-d)(j+1+d)(s-j-1)(s+j+1) = (t+1)(2d+t+1)(2l1-t)(2l2+t+2).
+__device__ __forceinline__ double fwd_P(int t, int d, int l1, int l2)
+{
+    long long u = (long long)(t + 1) * (long long)(2 * d + t + 1);
+    long long v = (long long)(2 * l1 - t) * (long long)(2 * l2 + t + 2);
+    return (double)(u * v);
+}
+
+// P(j) at backward step t (j = jmax - t): (2l1-t)(2l2-t)(1+t)(2l1+2l2+1-t).
+__device__ __forceinline__ double bwd_P(int t, int l1, int l2)
+{
+    long long u = (long long)(2 * l1 - t) * (long long)(2 * l2 - t);
+    long long v = (long long)(1 + t) * (long long)(2 * l1 + 2 * l2 + 1 - t);
+    return (double)(u * v);
+}
+
+struct Sums {
+    double acc[kMaxWin];
+    double n0, n2;
+};
+
+// Point with l1 + l2 + l3 even: every window except ODD-parity ones takes a term.
+template <bool N00, bool N22>
+__device__ __forceinline__ void acc_even(Sums& s, const CouplingParams& p, double g0, double g2, double w, int j)
+{
+    double x00 = g0 * g0, x22 = g2 * g2, x02 = g0 * g2;
+    if (N00) s.n0 = fma(w, x00, s.n0);
+    if (N22) s.n2 = fma(w, x22, s.n2);
+#pragma unroll
+    for (int k = 0; k < kMaxWin; ++k) {
+        if (k < p.nwin && p.win[k].parity != PAR_ODD) {
+            double ww = __ldg(p.win[k].wW + j);
+            double x = p.win[k].product == PROD_00_00 ? x00 : (p.win[k].product == PROD_22_22 ? x22 : x02);
+            s.acc[k] = fma(x, ww, s.acc[k]);
+        }
+    }
+}
+
+// Point with l1 + l2 + l3 odd: the 00 family vanishes, only 22^2 windows that
+// are not EVEN-only take a term.
+template <bool N22>
+__device__ __forceinline__ void acc_odd(Sums& s, const CouplingParams& p, double g2, double w, int j)
+{
+    if (!N22) return;
+    double x22 = g2 * g2;
+    s.n2 = fma(w, x22, s.n2);
+#pragma unroll
+    for (int k = 0; k < kMaxWin; ++k) {
+        if (k < p.nwin && p.win[k].product == PROD_22_22 && p.win[k].parity != PAR_EVEN) {
+            double ww = __ldg(p.win[k].wW + j);
+            s.acc[k] = fma(x22, ww, s.acc[k]);
+        }
+    }
+}
+
+template <bool N00, bool N22>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_fp64(const CouplingParams p)
+{
+    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (gw >= p.ntasks) return;  // warp-uniform
+    const int lane = threadIdx.x & 31;
+    const int2 task = p.tasks[gw];
+    const int l1 = task.x;
+    const int l2raw = task.y + lane;
+    const bool active = l2raw <= p.lmax;
+    const int l2 = active ? l2raw : p.lmax;
+    const int d = l2 - l1;
+    const int jmin = d, jmax = l1 + l2;
+    const int T = l1;
+    const bool fam22 = N22 && (l1 >= 2);
+
+    double Xi[kMaxWin];
+    if (T == 0) {
+        // single term l3 = l2 with f00^2 = 1/(2 l2 + 1); the 22 family is identically zero.
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) {
+            Xi[k] = 0.0;
+            if (k < p.nwin && p.win[k].product == PROD_00_00 && p.win[k].parity != PAR_ODD)
+                Xi[k] = __ldg(p.win[k].wW + l2) / (2.0 * l2 + 1.0) * kInv4Pi;
+        }
+    } else {
+        // ---------------- forward from jmin: points jmin .. jm ----------------
+        Sums F;
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) F.acc[k] = 0.0;
+        F.n0 = F.n2 = 0.0;
+        double w = 2.0 * jmin + 1.0;
+        int j = jmin;
+        double g2c = 1.0, g2p = 0.0, aj = 0.0, g0 = 1.0;
+        int t = 0;
+        for (; t + 1 <= T; t += 2) {
+            acc_even<N00, N22>(F, p, g0, g2c, w, j);
+            double P1 = fwd_P(t, d, l1, l2);
+            double P2 = fwd_P(t + 1, d, l1, l2);
+            if (N22) {
+                double r1 = rsqrt(P1), a1 = P1 * r1;
+                double g2n = -fma(4.0 * w, g2c, aj * g2p) * r1;
+                acc_odd<N22>(F, p, g2n, w + 2.0, j + 1);
+                double r2 = rsqrt(P2), a2 = P2 * r2;
+                double g2nn = -fma(4.0 * (w + 2.0), g2n, a1 * g2c) * r2;
+                if (N00) g0 = -(a1 * r2) * g0;
+                g2p = g2n;
+                g2c = g2nn;
+                aj = a2;
+            } else {
+                // 00 alone: a(j+1)/a(j+2) = P1 / sqrt(P1 P2)
+                g0 = -(P1 * rsqrt(P1 * P2)) * g0;
+            }
+            j += 2;
+            w += 4.0;
+        }
+        double gm0 = 0.0, gm1 = 0.0;  // 22 at jm, jm + 1
+        if (t == T) {                 // T even: last point jm is an even point
+            acc_even<N00, N22>(F, p, g0, g2c, w, j);
+            if (N22) {
+                double P1 = fwd_P(t, d, l1, l2);
+                gm0 = g2c;
+                gm1 = -fma(4.0 * w, g2c, aj * g2p) * rsqrt(P1);
+            }
+        } else if (N22) {  // T odd: the loop stopped at jm + 1
+            gm0 = g2p;
+            gm1 = g2c;
+        }
+        const double g0s = g0;  // 00 at its non-zero matching point (jm if T even, jm + 1 if T odd)
+
+        // ---------------- backward from jmax: points jmax .. jm + 1 ----------------
+        Sums B;
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) B.acc[k] = 0.0;
+        B.n0 = B.n2 = 0.0;
+        double hw = 2.0 * jmax + 1.0;
+        int jb = jmax;
+        double h2c = 1.0, h2n = 0.0, an = 0.0, h0 = 1.0;
+        int tb = 0;
+        for (; tb + 2 <= T; tb += 2) {
+            acc_even<N00, N22>(B, p, h0, h2c, hw, jb);
+            double P1 = bwd_P(tb, l1, l2);
+            double P2 = bwd_P(tb + 1, l1, l2);
+            if (N22) {
+                double r1 = rsqrt(P1), a1 = P1 * r1;
+                double h2m = -fma(4.0 * hw, h2c, an * h2n) * r1;
+                acc_odd<N22>(B, p, h2m, hw - 2.0, jb - 1);
+                double r2 = rsqrt(P2), a2 = P2 * r2;
+                double h2mm = -fma(4.0 * (hw - 2.0), h2m, a1 * h2c) * r2;
+                if (N00) h0 = -(a1 * r2) * h0;
+                h2n = h2m;
+                h2c = h2mm;
+                an = a2;
+            } else {
+                h0 = -(P1 * rsqrt(P1 * P2)) * h0;
+            }
+            jb -= 2;
+            hw -= 4.0;
+        }
+        double hm0 = 0.0, hm1 = 0.0;
+        if (tb < T) {  // T odd: one more even point at jm + 1
+            acc_even<N00, N22>(B, p, h0, h2c, hw, jb);
+            if (N22) {
+                double P1 = bwd_P(tb, l1, l2);
+                hm1 = h2c;
+                hm0 = -fma(4.0 * hw, h2c, an * h2n) * rsqrt(P1);
+            }
+        } else if (N22) {
+            hm0 = h2c;
+            hm1 = h2n;
+        }
+        const double h0s = h0;
+
+        // ---------------- match, normalise, sign ----------------
+        double lam0 = N00 ? g0s / h0s : 0.0;
+        double lam2 = 0.0;
+        if (fam22) lam2 = (gm0 * hm0 + gm1 * hm1) / (hm0 * hm0 + hm1 * hm1);
+        double N0 = fma(lam0 * lam0, B.n0, F.n0);
+        double N2 = fma(lam2 * lam2, B.n2, F.n2);
+        double inv0 = N00 ? kInv4Pi / N0 : 0.0;
+        double inv2 = fam22 ? kInv4Pi / N2 : 0.0;
+        double inv02 = 0.0;
+        if (N00 && fam22) {
+            double sg = ((lam0 < 0.0) != (lam2 < 0.0)) ? -1.0 : 1.0;
+            inv02 = sg * kInv4Pi * rsqrt(N0 * N2);
+        }
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) {
+            Xi[k] = 0.0;
+            if (k < p.nwin) {
+                int pr = p.win[k].product;
+                if (pr != PROD_00_00 && !fam22)
+                    Xi[k] = 0.0;  // |m| = 2 > l1: the 22 family is identically zero
+                else if (pr == PROD_00_00)
+                    Xi[k] = fma(lam0 * lam0, B.acc[k], F.acc[k]) * inv0;
+                else if (pr == PROD_22_22)
+                    Xi[k] = fma(lam2 * lam2, B.acc[k], F.acc[k]) * inv2;
+                else
+                    Xi[k] = fma(lam0 * lam2, B.acc[k], F.acc[k]) * inv02;
+            }
+        }
+    }
+
+    if (!active) return;
+    const long long r1 = l1 - p.lmin, r2 = l2 - p.lmin;
+    if (p.epilogue == EPI_MCM) {
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) {
+            if (k < p.nwin) {
+                p.out[k][r1 + r2 * p.ldo] = (2.0 * l2 + 1.0) * Xi[k];
+                p.out[k][r2 + r1 * p.ldo] = (2.0 * l1 + 1.0) * Xi[k];
+            }
+        }
+    } else if (p.epilogue == EPI_XI) {
+#pragma unroll
+        for (int k = 0; k < kMaxWin; ++k) {
+            if (k < p.nwin) {
+                p.out[k][r1 + r2 * p.ldo] = Xi[k];
+                p.out[k][r2 + r1 * p.ldo] = Xi[k];
+            }
+        }
+    } else {
+        double c = cov_combine(p.cov_kind, p.S, p.R, Xi, l1, l2);
+        p.out[0][r1 + r2 * p.ldo] = c;
+        p.out[0][r2 + r1 * p.ldo] = c;
+    }
+}
+
+cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s)
+{
+    bool n00 = false, n22 = false;
+    for (int k = 0; k < p.nwin; ++k) {
+        if (p.win[k].product != PROD_22_22) n00 = true;
+        if (p.win[k].product != PROD_00_00) n22 = true;
+    }
+    const int threads = kWarpsPerBlock * 32;
+    const unsigned blocks = (unsigned)((p.ntasks + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    if (blocks == 0) return cudaSuccess;
+    if (n00 && n22)
+        k_coupling_fp64<true, true><<<blocks, threads, 0, s>>>(p);
+    else if (n22)
+        k_coupling_fp64<false, true><<<blocks, threads, 0, s>>>(p);
+    else
+        k_coupling_fp64<true, false><<<blocks, threads, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// window padding: dst[j] = (2j+1) src[j] for j < nW, 0 for nW <= j < wlen
+__global__ void k_pad_windows(double* __restrict__ dst, const double* __restrict__ src, long long nW, int wlen)
+{
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < wlen; j += gridDim.x * blockDim.x)
+        dst[j] = (j < nW) ? (2.0 * j + 1.0) * src[j] : 0.0;
+}
+
+cudaError_t launch_pad_windows(double* dst, const double* src, long long nW, int wlen, cudaStream_t s)
+{
+    int threads = 256;
+    int blocks = (wlen + threads - 1) / threads;
+    if (blocks > 1024) blocks = 1024;
+    k_pad_windows<<<blocks, threads, 0, s>>>(dst, src, nW, wlen);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FMA-pipe probe: 8 independent FMA chains per thread, FMA counted as 2 flops.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_probe(T* sink, int iters)
+{
+    T a0 = (T)threadIdx.x * (T)1e-3, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+    T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+    const T b = (T)0.999999, c = (T)1e-6;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    T r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (r == (T)-12345.0) sink[blockIdx.x] = r;  // keeps the chains alive; never true
+}
+
+cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cudaStream_t s)
+{
+    if (fp64)
+        k_fma_probe<double><<<blocks, 256, 0, s>>>(sink, iters);
+    else
+        k_fma_probe<float><<<blocks, 256, 0, s>>>((float*)sink, iters);
+    return cudaGetLastError();
+}
+
+}  // namespace ps

@@ -1,0 +1,240 @@
+"""ctypes binding of libpowerspectra_gpu.so (the C ABI in include/powerspectra_gpu.h).
+
+The library is built in-tree by powerspectra.jl_gb300/build.py.  There is no
+CPU fallback: if the shared library is missing or no CUDA device is visible,
+every call raises.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG_ROOT, "lib", "libpowerspectra_gpu.so")
+
+PS_OK, PS_ERR_ARG, PS_ERR_CUDA, PS_ERR_OOM, PS_ERR_TIMEOUT, PS_ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5
+PS_SPIN_00, PS_SPIN_02, PS_SPIN_PP, PS_SPIN_MM = 0, 1, 2, 3
+PS_MODE_PLAIN_FP64, PS_MODE_CHOSEN = 0, 1
+PS_PROD_00_00, PS_PROD_22_22, PS_PROD_00_22 = 0, 1, 2
+PS_PARITY_ALL, PS_PARITY_EVEN, PS_PARITY_ODD = 0, 1, 2
+COV_KINDS = {"TTTT": 0, "EEEE": 1, "TTTE": 2, "TETE": 3, "TEEE": 4, "TEEE_PLANCK": 5, "TTEE": 6}
+COV_NWINDOWS = {0: 8, 1: 8, 2: 4, 3: 5, 4: 4, 5: 4, 6: 2}
+COV_NRATIOS = {0: 4, 1: 4, 2: 2, 3: 2, 4: 2, 5: 2, 6: 0}
+MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_MODE_CHOSEN}
+
+# every symbol declared in include/powerspectra_gpu.h
+EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
+           "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_last_kernel_ms",
+           "ps_launch_count", "ps_probe_fma_peak")
+
+
+class PowerSpectraGPUError(RuntimeError):
+    """A non-zero status from the C ABI; `.code` holds it."""
+
+    def __init__(self, code, msg):
+        super().__init__("powerspectra_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class PowerSpectraArgumentError(PowerSpectraGPUError, ValueError):
+    """PS_ERR_ARG: the reference raises ArgumentError / fails an @assert here."""
+
+
+_lib = None
+_lock = threading.RLock()
+_DP = ctypes.POINTER(ctypes.c_double)
+_DPP = ctypes.POINTER(_DP)
+
+
+def load(path=None):
+    """Load the shared library (no build, no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError("libpowerspectra_gpu.so not found at %s: run powerspectra.jl_gb300/build.py "
+                               "(there is no CPU fallback)" % p)
+        lib = ctypes.CDLL(p)
+        vp, ci, i64, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64
+        lib.ps_create.argtypes = [ci, ctypes.POINTER(vp)]
+        lib.ps_create.restype = ci
+        lib.ps_destroy.argtypes = [vp]
+        lib.ps_destroy.restype = None
+        lib.ps_last_error.argtypes = [vp]
+        lib.ps_last_error.restype = ctypes.c_char_p
+        lib.ps_set_stream.argtypes = [vp, vp]
+        lib.ps_set_stream.restype = ci
+        lib.ps_synchronize.argtypes = [vp]
+        lib.ps_synchronize.restype = ci
+        lib.ps_mcm.argtypes = [vp, ci, _DP, i64, ci, ci, ci, _DP, i64]
+        lib.ps_mcm.restype = ci
+        lib.ps_mcm_multi.argtypes = [vp, ctypes.c_uint, _DPP, i64, ci, ci, ci, _DPP, i64]
+        lib.ps_mcm_multi.restype = ci
+        lib.ps_mcm_multi_device.argtypes = [vp, ctypes.c_uint, _DPP, i64, ci, ci, ci, _DPP, i64]
+        lib.ps_mcm_multi_device.restype = ci
+        lib.ps_xi.argtypes = [vp, ci, ci, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
+        lib.ps_xi.restype = ci
+        lib.ps_coupledcov.argtypes = [vp, ci, _DPP, _DPP, _DPP, i64, ci, ci, ci, _DP, i64]
+        lib.ps_coupledcov.restype = ci
+        lib.ps_coupledcov_device.argtypes = [vp, ci, _DPP, _DPP, _DPP, i64, ci, ci, ci, _DP, i64]
+        lib.ps_coupledcov_device.restype = ci
+        lib.ps_last_kernel_ms.argtypes = [vp]
+        lib.ps_last_kernel_ms.restype = ctypes.c_double
+        lib.ps_launch_count.argtypes = [vp]
+        lib.ps_launch_count.restype = u64
+        lib.ps_probe_fma_peak.argtypes = [vp, ci, ctypes.POINTER(ctypes.c_double)]
+        lib.ps_probe_fma_peak.restype = ci
+        _lib = lib
+        return lib
+
+
+def dptr(a):
+    """double* of a numpy array (host) or of an int device address."""
+    if isinstance(a, int):
+        return ctypes.cast(ctypes.c_void_p(a), _DP)
+    if a is None:
+        return _DP()
+    return a.ctypes.data_as(_DP)
+
+
+def dptr_array(items):
+    arr = (_DP * max(len(items), 1))()
+    for i, a in enumerate(items):
+        arr[i] = dptr(a)
+    return arr
+
+
+def mode_code(mode):
+    if isinstance(mode, int):
+        return mode
+    try:
+        return MODES[mode]
+    except KeyError:
+        raise ValueError("unknown mode %r (use 'plain' or 'chosen')" % (mode,))
+
+
+class Context:
+    """Owns one ps_ctx (device buffers, stream, error message)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        st = self.lib.ps_create(int(device), ctypes.byref(h))
+        if st != PS_OK:
+            raise PowerSpectraGPUError(st, "ps_create(%d) failed: no usable CUDA device" % device)
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.ps_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st):
+        if st != PS_OK:
+            msg = self.lib.ps_last_error(self.handle).decode(errors="replace")
+            cls = PowerSpectraArgumentError if st == PS_ERR_ARG else PowerSpectraGPUError
+            raise cls(st, msg)
+
+    def set_stream(self, stream_handle):
+        self.check(self.lib.ps_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)))
+
+    def synchronize(self):
+        self.check(self.lib.ps_synchronize(self.handle))
+
+    def last_kernel_ms(self):
+        return self.lib.ps_last_kernel_ms(self.handle)
+
+    def launch_count(self):
+        return int(self.lib.ps_launch_count(self.handle))
+
+    def fma_peak(self, fp64=True):
+        out = ctypes.c_double(0.0)
+        self.check(self.lib.ps_probe_fma_peak(self.handle, 1 if fp64 else 0, ctypes.byref(out)))
+        return out.value
+
+    # ---- raw entry points (host numpy arrays) ----
+    def mcm(self, spin, W, lmin, lmax, mode="plain", out=None):
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        n = lmax - lmin + 1
+        M = np.empty((n, n), dtype=np.float64, order="F") if out is None else out
+        self.check(self.lib.ps_mcm(self.handle, int(spin), dptr(W), len(W), lmin, lmax, mode_code(mode), dptr(M),
+                                   M.shape[0]))
+        return M
+
+    def mcm_multi(self, Ws, lmin, lmax, mode="plain", outs=None):
+        """Ws: dict spin -> W.  Returns dict spin -> matrix (Fortran order)."""
+        cases = 0
+        wl, ml = [None] * 4, [None] * 4
+        n = lmax - lmin + 1
+        nW = None
+        keep = []
+        for s, W in Ws.items():
+            W = np.ascontiguousarray(W, dtype=np.float64)
+            keep.append(W)
+            nW = len(W) if nW is None else min(nW, len(W))
+            cases |= 1 << s
+            wl[s] = W
+            ml[s] = (outs[s] if outs is not None else np.empty((n, n), dtype=np.float64, order="F"))
+        self.check(self.lib.ps_mcm_multi(self.handle, cases, dptr_array(wl), nW, lmin, lmax, mode_code(mode),
+                                         dptr_array(ml), n))
+        return {s: ml[s] for s in Ws}
+
+    def mcm_multi_device(self, dWs, nW, lmin, lmax, dMs, ldm, mode="plain"):
+        """Device-pointer variant: dWs / dMs map spin -> device address (int)."""
+        cases = 0
+        wl, ml = [None] * 4, [None] * 4
+        for s, p in dWs.items():
+            cases |= 1 << s
+            wl[s] = int(p)
+            ml[s] = int(dMs[s])
+        self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
+                                                mode_code(mode), dptr_array(ml), int(ldm)))
+
+    def xi(self, product, parity, Ws, lmin, lmax, mode="plain"):
+        Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]
+        n = lmax - lmin + 1
+        outs = [np.empty((n, n), dtype=np.float64, order="F") for _ in Ws]
+        nW = min(len(w) for w in Ws)
+        self.check(self.lib.ps_xi(self.handle, int(product), int(parity), dptr_array(Ws), len(Ws), nW, lmin, lmax,
+                                  mode_code(mode), dptr_array(outs), n))
+        return outs
+
+    def coupledcov(self, kind, S, R, Ws, lmin, lmax, mode="plain", out=None):
+        k = COV_KINDS[kind] if isinstance(kind, str) else int(kind)
+        S = [np.ascontiguousarray(s, dtype=np.float64) for s in S]
+        R = [np.ascontiguousarray(s, dtype=np.float64) for s in R]
+        Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]
+        if k in COV_NWINDOWS and (len(Ws) != COV_NWINDOWS[k] or len(R) != COV_NRATIOS[k] or len(S) != 4):
+            raise PowerSpectraArgumentError(PS_ERR_ARG, "kind %d takes 4 spectra, %d ratios and %d windows"
+                                            % (k, COV_NRATIOS[k], COV_NWINDOWS[k]))
+        for a in S + R:
+            if len(a) < lmax + 1:
+                raise PowerSpectraArgumentError(PS_ERR_ARG, "spectra and noise ratios need lmax+1 entries")
+        n = lmax - lmin + 1
+        C = np.empty((n, n), dtype=np.float64, order="F") if out is None else out
+        nW = min(len(w) for w in Ws) if Ws else 1
+        self.check(self.lib.ps_coupledcov(self.handle, k, dptr_array(S), dptr_array(R), dptr_array(Ws), nW, lmin,
+                                          lmax, mode_code(mode), dptr(C), C.shape[0]))
+        return C
+
+
+_default_ctx = None
+
+
+def default_context():
+    """Process-wide context on device 0 (created on first use)."""
+    global _default_ctx
+    with _lock:
+        if _default_ctx is None:
+            _default_ctx = Context(int(os.environ.get("PS_GPU_DEVICE", "0")))
+        return _default_ctx

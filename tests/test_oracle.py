@@ -1,0 +1,139 @@
+"""CPU checks of the oracle (test infrastructure) against golden vectors.
+
+Pins: (1) arbitrary-precision 3j values, (2) the reference test suite's
+NaMaster diagonals (test/data/mcm_{TT,EE,TE}_diag.txt), (3) analytic known
+answers, (4) the committed oracle fixtures.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as o
+
+
+def test_families_vs_exact():
+    rows = json.load(open(os.path.join(GOLDEN, "w3j_exact.json")))["rows"]
+    cache = {}
+    worst = 0.0
+    for l1, l2, l3, m1, m2, sval in rows:
+        key = (l1, l2, m1, m2)
+        if key not in cache:
+            cache[key] = o.w3j_family(l1, l2, m1, m2)
+        jmin, f = cache[key]
+        ex = float(sval)
+        got = f[l3 - jmin] if 0 <= l3 - jmin < len(f) else 0.0
+        # typical family amplitude: sum_l3 (2 l3 + 1) f^2 = 1 over the family
+        amp = 1.0 / math.sqrt(max((l1 + l2 + 1) ** 2 - jmin ** 2, 1))
+        err = abs(got - ex)
+        assert err <= 1e-12 * abs(ex) + 1e-12 * amp, (l1, l2, l3, m1, m2, got, ex)
+        worst = max(worst, err / max(abs(ex), amp))
+    assert worst < 1e-12
+
+
+@pytest.mark.parametrize("l1,l2", [(0, 0), (1, 1), (2, 5), (17, 4), (300, 299), (1000, 3), (2500, 2400), (8191, 8190)])
+@pytest.mark.parametrize("m", [(0, 0), (-2, 2)])
+def test_family_orthonormal(l1, l2, m):
+    jmin, f = o.w3j_family(l1, l2, *m)
+    if abs(m[0]) > min(l1, l2):
+        assert not np.any(f)
+        return
+    j = np.arange(jmin, jmin + len(f))
+    assert abs(np.sum((2 * j + 1) * f * f) - 1.0) < 1e-13
+    # Condon-Shortley sign at l3 = l1 + l2
+    assert np.sign(f[-1]) == (-1) ** (l1 - l2)
+
+
+def _namaster_design(ells, nW):
+    """Rows: l = 2..766 diagonal entries; columns: W at even l3 (odd l3 never reach a diagonal)."""
+    evens = np.arange(0, nW, 2)
+    A = {k: np.zeros((len(ells), len(evens))) for k in ("TT", "EE", "TE")}
+    for r, l in enumerate(ells):
+        _, f0 = o.w3j_family(l, l, 0, 0)
+        _, f2 = o.w3j_family(l, l, -2, 2)
+        top = min(2 * l, nW - 1)
+        l3 = evens[evens <= top]
+        w = (2 * l + 1) * (2 * l3 + 1) / (4 * math.pi)
+        A["TT"][r, :len(l3)] = w * f0[l3] ** 2
+        A["EE"][r, :len(l3)] = w * f2[l3] ** 2
+        A["TE"][r, :len(l3)] = w * f0[l3] * f2[l3]
+    return A
+
+
+@pytest.mark.parametrize("fit,held", [(("TT", "EE"), "TE"), (("TT", "TE"), "EE"), (("EE", "TE"), "TT")])
+def test_namaster_diagonals(fit, held):
+    """The reference's NaMaster golden diagonals (TT, ++, TE of one mask, lmax 767, l3 <= 767)
+    depend only on W at even l3 <= 767: 384 unknowns, 765 equations per spin case.  Fitting W
+    on two spin cases and predicting the third checks the oracle's 00 and 22 families, the
+    TE sign, the (2l3+1)/4pi weights and the parity rules against the reference's vectors."""
+    gold = dict(np.load(os.path.join(GOLDEN, "namaster_diag.npz")))
+    ells = np.arange(2, 767)
+    A = _namaster_design(ells, 768)
+    Afit = np.vstack([A[k] for k in fit])
+    bfit = np.concatenate([gold[k] for k in fit])
+    W, *_ = np.linalg.lstsq(Afit, bfit, rcond=None)
+    for k in fit:
+        assert np.max(np.abs(A[k] @ W / gold[k] - 1)) < 1e-12
+    pred = A[held] @ W
+    assert np.max(np.abs(pred / gold[held] - 1)) < 1e-11
+
+
+def test_full_sky_identity():
+    L = 48
+    W = np.zeros(2 * L + 1)
+    W[0] = 4 * math.pi
+    I = np.eye(L + 1)
+    assert np.allclose(o.inner_mcm(0, W, 0, L), I, atol=1e-14)
+    for spin, want in ((1, I), (2, I), (3, 0 * I)):
+        M = o.inner_mcm(spin, W, 0, L)
+        assert np.allclose(M[2:, 2:], want[2:, 2:], atol=1e-14)
+        assert not np.any(M[:2, :]) and not np.any(M[:, :2])  # l < 2 rows of spin-2 cases are defined as 0
+
+
+def test_row_column_weights():
+    L = 30
+    W = np.abs(np.random.default_rng(0).standard_normal(2 * L + 1))
+    for spin in range(4):
+        M = o.inner_mcm(spin, W, 0, L)
+        l = np.arange(L + 1)
+        # M[l1,l2] = (2l2+1) Xi, M[l2,l1] = (2l1+1) Xi  (src/modecoupling.jl:90-91)
+        assert np.allclose(M / (2 * l[None, :] + 1), (M / (2 * l[None, :] + 1)).T, rtol=1e-14, atol=0)
+
+
+def test_oracle_fixture_stable():
+    g = dict(np.load(os.path.join(GOLDEN, "oracle_small.npz")))
+    L = 40
+    for nWname in ("2L1", "L1"):
+        for spin in range(4):
+            M = o.inner_mcm(spin, g["W_" + nWname], 0, L)
+            np.testing.assert_allclose(M, g["M%d_%s" % (spin, nWname)], rtol=1e-13, atol=1e-300)
+    np.testing.assert_allclose(o.inner_mcm(0, g["W_2L1"], 5, L), g["M0_lmin5"], rtol=1e-13, atol=1e-300)
+    S = [g["cov_S%d" % i] for i in range(4)]
+    R = [g["cov_R%d" % i] for i in range(4)]
+    Ws = [g["cov_W%d" % k] for k in range(8)]
+    for name in o.COV_KINDS:
+        C = o.loop_cov(name, S, R[:o.COV_NRATIOS[name]], Ws[:o.COV_NWINDOWS[name]], 0, 32)
+        np.testing.assert_allclose(C, g["cov_" + name], rtol=1e-13, atol=1e-300)
+
+
+def test_lmin_submatrix():
+    """lmin only crops the grid: the families do not depend on it."""
+    g = dict(np.load(os.path.join(GOLDEN, "oracle_small.npz")))
+    np.testing.assert_allclose(g["M0_lmin5"], g["M0_2L1"][5:, 5:], rtol=1e-15, atol=0)
+
+
+def test_covariance_symmetric_and_reference_formula():
+    """TTEE at one pair written out by hand from src/covariance.jl:438-441."""
+    g = dict(np.load(os.path.join(GOLDEN, "oracle_small.npz")))
+    S = [g["cov_S%d" % i] for i in range(4)]
+    Ws = [g["cov_W%d" % k] for k in range(2)]
+    C = o.loop_cov("TTEE", S, [], Ws, 0, 32)
+    assert np.array_equal(C, C.T)
+    X = [o.xi(0, 0, w, 0, 32) for w in Ws]
+    a, b = 7, 19
+    TEip, TEiq, TEjq, TEjp = S
+    want = ((TEip[a] * TEjq[b] + TEjq[a] * TEip[b]) * X[0][a, b] + (TEiq[a] * TEjp[b] + TEjp[a] * TEiq[b]) * X[1][a, b]) / 2
+    assert abs(C[a, b] - want) <= 1e-14 * abs(want)
