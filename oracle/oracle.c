@@ -117,7 +117,8 @@ int or_w3j_family(int l1, int l2, int m1, int m2, double *out, int *jmin_out)
 /* Xi projectors, src/modecoupling.jl:3-66.  parity: 0 all l3 (Xi_TT), 1 even
  * l1+l2+l3 (Xi_EE, Xi_TE), 2 odd l1+l2+l3 (Xi_EB).  x holds the family product
  * over [jmin, jmax]; W is 0-indexed with length nW. */
-static double xi_sum(const double *W, long nW, const double *x, int jmin, int jmax, int l1, int l2, int parity)
+static double xi_sum(const double *W, long nW, const double *x, int jmin, int jmax, int l1, int l2, int parity,
+                     int absmode)
 {
     long js = jmin > 0 ? jmin : 0;
     long je = (long)jmax < nW - 1 ? (long)jmax : nW - 1;
@@ -125,7 +126,10 @@ static double xi_sum(const double *W, long nW, const double *x, int jmin, int jm
     if (parity == 2 && !((l1 + l2 + js) & 1)) js++;
     long step = parity ? 2 : 1;
     double s = 0.0;
-    for (long j = js; j <= je; j += step) s += (2.0 * j + 1.0) * x[j - jmin] * W[j];
+    if (absmode)
+        for (long j = js; j <= je; j += step) s += (2.0 * j + 1.0) * fabs(x[j - jmin]) * fabs(W[j]);
+    else
+        for (long j = js; j <= je; j += step) s += (2.0 * j + 1.0) * x[j - jmin] * W[j];
     return s / (4.0 * M_PI);
 }
 
@@ -151,8 +155,8 @@ int or_max_threads(void)
 /* Row list helper: rows == NULL means every l1 in [lmin, lmax]. */
 static inline int row_at(const int *rows, int i, int lmin) { return rows ? rows[i] : lmin + i; }
 
-int or_inner_mcm(int spin, const double *W, long nW, int lmin, int lmax, double *M, long ldm,
-                 const int *rows, int nrows, int nthreads)
+static int inner_mcm_impl(int spin, const double *W, long nW, int lmin, int lmax, double *M, long ldm,
+                          const int *rows, int nrows, int nthreads, int absmode)
 {
     if (spin < 0 || spin > 3 || lmin < 0 || lmax < lmin || nW < 1 || ldm < lmax - lmin + 1) return 1;
     int nr = rows ? nrows : lmax - lmin + 1;
@@ -177,17 +181,17 @@ int or_inner_mcm(int spin, const double *W, long nW, int lmin, int lmax, double 
                 if (spin == 0) { /* inner_mcm00!, src/modecoupling.jl:78-95 */
                     int n = or_w3j_family(l1, l2, 0, 0, b0, &jmin);
                     for (int k = 0; k < n; ++k) b0[k] = b0[k] * b0[k];
-                    xi = xi_sum(W, nW, b0, jmin, jmax, l1, l2, 0);
+                    xi = xi_sum(W, nW, b0, jmin, jmax, l1, l2, 0, absmode);
                 } else if (spin == 1) { /* inner_mcm02!, src/modecoupling.jl:99-119 */
                     int n = or_w3j_family(l1, l2, 0, 0, b0, &jmin);
                     int jmin2;
                     or_w3j_family(l1, l2, -2, 2, b2, &jmin2);
                     for (int k = 0; k < n; ++k) b0[k] *= b2[k];
-                    xi = xi_sum(W, nW, b0, jmin, jmax, l1, l2, 1);
+                    xi = xi_sum(W, nW, b0, jmin, jmax, l1, l2, 1, absmode);
                 } else { /* inner_mcm++! / --!, src/modecoupling.jl:123-159 */
                     int n = or_w3j_family(l1, l2, -2, 2, b2, &jmin);
                     for (int k = 0; k < n; ++k) b2[k] = b2[k] * b2[k];
-                    xi = xi_sum(W, nW, b2, jmin, jmax, l1, l2, spin == 2 ? 1 : 2);
+                    xi = xi_sum(W, nW, b2, jmin, jmax, l1, l2, spin == 2 ? 1 : 2, absmode);
                 }
                 M[(long)(l1 - lmin) + (long)(l2 - lmin) * ldm] = (2.0 * l2 + 1.0) * xi;
                 M[(long)(l2 - lmin) + (long)(l1 - lmin) * ldm] = (2.0 * l1 + 1.0) * xi;
@@ -197,6 +201,18 @@ int or_inner_mcm(int spin, const double *W, long nW, int lmin, int lmax, double 
         free(b2);
     }
     return err;
+}
+
+int or_inner_mcm(int spin, const double *W, long nW, int lmin, int lmax, double *M, long ldm,
+                 const int *rows, int nrows, int nthreads)
+{
+    return inner_mcm_impl(spin, W, nW, lmin, lmax, M, ldm, rows, nrows, nthreads, 0);
+}
+
+int or_inner_mcm_abs(int spin, const double *W, long nW, int lmin, int lmax, double *M, long ldm,
+                     const int *rows, int nrows, int nthreads)
+{
+    return inner_mcm_impl(spin, W, nW, lmin, lmax, M, ldm, rows, nrows, nthreads, 1);
 }
 
 int or_xi(int product, int parity, const double *W, long nW, int lmin, int lmax, double *X, long ldx, int nthreads)
@@ -230,7 +246,7 @@ int or_xi(int product, int parity, const double *W, long nW, int lmin, int lmax,
                     or_w3j_family(l1, l2, -2, 2, b2, &jmin2);
                     for (int k = 0; k < n; ++k) b0[k] *= b2[k];
                 }
-                double xi = xi_sum(W, nW, b0, jmin, l1 + l2, l1, l2, parity);
+                double xi = xi_sum(W, nW, b0, jmin, l1 + l2, l1, l2, parity, 0);
                 X[(long)(l1 - lmin) + (long)(l2 - lmin) * ldx] = xi;
                 X[(long)(l2 - lmin) + (long)(l1 - lmin) * ldx] = xi;
             }
@@ -257,8 +273,9 @@ int or_cov_nwindows(int kind)
  *   TEEE  S={EEjq,EEjp,TEip,TEiq} R={r_EE_jq,r_EE_jp}     W1..W4  (00x22, Xi_EE)
  *   TEEE_PLANCK  same arguments                             W1..W4  (22^2, Xi_EE)
  *   TTEE  S={TEip,TEiq,TEjq,TEjp} R={}                    W1..W2  (00^2, Xi_TT)  */
-int or_loop_cov(int kind, const double *const *S, const double *const *R, const double *const *Wk, long nW, int lmin,
-                int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads)
+
+static int loop_cov_impl(int kind, const double *const *S, const double *const *R, const double *const *Wk, long nW,
+                         int lmin, int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads, int absmode)
 {
     int K = or_cov_nwindows(kind);
     if (K < 0 || lmin < 0 || lmax < lmin || ldc < lmax - lmin + 1) return 1;
@@ -285,26 +302,26 @@ int or_loop_cov(int kind, const double *const *S, const double *const *R, const 
                 if (kind == 0 || kind == 2 || kind == 6) { /* one 00 family, squared */
                     int n = or_w3j_family(a, b, 0, 0, b0, &jmin);
                     for (int k = 0; k < n; ++k) b0[k] = b0[k] * b0[k];
-                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b0, jmin, jmax, a, b, 0);
+                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b0, jmin, jmax, a, b, 0, absmode);
                 } else if (kind == 1 || kind == 5) { /* one 22 family, squared, even parity */
                     int n = or_w3j_family(a, b, -2, 2, b0, &jmin);
                     for (int k = 0; k < n; ++k) b0[k] = b0[k] * b0[k];
-                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b0, jmin, jmax, a, b, 1);
+                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b0, jmin, jmax, a, b, 1, absmode);
                 } else if (kind == 4) { /* 00 x 22, even parity */
                     int n = or_w3j_family(a, b, 0, 0, b0, &jmin);
                     or_w3j_family(a, b, -2, 2, b2, &jmin2);
                     for (int k = 0; k < n; ++k) b2[k] *= b0[k];
-                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b2, jmin, jmax, a, b, 1);
+                    for (int k = 0; k < K; ++k) X[k] = xi_sum(Wk[k], nW, b2, jmin, jmax, a, b, 1, absmode);
                 } else { /* TETE: 00x22 for W1,3,4,5 (Xi_TE) and 00^2 for W2 (Xi_TT) */
                     int n = or_w3j_family(a, b, 0, 0, b0, &jmin);
                     or_w3j_family(a, b, -2, 2, b2, &jmin2);
                     for (int k = 0; k < n; ++k) b2[k] *= b0[k];
                     for (int k = 0; k < n; ++k) b0[k] *= b0[k];
-                    X[0] = xi_sum(Wk[0], nW, b2, jmin, jmax, a, b, 1);
-                    X[1] = xi_sum(Wk[1], nW, b0, jmin, jmax, a, b, 0);
-                    X[2] = xi_sum(Wk[2], nW, b2, jmin, jmax, a, b, 1);
-                    X[3] = xi_sum(Wk[3], nW, b2, jmin, jmax, a, b, 1);
-                    X[4] = xi_sum(Wk[4], nW, b2, jmin, jmax, a, b, 1);
+                    X[0] = xi_sum(Wk[0], nW, b2, jmin, jmax, a, b, 1, absmode);
+                    X[1] = xi_sum(Wk[1], nW, b0, jmin, jmax, a, b, 0, absmode);
+                    X[2] = xi_sum(Wk[2], nW, b2, jmin, jmax, a, b, 1, absmode);
+                    X[3] = xi_sum(Wk[3], nW, b2, jmin, jmax, a, b, 1, absmode);
+                    X[4] = xi_sum(Wk[4], nW, b2, jmin, jmax, a, b, 1, absmode);
                 }
                 switch (kind) {
                 case 0:
@@ -377,4 +394,34 @@ double or_l3_terms(int lmin, int lmax, long nW, const int *rows, int nrows)
         }
     }
     return tot;
+}
+
+int or_loop_cov(int kind, const double *const *S, const double *const *R, const double *const *Wk, long nW, int lmin,
+                int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads)
+{
+    return loop_cov_impl(kind, S, R, Wk, nW, lmin, lmax, C, ldc, rows, nrows, nthreads, 0);
+}
+
+/* The same covariance formula evaluated on |spectra|, |ratios|, |W| and |3j
+ * products|: the size of the sum of |terms| behind each element, i.e. the
+ * scale below which an FP64 evaluation cannot resolve a cancelling element. */
+int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, const double *const *Wk, long nW,
+                    int lmin, int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads)
+{
+    int nr = kind == 6 ? 0 : (kind >= 0 && kind < 7 ? (kind < 2 ? 4 : 2) : 0);
+    size_t n = (size_t)lmax + 1;
+    double *buf = (double *)malloc(sizeof(double) * n * 8);
+    if (!buf) return 2;
+    const double *Sa[4], *Ra[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 4; ++i) {
+        for (size_t l = 0; l < n; ++l) buf[i * n + l] = fabs(S[i][l]);
+        Sa[i] = buf + i * n;
+    }
+    for (int i = 0; i < nr; ++i) {
+        for (size_t l = 0; l < n; ++l) buf[(4 + i) * n + l] = fabs(R[i][l]);
+        Ra[i] = buf + (4 + i) * n;
+    }
+    int st = loop_cov_impl(kind, Sa, Ra, Wk, nW, lmin, lmax, C, ldc, rows, nrows, nthreads, 1);
+    free(buf);
+    return st;
 }

@@ -29,6 +29,13 @@ int or_xi(int product, int parity, const double *W, long nW, int lmin, int lmax,
 int or_loop_cov(int kind, const double *const *S, const double *const *R, const double *const *W, long nW, int lmin,
                 int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads);
 
+/* Same loops on |W|, |3j products| (and |spectra|, |ratios| for covariance):
+ * the sum of |terms| behind each element, the resolution scale of an FP64 sum. */
+int or_inner_mcm_abs(int spin, const double *W, long nW, int lmin, int lmax, double *M, long ldm,
+                     const int *rows, int nrows, int nthreads);
+int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, const double *const *W, long nW,
+                    int lmin, int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads);
+
 int or_cov_nwindows(int kind);
 int or_max_threads(void);
 double or_l3_terms(int lmin, int lmax, long nW, const int *rows, int nrows);

@@ -48,6 +48,11 @@ def _load():
         lib.or_w3j_family.restype = ci
         lib.or_inner_mcm.argtypes = [ci, dp, cl, ci, ci, dp, cl, ip, ci, ci]
         lib.or_inner_mcm.restype = ci
+        lib.or_inner_mcm_abs.argtypes = [ci, dp, cl, ci, ci, dp, cl, ip, ci, ci]
+        lib.or_inner_mcm_abs.restype = ci
+        lib.or_loop_cov_abs.argtypes = [ci, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp), cl, ci, ci, dp,
+                                        cl, ip, ci, ci]
+        lib.or_loop_cov_abs.restype = ci
         lib.or_xi.argtypes = [ci, ci, dp, cl, ci, ci, dp, cl, ci]
         lib.or_xi.restype = ci
         lib.or_loop_cov.argtypes = [ci, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp), cl, ci, ci, dp, cl,
@@ -87,14 +92,16 @@ def w3j_family(l1, l2, m1, m2):
     return jmin.value, out[:n].copy()
 
 
-def inner_mcm(spin, W, lmin, lmax, rows=None, nthreads=0, out=None):
-    """One spin-case mode-coupling matrix (inner_mcm00!/02!/++!/--!)."""
+def inner_mcm(spin, W, lmin, lmax, rows=None, nthreads=0, out=None, absolute=False):
+    """One spin-case mode-coupling matrix (inner_mcm00!/02!/++!/--!).  With
+    absolute=True: the same sums over |3j product| * |W| (sum of |terms|)."""
     lib = _load()
     W = np.ascontiguousarray(W, dtype=np.float64)
     n = lmax - lmin + 1
     M = np.zeros((n, n), dtype=np.float64, order="F") if out is None else out
     r, rp, nr = _rows(rows)
-    st = lib.or_inner_mcm(int(spin), _dptr(W), len(W), lmin, lmax, _dptr(M), n, rp, nr, nthreads)
+    fn = lib.or_inner_mcm_abs if absolute else lib.or_inner_mcm
+    st = fn(int(spin), _dptr(W), len(W), lmin, lmax, _dptr(M), n, rp, nr, nthreads)
     if st:
         raise RuntimeError("oracle inner_mcm failed (%d)" % st)
     return M
@@ -111,8 +118,9 @@ def xi(product, parity, W, lmin, lmax, nthreads=0):
     return X
 
 
-def loop_cov(kind, spectra, ratios, windows, lmin, lmax, rows=None, nthreads=0):
-    """Covariance block by the reference loop_cov*! formula for `kind`."""
+def loop_cov(kind, spectra, ratios, windows, lmin, lmax, rows=None, nthreads=0, absolute=False):
+    """Covariance block by the reference loop_cov*! formula for `kind`.  With
+    absolute=True: the formula on absolute values (sum of |terms| per element)."""
     lib = _load()
     k = COV_KINDS[kind] if isinstance(kind, str) else int(kind)
     name = [n for n, v in COV_KINDS.items() if v == k][0]
@@ -132,7 +140,8 @@ def loop_cov(kind, spectra, ratios, windows, lmin, lmax, rows=None, nthreads=0):
     n = lmax - lmin + 1
     C = np.zeros((n, n), dtype=np.float64, order="F")
     r, rp, nr = _rows(rows)
-    st = lib.or_loop_cov(k, Sa, Ra, Wa, nW, lmin, lmax, _dptr(C), n, rp, nr, nthreads)
+    fn = lib.or_loop_cov_abs if absolute else lib.or_loop_cov
+    st = fn(k, Sa, Ra, Wa, nW, lmin, lmax, _dptr(C), n, rp, nr, nthreads)
     if st:
         raise RuntimeError("oracle loop_cov failed (%d)" % st)
     return C

@@ -12,3 +12,24 @@ def max_rel(got, ref, floor_frac=0.0):
     err = np.abs(got - ref) / den
     err[bad] = np.abs(got[bad] - ref[bad])
     return float(np.max(err)) if err.size else 0.0
+
+
+def cond_scale(spin, W, lmin, lmax, rows=None):
+    """Sum of |terms| behind each mode-coupling element (the oracle's loops on
+    |3j product| |W|).  It equals |M| when nothing cancels (W >= 0 and a squared
+    family); an FP64 sum cannot resolve an element below eps times it."""
+    from oracle import oracle as o
+    return o.inner_mcm(spin, W, lmin, lmax, rows=rows, absolute=True)
+
+
+def cov_scale(kind, S, R, Ws, lmin, lmax):
+    """Sum of |terms| behind each covariance element (oracle formula on absolute values)."""
+    from oracle import oracle as o
+    return o.loop_cov(kind, S, R, Ws, lmin, lmax, absolute=True)
+
+
+def max_err_scaled(got, ref, scale):
+    """Largest |got - ref| / max(|ref|, scale) (elements with zero scale compare absolutely)."""
+    den = np.maximum(np.abs(ref), scale)
+    den = np.where(den == 0, 1.0, den)
+    return float(np.max(np.abs(np.asarray(got) - ref) / den)) if np.size(ref) else 0.0

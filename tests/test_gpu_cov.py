@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from gpu_util import max_rel
+from gpu_util import cov_scale, max_err_scaled, max_rel
 from oracle import oracle as o
 
 pytestmark = pytest.mark.gpu
@@ -19,10 +19,10 @@ def test_cov_kinds_vs_fixture_and_oracle(ctx, kind):
     R = [g["cov_R%d" % i] for i in range(4)][:o.COV_NRATIOS[kind]]
     Ws = [g["cov_W%d" % k] for k in range(8)][:o.COV_NWINDOWS[kind]]
     C = ctx.coupledcov(kind, S, R, Ws, 0, 32)
-    assert max_rel(C, g["cov_" + kind], 1e-9) < RTOL
+    assert max_err_scaled(C, g["cov_" + kind], cov_scale(kind, S, R, Ws, 0, 32)) < RTOL
     assert np.array_equal(C, C.T)
     C2 = ctx.coupledcov(kind, S, R, Ws, 3, 32)
-    assert max_rel(C2, o.loop_cov(kind, S, R, Ws, 3, 32), 1e-9) < RTOL
+    assert max_err_scaled(C2, o.loop_cov(kind, S, R, Ws, 3, 32), cov_scale(kind, S, R, Ws, 3, 32)) < RTOL
 
 
 @pytest.mark.parametrize("kind", list(o.COV_KINDS))
@@ -36,7 +36,7 @@ def test_cov_kinds_at_400(ctx, kind):
     R = R[:o.COV_NRATIOS[kind]]
     Ws = [syn.window_for_key(("t", k), L) for k in range(o.COV_NWINDOWS[kind])]
     C = ctx.coupledcov(kind, S, R, Ws, 0, L)
-    assert max_rel(C, o.loop_cov(kind, S, R, Ws, 0, L), 1e-9) < RTOL
+    assert max_err_scaled(C, o.loop_cov(kind, S, R, Ws, 0, L), cov_scale(kind, S, R, Ws, 0, L)) < RTOL
 
 
 @pytest.mark.parametrize("product,parity", [(0, 0), (0, 1), (1, 1), (1, 2), (1, 0), (2, 1), (2, 0)])
@@ -45,8 +45,15 @@ def test_xi_vs_oracle(ctx, product, parity):
     L = 90
     Ws = [syn.mask_spectrum(2 * L + 1, 0.5 + 0.05 * k, 40.0, seed=k) for k in range(3)]
     Xs = ctx.xi(product, parity, Ws, 0, L)
+    spin_of = {(0, 0): 0, (0, 1): 0, (1, 1): 2, (1, 2): 3, (2, 1): 1}
     for X, W in zip(Xs, Ws):
-        assert max_rel(X, o.xi(product, parity, W, 0, L), 1e-9 if product == 2 else 0.0) < RTOL
+        ref = o.xi(product, parity, W, 0, L)
+        if (product, parity) in spin_of:
+            l = np.arange(L + 1)
+            scale = o.inner_mcm(spin_of[product, parity], W, 0, L, absolute=True) / (2 * l[None, :] + 1)
+            assert max_err_scaled(X, ref, scale) < RTOL
+        else:
+            assert max_rel(X, ref, 1e-9) < RTOL
 
 
 def test_coupledcov_mirror_matches_oracle_gathering(ctx):
@@ -63,7 +70,7 @@ def test_coupledcov_mirror_matches_oracle_gathering(ctx):
     C = pg.coupledcov("TT", "EE", ws, spectra, noise, ctx=ctx)
     S = [spectra["TE", i, p], spectra["TE", i, q], spectra["TE", j, q], spectra["TE", j, p]]
     Ws = [Wf("∅∅", "∅∅", i, p, "TP", j, q, "TP"), Wf("∅∅", "∅∅", i, q, "TP", j, p, "TP")]
-    assert max_rel(C.parent, o.loop_cov("TTEE", S, [], Ws, 0, L), 1e-9) < RTOL
+    assert max_err_scaled(C.parent, o.loop_cov("TTEE", S, [], Ws, 0, L), cov_scale("TTEE", S, [], Ws, 0, L)) < RTOL
     # default noise ratios are ones (ConstantDict, src/covariance.jl:41-45)
     C1 = pg.coupledcov("TT", "TT", ws, spectra, ctx=ctx)
     one = np.ones(L + 1)
@@ -72,8 +79,9 @@ def test_coupledcov_mirror_matches_oracle_gathering(ctx):
             ("∅∅", "TT", i, p, "TT", j, q, "TT"), ("∅∅", "TT", j, q, "TT", i, p, "TT"),
             ("∅∅", "TT", i, q, "TT", j, p, "TT"), ("∅∅", "TT", j, p, "TT", i, q, "TT"),
             ("TT", "TT", i, p, "TT", j, q, "TT"), ("TT", "TT", i, q, "TT", j, p, "TT")]
-    ref = o.loop_cov("TTTT", S, [one] * 4, [Wf(*k) for k in keys], 0, L)
-    assert max_rel(C1.parent, ref, 1e-9) < RTOL
+    Wl = [Wf(*k) for k in keys]
+    ref = o.loop_cov("TTTT", S, [one] * 4, Wl, 0, L)
+    assert max_err_scaled(C1.parent, ref, cov_scale("TTTT", S, [one] * 4, Wl, 0, L)) < RTOL
 
 
 def test_cov_argument_errors(ctx):
