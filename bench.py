@@ -171,6 +171,27 @@ def run_reference(args):
     return 0
 
 
+def _accuracy(ctx, wl, got, ref):
+    """Max elementwise relative error of `got` (chosen) against `ref` (plain FP64) per spin
+    case, on the device.  TE elements are measured against the Cauchy-Schwarz bound of
+    their sum of |terms|, sqrt(M00(|W|) (M++(|W|) + M--(|W|))), computed in FP64."""
+    import torch
+    out = {}
+    names = {0: "TT", 1: "TE", 2: "EE_BB_pp", 3: "EE_BB_mm"}
+    for s in sorted(got):
+        den = ref[s].abs()
+        if s == 1:
+            import numpy as np
+            A = np.abs(wl["Ws"][1])
+            n = wl["lmax"] - wl["lmin"] + 1
+            m = ctx.mcm_multi({0: A, 2: A, 3: A}, wl["lmin"], wl["lmax"], mode="plain")
+            b = torch.from_numpy(np.sqrt(np.abs(m[0] * (m[2] + m[3]))).T.copy()).to(ref[s].device)
+            den = torch.maximum(den, b.reshape(n, n))
+        den = torch.where(den == 0, torch.ones_like(den), den)
+        out[names[s]] = float(((got[s] - ref[s]).abs() / den).max().item())
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -190,6 +211,13 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        tt = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
     wl = workload(args.config, rank)
     lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
     n = lmax - lmin + 1
@@ -205,8 +233,8 @@ def run_ours(args):
     wptr = {s: dW[s].data_ptr() for s in spins}
     mptr = {s: dM[s].data_ptr() for s in spins}
 
-    def step():
-        ctx.mcm_multi_device(wptr, nW, lmin, lmax, mptr, n, mode=mode)
+    def step(m=mode, outp=mptr):
+        ctx.mcm_multi_device(wptr, nW, lmin, lmax, outp, n, mode=m)
 
     peak64 = ctx.fma_peak(fp64=True)
     peak32 = ctx.fma_peak(fp64=False)
@@ -230,13 +258,36 @@ def run_ours(args):
     barrier()
     launches = ctx.launch_count() - n_launch0
     clk = clocks.stop()
-    elapsed = t0.elapsed_time(t1) / 1e3
-    if dist is not None:
-        tt = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3)
     elements = len(spins) * n * n
     value = world * elements * args.steps / elapsed
+
+    # the plain FP64 kernel on the same workload (the chosen form's comparison point)
+    plain = None
+    if mode == "chosen" and not args.no_plain:
+        pM = {s: torch.empty((n, n), dtype=torch.float64, device="cuda") for s in spins}
+        pptr = {s: pM[s].data_ptr() for s in spins}
+        step("plain", pptr)
+        torch.cuda.synchronize()
+        ksteps = max(1, min(args.steps, 2))
+        pk = []
+        barrier()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(ksteps):
+            flush.zero_()
+            step("plain", pptr)
+            pk.append(ctx.last_kernel_ms())
+        p1.record(stream)
+        barrier()
+        pel = max_over_ranks(p0.elapsed_time(p1) / 1e3)
+        acc = _accuracy(ctx, wl, dM, pM) if rank == 0 else None
+        plain = {"value": world * elements * ksteps / pel, "unit": UNIT, "kernel_ms_per_launch": statistics.mean(pk),
+                 "steps": ksteps}
+        plain["chosen_over_plain"] = value / plain["value"]
+        plain["max_rel_err_chosen_vs_fp64"] = acc
+        del pM
 
     # end to end through the host-pointer ABI: pinned spectra in, pinned matrices out
     hW = {s: torch.from_numpy(np.ascontiguousarray(wl["Ws"][s])).pin_memory().numpy() for s in spins}
@@ -248,11 +299,7 @@ def run_ours(args):
     for _ in range(args.steps):
         ctx.mcm_multi(hW, lmin, lmax, mode=mode, outs=hM)
     barrier()
-    e_el = time.perf_counter() - e0
-    if dist is not None:
-        tt = torch.tensor([e_el], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e_el = float(tt.item())
+    e_el = max_over_ranks(time.perf_counter() - e0)
     e2e = {"value": world * elements * args.steps / e_el, "unit": UNIT,
            "h2d_bytes_per_step": int(sum(min(len(hW[s]), 2 * lmax + 1) * 8 for s in spins)),
            "d2h_bytes_per_step": int(elements * 8)}
@@ -265,24 +312,26 @@ def run_ours(args):
     terms = l3_terms(lmin, lmax, nW)
     fl = flops_per_launch(wl, terms)
     kms = statistics.mean(kernel_ms)
-    peak = peak64 if mode in ("plain", "fp64") else peak32
+    peak = peak64 if mode == "plain" else peak32
     achieved = fl / (kms * 1e-3)
-    roofline = {"bound": "fp64_fma_pipe" if mode in ("plain", "fp64") else "fp32_fma_pipe",
+    roofline = {"bound": "fp64_fma_pipe" if mode == "plain" else "fp32_fma_pipe",
                 "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": None,
                 "peak_source": "measured live by the library's FMA-chain probe kernel (MEASURED_PEAKS.json has no "
                                "CUDA-core FP64/FP32 figure)",
                 "algorithmic_flops_per_launch": fl, "l3_terms_per_family": terms,
-                "kernel_ms_per_launch": kms}
+                "flops_per_l3_term": fl / terms, "kernel_ms_per_launch": kms}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if mode in ("plain", "fp64") else "f32",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if mode == "plain" else "f32",
             "data": "synthetic",
             "config": {"workload": wl["name"], "lmax": lmax, "nW": nW, "matrices_per_step": len(spins),
                        "cases": wl["cases"], "mode": mode, "per_rank": "independent problem per GPU",
                        "l2": "256 MiB buffer written between timed steps"},
             "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
             "fma_peaks_tflops": {"fp64": peak64 / 1e12, "fp32": peak32 / 1e12}}
+    if plain is not None:
+        line["plain_fp64"] = plain
     if world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, {"all_spins_3071": 8, "tt_767": 1}[args.config])
     print(json.dumps(line))
@@ -299,8 +348,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", default="all_spins_3071")
-    ap.add_argument("--mode", default="plain", choices=("plain", "chosen"))
+    ap.add_argument("--mode", default="chosen", choices=("plain", "chosen"),
+                    help="chosen: FP32-pipe recurrence with compensation (the product path); plain: FP64")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 kernel")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -35,6 +35,8 @@ struct ps_ctx {
     double* d_out = nullptr;
     size_t out_cap = 0;
     double* d_probe = nullptr;
+    int2* d_bf = nullptr;  // split (mantissa, exponent) windows for the chosen kernel
+    size_t bf_cap = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
     double last_ms = 0.0;
@@ -116,8 +118,7 @@ static int check_grid(ps_ctx* c, int lmin, int lmax, int64_t nW, int64_t ld)
 
 static int check_mode(ps_ctx* c, int mode)
 {
-    if (mode == PS_MODE_PLAIN_FP64) return PS_OK;
-    if (mode == PS_MODE_CHOSEN) return set_err(c, PS_ERR_UNSUPPORTED, "PS_MODE_CHOSEN is not built into this library");
+    if (mode == PS_MODE_PLAIN_FP64 || mode == PS_MODE_CHOSEN) return PS_OK;
     return set_err(c, PS_ERR_ARG, "unknown mode %d", mode);
 }
 
@@ -161,24 +162,44 @@ void cov_window_spec(int kind, int k, int* product, int* parity)
 // Launch the coupling kernel with event timing on the context stream.
 static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode)
 {
-    (void)mode;
     int st = ensure_tasks(c, p.lmin, p.lmax);
     if (st) return st;
     p.tasks = c->d_tasks;
     p.ntasks = c->ntasks;
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    PS_CUDA(c, ps::launch_plain_fp64(p, c->stream));
+    if (mode == PS_MODE_CHOSEN)
+        PS_CUDA(c, ps::launch_chosen(p, c->stream));
+    else
+        PS_CUDA(c, ps::launch_plain_fp64(p, c->stream));
     c->launches++;
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->timed = true;
     return PS_OK;
 }
 
-// Upload (if host) and pad K windows into ctx->d_win; fills p.win[k].wW.
+static int ensure_int2(ps_ctx* c, int2** p, size_t* cap, size_t need)
+{
+    if (need <= *cap) return PS_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, need * sizeof(int2));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_err(c, PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", need * sizeof(int2), cudaGetErrorString(e));
+    }
+    *cap = need;
+    return PS_OK;
+}
+
+// Upload (if host) and pad K windows into ctx->d_win; fills p.win[k].wW (and,
+// for the chosen kernel, the split copies p.win[k].bf).
 static int stage_windows(ps_ctx* c, ps::CouplingParams& p, const double* const* W, int K, int64_t nW, int lmax,
-                         bool host)
+                         bool host, int mode)
 {
     int wlen = 2 * lmax + 2;
+    p.wlen = wlen;
     long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
     int st = ensure(c, &c->d_win, &c->win_cap, (size_t)K * wlen);
     if (st) return st;
@@ -197,6 +218,14 @@ static int stage_windows(ps_ctx* c, ps::CouplingParams& p, const double* const* 
         PS_CUDA(c, ps::launch_pad_windows(c->d_win + (size_t)k * wlen, src, nuse, wlen, c->stream));
         c->launches++;
         p.win[k].wW = c->d_win + (size_t)k * wlen;
+    }
+    if (mode == PS_MODE_CHOSEN) {
+        if ((st = ensure_int2(c, &c->d_bf, &c->bf_cap, (size_t)K * wlen))) return st;
+        for (int k = 0; k < K; ++k) {
+            PS_CUDA(c, ps::launch_split_windows(c->d_bf + (size_t)k * wlen, p.win[k].wW, wlen, c->stream));
+            c->launches++;
+            p.win[k].bf = c->d_bf + (size_t)k * wlen;
+        }
     }
     return PS_OK;
 }
@@ -237,6 +266,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_spec);
     cudaFree(c->d_out);
     cudaFree(c->d_probe);
+    cudaFree(c->d_bf);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -298,7 +328,7 @@ static int mcm_multi_impl(ps_ctx* c, unsigned cases, const double* const W[4], i
         ++K;
     }
     p.nwin = K;
-    if ((st = stage_windows(c, p, wsel, K, nW, lmax, host))) return st;
+    if ((st = stage_windows(c, p, wsel, K, nW, lmax, host, mode))) return st;
     const long long n = lmax - lmin + 1;
     if (host) {
         if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
@@ -364,7 +394,7 @@ int ps_xi(ps_ctx* c, int product, int parity, const double* const* W, int K, int
         p.win[k].product = product;
         p.win[k].parity = parity;
     }
-    if ((st = stage_windows(c, p, W, K, nW, lmax, true))) return st;
+    if ((st = stage_windows(c, p, W, K, nW, lmax, true, mode))) return st;
     const long long n = lmax - lmin + 1;
     if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
     for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
@@ -399,7 +429,7 @@ static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* c
     p.cov_kind = kind;
     p.nwin = K;
     for (int k = 0; k < K; ++k) ps::cov_window_spec(kind, k, &p.win[k].product, &p.win[k].parity);
-    if ((st = stage_windows(c, p, W, K, nW, lmax, host))) return st;
+    if ((st = stage_windows(c, p, W, K, nW, lmax, host, mode))) return st;
     const size_t ns = (size_t)lmax + 1;
     if (host) {
         if ((st = ensure(c, &c->d_spec, &c->spec_cap, 8 * ns))) return st;

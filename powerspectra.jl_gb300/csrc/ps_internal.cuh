@@ -31,7 +31,8 @@ enum Parity : int { PAR_ALL = 0, PAR_EVEN = 1, PAR_ODD = 2 };
 enum Epilogue : int { EPI_MCM = 0, EPI_XI = 1, EPI_COV = 2 };
 
 struct WinDesc {
-    const double* wW;  // padded (2 l3 + 1) W[l3], length >= 2 lmax + 1
+    const double* wW;  // padded (2 l3 + 1) W[l3], length wlen >= 2 lmax + 2
+    const int2* bf;    // the same values split as (float mantissa bits, int exponent) for the chosen kernel
     int product;
     int parity;
 };
@@ -45,14 +46,20 @@ struct CouplingParams {
     int epilogue;
     double* out[kMaxWin];  // EPI_MCM / EPI_XI: one matrix per window; EPI_COV: out[0]
     long long ldo;
+    int wlen;  // length of the padded window arrays
     int cov_kind;
     const double* S[4];  // covariance signal spectra (length >= lmax + 1), reference argument order
     const double* R[4];  // covariance noise ratios
 };
 
-// Launchers (ps_plain_fp64.cu).
+// Launchers (ps_plain_fp64.cu, ps_chosen.cu).
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
+cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_pad_windows(double* dst, const double* src, long long nW, int wlen, cudaStream_t s);
+cudaError_t launch_split_windows(int2* dst, const double* wW, int wlen, cudaStream_t s);
+
+// Exponent marking an exact zero in the split window arrays.
+constexpr int kZeroExp = -100000;
 cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cudaStream_t s);
 
 // Host-side covariance table (ps_api.cu).

@@ -23,7 +23,7 @@
 // Only the two normalisation sums and the window sums are kept per pair, so
 // normalisation, matching and sign are applied once at the end.
 #include "ps_internal.cuh"
-#include "ps_cov_epilogue.cuh"
+#include "ps_epilogue.cuh"
 
 namespace ps {
 
@@ -101,13 +101,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_fp64(const Cou
 
     double Xi[kMaxWin];
     if (T == 0) {
-        // single term l3 = l2 with f00^2 = 1/(2 l2 + 1); the 22 family is identically zero.
-#pragma unroll
-        for (int k = 0; k < kMaxWin; ++k) {
-            Xi[k] = 0.0;
-            if (k < p.nwin && p.win[k].product == PROD_00_00 && p.win[k].parity != PAR_ODD)
-                Xi[k] = __ldg(p.win[k].wW + l2) / (2.0 * l2 + 1.0) * kInv4Pi;
-        }
+        xi_single_term(p, l2, Xi);
     } else {
         // ---------------- forward from jmin: points jmin .. jm ----------------
         Sums F;
@@ -226,29 +220,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_fp64(const Cou
         }
     }
 
-    if (!active) return;
-    const long long r1 = l1 - p.lmin, r2 = l2 - p.lmin;
-    if (p.epilogue == EPI_MCM) {
-#pragma unroll
-        for (int k = 0; k < kMaxWin; ++k) {
-            if (k < p.nwin) {
-                p.out[k][r1 + r2 * p.ldo] = (2.0 * l2 + 1.0) * Xi[k];
-                p.out[k][r2 + r1 * p.ldo] = (2.0 * l1 + 1.0) * Xi[k];
-            }
-        }
-    } else if (p.epilogue == EPI_XI) {
-#pragma unroll
-        for (int k = 0; k < kMaxWin; ++k) {
-            if (k < p.nwin) {
-                p.out[k][r1 + r2 * p.ldo] = Xi[k];
-                p.out[k][r2 + r1 * p.ldo] = Xi[k];
-            }
-        }
-    } else {
-        double c = cov_combine(p.cov_kind, p.S, p.R, Xi, l1, l2);
-        p.out[0][r1 + r2 * p.ldo] = c;
-        p.out[0][r2 + r1 * p.ldo] = c;
-    }
+    if (active) write_pair(p, l1, l2, Xi);
 }
 
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s)

@@ -185,7 +185,7 @@ class Context:
             cases |= 1 << s
             wl[s] = W
             ml[s] = (outs[s] if outs is not None else np.empty((n, n), dtype=np.float64, order="F"))
-        self.check(self.lib.ps_mcm_multi(self.handle, cases, dptr_array(wl), nW, lmin, lmax, mode_code(mode),
+        self.check(self.lib.ps_mcm_multi(self.handle, cases, dptr_array(wl), nW or 1, lmin, lmax, mode_code(mode),
                                          dptr_array(ml), n))
         return {s: ml[s] for s in Ws}
 

@@ -33,3 +33,14 @@ def max_err_scaled(got, ref, scale):
     den = np.maximum(np.abs(ref), scale)
     den = np.where(den == 0, 1.0, den)
     return float(np.max(np.abs(np.asarray(got) - ref) / den)) if np.size(ref) else 0.0
+
+
+def gpu_cond_scale(ctx, spin, W, lmin, lmax):
+    """cond_scale computed with the GPU's plain FP64 path (for sizes the oracle is too slow
+    for): |M| of |W| for squared families; for 00x22 the Cauchy-Schwarz bound
+    sqrt(M00(|W|) (M++(|W|) + M--(|W|)))."""
+    A = np.abs(np.asarray(W, dtype=np.float64))
+    if spin != 1:
+        return np.abs(ctx.mcm(spin, A, lmin, lmax, mode="plain"))
+    m = ctx.mcm_multi({0: A, 2: A, 3: A}, lmin, lmax, mode="plain")
+    return np.sqrt(np.abs(m[0] * (m[2] + m[3])))

@@ -103,3 +103,14 @@ def test_synthetic_forms():
     w1 = ws.window_function_W("∅∅", "∅∅", "a", "b", "TT", "c", "d", "TT")
     w2 = ws.window_function_W("∅∅", "∅∅", "a", "b", "TT", "c", "d", "TT")
     assert np.array_equal(w1, w2) and len(w1) == 21
+
+
+def test_bench_work_accounting_matches_oracle():
+    import bench
+    from oracle import oracle as o
+    for (lmin, lmax, nW) in ((0, 100, 201), (0, 100, 101), (3, 57, 40)):
+        assert bench.l3_terms(lmin, lmax, nW) == int(o.l3_terms(lmin, lmax, nW))
+    wl = bench.workload("all_spins_3071")
+    assert wl["nW"] == 6143 and sorted(wl["Ws"]) == [0, 1, 2, 3]
+    # fixed accounting: 9 (00) + 16 (22) + 3 per distinct spectrum
+    assert bench.flops_per_launch(wl, 1) == 9 + 16 + 3 * 3
