@@ -58,10 +58,11 @@ def l3_terms(lmin, lmax, nW):
 
 def workload(name, rank=0):
     from powerspectra_gpu import synthetic as syn
-    if name == "all_spins_3071":
-        c = syn.all_spins(3071, seed=1 + 10 * rank)
+    if name.startswith("all_spins_"):
+        L = int(name.rsplit("_", 1)[1])  # all_spins_3071 is the benchmark; smaller ones are profiling cases
+        c = syn.all_spins(L, seed=1 + 10 * rank)
         Ws = {0: c["WT"], 1: c["WTP"], 2: c["WP"], 3: c["WP"]}
-        return {"name": name, "lmin": 0, "lmax": 3071, "nW": c["nW"], "Ws": Ws, "spectra": 3,
+        return {"name": name, "lmin": 0, "lmax": L, "nW": c["nW"], "Ws": Ws, "spectra": 3,
                 "cases": ["TT (M00, W_T)", "TE (M02, W_TxP)", "EE/BB diagonal (M++, W_P)", "EE/BB off-diagonal (M--, W_P)"]}
     if name == "tt_767":
         c = syn.tt_767(seed=rank)
@@ -151,7 +152,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     wl = workload(args.config)
-    stride = {"all_spins_3071": 48, "tt_767": 4}[args.config]
+    stride = {"tt_767": 4}.get(args.config, 48)
     for _ in range(args.warmup):
         cpu_baseline(wl, stride)
     vals = [cpu_baseline(wl, stride) for _ in range(args.steps)]
@@ -333,7 +334,7 @@ def run_ours(args):
     if plain is not None:
         line["plain_fp64"] = plain
     if world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(wl, {"all_spins_3071": 8, "tt_767": 1}[args.config])
+        line["cpu_baseline"] = cpu_baseline(wl, {"tt_767": 1}.get(args.config, 8))
     print(json.dumps(line))
     ctx.close()
     if dist is not None:

@@ -1,0 +1,125 @@
+# PowerSpectraGPU.jl -- ccall shim that routes PowerSpectra.jl's hot loops to
+# libpowerspectra_gpu.so (the C ABI in include/powerspectra_gpu.h).
+#
+# Loading this module after PowerSpectra adds more specific methods for
+# Float64 matrix-backed SpectralArrays to
+#     inner_mcm⁰⁰!, inner_mcm⁰²!, inner_mcm⁺⁺!, inner_mcm⁻⁻!   (src/modecoupling.jl:78-159)
+#     loop_covTTTT!, loop_covEEEE!, loop_covTTTE!, loop_covTETE!,
+#     loop_covTEEE!, loop_covTEEE_planck!, loop_covTTEE!        (src/covariance.jl:92-446)
+# so `mcm`, `coupledcov` and `master` keep their signatures and return types
+# while the (l1, l2) loops run on the GPU.  There is no CPU fallback: a missing
+# library or device raises.
+module PowerSpectraGPU
+
+using PowerSpectra
+import PowerSpectra: SpectralArray, SpectralVector
+
+const libps = get(ENV, "POWERSPECTRA_GPU_LIB",
+                  joinpath(@__DIR__, "..", "lib", "libpowerspectra_gpu.so"))
+
+const PS_SPIN_00 = Cint(0)
+const PS_SPIN_02 = Cint(1)
+const PS_SPIN_PP = Cint(2)
+const PS_SPIN_MM = Cint(3)
+const PS_MODE_PLAIN_FP64 = Cint(0)
+const PS_MODE_CHOSEN = Cint(1)
+const COV = Dict(:TTTT => Cint(0), :EEEE => Cint(1), :TTTE => Cint(2), :TETE => Cint(3),
+                 :TEEE => Cint(4), :TEEE_planck => Cint(5), :TTEE => Cint(6))
+
+# arithmetic used by the overrides; PS_MODE_PLAIN_FP64 reproduces the FP64 loops
+const MODE = Ref(PS_MODE_CHOSEN)
+# one library context per Julia thread (a context is not thread-safe)
+const CTXS = Dict{Int,Ptr{Cvoid}}()
+const CTX_LOCK = ReentrantLock()
+
+function ctx()
+    tid = Threads.threadid()
+    lock(CTX_LOCK) do
+        get!(CTXS, tid) do
+            h = Ref{Ptr{Cvoid}}(C_NULL)
+            st = ccall((:ps_create, libps), Cint, (Cint, Ref{Ptr{Cvoid}}), Cint(0), h)
+            st == 0 || error("powerspectra_gpu: ps_create failed with status $st (no usable CUDA device?)")
+            h[]
+        end
+    end
+end
+
+function check(st, c)
+    st == 0 && return nothing
+    msg = unsafe_string(ccall((:ps_last_error, libps), Cstring, (Ptr{Cvoid},), c))
+    st == 1 ? throw(ArgumentError(msg)) : error("powerspectra_gpu error $st: $msg")
+end
+
+const FMat = SpectralArray{Float64,2,Matrix{Float64}}
+
+function gpu_mcm!(spin::Cint, 𝐌::FMat, V::SpectralVector{Float64})
+    @assert axes(𝐌, 1) == axes(𝐌, 2)
+    lmin, lmax = first(axes(𝐌, 1)), last(axes(𝐌, 1))
+    M = parent(𝐌)          # column-major Matrix{Float64}, element (l1,l2) at [l1-lmin+1, l2-lmin+1]
+    W = collect(parent(V))  # 0-indexed spectrum: W[1] is l = 0
+    c = ctx()
+    st = ccall((:ps_mcm, libps), Cint,
+               (Ptr{Cvoid}, Cint, Ptr{Float64}, Int64, Cint, Cint, Cint, Ptr{Float64}, Int64),
+               c, spin, W, length(W), lmin, lmax, MODE[], M, stride(M, 2))
+    check(st, c)
+    return 𝐌
+end
+
+PowerSpectra.inner_mcm⁰⁰!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!(PS_SPIN_00, 𝐌, V)
+PowerSpectra.inner_mcm⁰²!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!(PS_SPIN_02, 𝐌, V)
+PowerSpectra.inner_mcm⁺⁺!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!(PS_SPIN_PP, 𝐌, V)
+PowerSpectra.inner_mcm⁻⁻!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!(PS_SPIN_MM, 𝐌, V)
+
+function gpu_cov!(kind::Symbol, 𝐂::FMat, spectra, ratios, windows)
+    @assert axes(𝐂, 1) == axes(𝐂, 2)
+    lmin, lmax = first(axes(𝐂, 1)), last(axes(𝐂, 1))
+    S = [collect(parent(x)) for x in spectra]
+    R = [collect(parent(x)) for x in ratios]
+    W = [collect(parent(x)) for x in windows]
+    nW = minimum(length, W)
+    C = parent(𝐂)
+    c = ctx()
+    GC.@preserve S R W begin
+        Sp = [pointer(x) for x in S]
+        Rp = isempty(R) ? [Ptr{Float64}(C_NULL)] : [pointer(x) for x in R]
+        Wp = [pointer(x) for x in W]
+        st = ccall((:ps_coupledcov, libps), Cint,
+                   (Ptr{Cvoid}, Cint, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Int64,
+                    Cint, Cint, Cint, Ptr{Float64}, Int64),
+                   c, COV[kind], Sp, Rp, Wp, nW, lmin, lmax, MODE[], C, stride(C, 2))
+    end
+    check(st, c)
+    return 𝐂
+end
+
+const SV = SpectralVector{Float64}
+
+PowerSpectra.loop_covTTTT!(𝐂::FMat, TTip::SV, TTjq::SV, TTiq::SV, TTjp::SV, r_ip::SV, r_jq::SV, r_iq::SV, r_jp::SV,
+                           W1, W2, W3, W4, W5, W6, W7, W8) =
+    gpu_cov!(:TTTT, 𝐂, (TTip, TTjq, TTiq, TTjp), (r_ip, r_jq, r_iq, r_jp), (W1, W2, W3, W4, W5, W6, W7, W8))
+PowerSpectra.loop_covEEEE!(𝐂::FMat, EEip::SV, EEjq::SV, EEiq::SV, EEjp::SV, r_ip::SV, r_jq::SV, r_iq::SV, r_jp::SV,
+                           W1, W2, W3, W4, W5, W6, W7, W8) =
+    gpu_cov!(:EEEE, 𝐂, (EEip, EEjq, EEiq, EEjp), (r_ip, r_jq, r_iq, r_jp), (W1, W2, W3, W4, W5, W6, W7, W8))
+PowerSpectra.loop_covTTTE!(𝐂::FMat, TTip::SV, TTjp::SV, TEiq::SV, TEjq::SV, r_ip::SV, r_jp::SV, W1, W2, W3, W4) =
+    gpu_cov!(:TTTE, 𝐂, (TTip, TTjp, TEiq, TEjq), (r_ip, r_jp), (W1, W2, W3, W4))
+PowerSpectra.loop_covTETE!(𝐂::FMat, TTip::SV, EEjq::SV, TEiq::SV, TEjp::SV, r_TT_ip::SV, r_PP_jq::SV,
+                           W1, W2, W3, W4, W5) =
+    gpu_cov!(:TETE, 𝐂, (TTip, EEjq, TEiq, TEjp), (r_TT_ip, r_PP_jq), (W1, W2, W3, W4, W5))
+PowerSpectra.loop_covTEEE!(𝐂::FMat, EEjq::SV, EEjp::SV, TEip::SV, TEiq::SV, r_EE_jq::SV, r_EE_jp::SV,
+                           W1, W2, W3, W4) =
+    gpu_cov!(:TEEE, 𝐂, (EEjq, EEjp, TEip, TEiq), (r_EE_jq, r_EE_jp), (W1, W2, W3, W4))
+PowerSpectra.loop_covTEEE_planck!(𝐂::FMat, EEjq::SV, EEjp::SV, TEip::SV, TEiq::SV, r_EE_jq::SV, r_EE_jp::SV,
+                                  W1, W2, W3, W4) =
+    gpu_cov!(:TEEE_planck, 𝐂, (EEjq, EEjp, TEip, TEiq), (r_EE_jq, r_EE_jp), (W1, W2, W3, W4))
+PowerSpectra.loop_covTTEE!(𝐂::FMat, TEip::SV, TEiq::SV, TEjq::SV, TEjp::SV, W1, W2) =
+    gpu_cov!(:TTEE, 𝐂, (TEip, TEiq, TEjq, TEjp), (), (W1, W2))
+
+function __init__()
+    atexit() do
+        for (_, h) in CTXS
+            ccall((:ps_destroy, libps), Cvoid, (Ptr{Cvoid},), h)
+        end
+    end
+end
+
+end # module
