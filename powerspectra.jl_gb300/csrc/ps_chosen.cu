@@ -25,6 +25,8 @@
 #include "ps_epilogue.cuh"
 #include "ps_ff.cuh"
 
+#include <stdint.h>
+
 namespace ps {
 
 constexpr int kChunk = 32;               // steps between window restaging / FP64 flushes
@@ -65,8 +67,81 @@ __device__ __forceinline__ float mul_ff(ff a, ff b)
     return __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmul_rn(a.h, b.h)));
 }
 
-template <int NWIN, bool N00, bool N22>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const CouplingParams p)
+// Window configuration: 4 bits per window, product + 1 in bits 0-1 (so a used
+// window is never 0) and parity in bits 2-3.  A non-zero SPEC fixes the
+// configuration at compile time (the common mode-coupling and covariance
+// sets); SPEC == 0 reads it from the launch parameters.
+constexpr uint32_t wspec(int prod, int par) { return (uint32_t)((prod + 1) | (par << 2)); }
+template <uint32_t SPEC>
+__device__ __forceinline__ int wprod(const CouplingParams& p, int k)
+{
+    return SPEC ? (int)((SPEC >> (4 * k)) & 3u) - 1 : p.win[k].product;
+}
+template <uint32_t SPEC>
+__device__ __forceinline__ int wpar(const CouplingParams& p, int k)
+{
+    return SPEC ? (int)((SPEC >> (4 * k + 2)) & 3u) : p.win[k].parity;
+}
+
+// Per-direction recurrence state.  `sgn` picks the direction of the factor
+// updates: forward P(j+1) = (t+1)(2d+t+1)(2l1-t)(2l2+t+2),
+// backward P(j) = (2l1-t)(2l2-t)(1+t)(2l1+2l2+1-t).
+struct Sweep {
+    ff f2, f2o;   // 22 family at the current point and at the previous one
+    ff a;         // a at the previous point (forward: a(j); backward: a(j+1))
+    ff f0;        // 00 family at the last even point
+    float A, B, C, D;  // integer factors of the next P
+    float w;      // 2j + 1 at the current point
+};
+
+template <bool N00, bool N22, bool ODD_STEP>
+__device__ __forceinline__ void sweep_step(Sweep& s, float dA, float dB, float dC, float dD, float dw)
+{
+    ff P = ff_mul_raw(two_prod(s.A, s.B), two_prod(s.C, s.D));
+    ff r = ff_rsqrt(P);
+    if (N22) {
+        // f(next) = -(c (2j+1) f(j) + a f(prev)) / a(next), c = 4
+        ff u = ff_mul_raw(s.f2, ff_make(4.0f * s.w));
+        ff v = ff_mul_raw(s.a, s.f2o);
+        ff nf = ff_neg(ff_mul(ff_add(u, v), r));
+        s.f2o = s.f2;
+        s.f2 = nf;
+    }
+    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul(ff_mul_raw(s.a, r), s.f0));  // 00 at the next even point
+    s.a = ff_mul_raw(P, r);
+    s.A += dA; s.B += dB; s.C += dC; s.D += dD;
+    s.w += dw;
+}
+
+template <int NWIN, bool N00, bool N22, uint32_t SPEC, bool EVEN>
+__device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& s, const float* sw, int slot,
+                                          float* c, float& n0, float& n2)
+{
+    float x22 = N22 ? sq_ff(s.f2) : 0.0f;
+    if (N22) n2 = __fmaf_rn(s.w, x22, n2);
+    if (EVEN) {
+        float x00 = N00 ? sq_ff(s.f0) : 0.0f;
+        float x02 = (N00 && N22) ? mul_ff(s.f0, s.f2) : 0.0f;
+        if (N00) n0 = __fmaf_rn(s.w, x00, n0);
+#pragma unroll
+        for (int k = 0; k < NWIN; ++k) {
+            if ((SPEC || k < p.nwin) && wpar<SPEC>(p, k) != PAR_ODD) {
+                const int pr = wprod<SPEC>(p, k);
+                float x = pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02);
+                c[k] = __fmaf_rn(x, sw[k * kSlots + slot], c[k]);
+            }
+        }
+    } else if (N22) {
+#pragma unroll
+        for (int k = 0; k < NWIN; ++k) {
+            if ((SPEC || k < p.nwin) && wprod<SPEC>(p, k) == PROD_22_22 && wpar<SPEC>(p, k) != PAR_EVEN)
+                c[k] = __fmaf_rn(x22, sw[k * kSlots + slot], c[k]);
+        }
+    }
+}
+
+template <int NWIN, bool N00, bool N22, uint32_t SPEC>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
 {
     __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
     const int warp = threadIdx.x >> 5;
@@ -91,12 +166,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
         return;
     }
 
-    // forward state (j = jmin + t) and backward state (j = jmax - t)
-    ff g2c = ff_make(1.0f), g2p = ff_make(0.0f), aj = ff_make(0.0f), g0 = ff_make(1.0f);
-    ff h2c = ff_make(1.0f), h2n = ff_make(0.0f), an = ff_make(0.0f), h0 = ff_make(1.0f);
-    float fA = 1.0f, fB = (float)(2 * d + 1), fC = (float)(2 * l1), fD = (float)(2 * l2 + 2);
-    float bA = (float)(2 * l1), bB = (float)(2 * l2), bC = 1.0f, bD = (float)(2 * l1 + 2 * l2 + 1);
-    float fw = (float)(2 * jmin + 1), bw = (float)(2 * jmax + 1);
+    Sweep F, B;
+    F.f2 = ff_make(1.0f); F.f2o = ff_make(0.0f); F.a = ff_make(0.0f); F.f0 = ff_make(1.0f);
+    F.A = 1.0f; F.B = (float)(2 * d + 1); F.C = (float)(2 * l1); F.D = (float)(2 * l2 + 2);
+    F.w = (float)(2 * jmin + 1);
+    B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.a = ff_make(0.0f); B.f0 = ff_make(1.0f);
+    B.A = (float)(2 * l1); B.B = (float)(2 * l2); B.C = 1.0f; B.D = (float)(2 * l1 + 2 * l2 + 1);
+    B.w = (float)(2 * jmax + 1);
     double FW[NWIN], BW[NWIN];
 #pragma unroll
     for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
@@ -109,7 +185,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
         int eF[NWIN], eB[NWIN];
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin) {
+            if (SPEC || k < p.nwin) {
                 eF[k] = stage_slice(sF + k * kSlots, p.win[k].bf, jmin0 + t0, p.wlen, lane);
                 eB[k] = stage_slice(sB + k * kSlots, p.win[k].bf, jmax0 - t0 - kChunk + 1, p.wlen, lane);
             } else {
@@ -121,75 +197,23 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) cF[k] = cB[k] = 0.0f;
         float n0F = 0.0f, n2F = 0.0f, n0B = 0.0f, n2B = 0.0f;
-        const int steps = min(kChunk, T - t0);
-        for (int s = 0; s < steps; ++s) {
-            const bool even = ((t0 + s) & 1) == 0;  // parity of l1 + l2 + l3, both directions
-            const int sf = lane + s, sb = lane - s + kChunk - 1;
-            // ---- accumulate the current forward and backward points ----
-            {
-                float x22f = N22 ? sq_ff(g2c) : 0.0f;
-                float x22b = N22 ? sq_ff(h2c) : 0.0f;
-                if (N22) {
-                    n2F = __fmaf_rn(fw, x22f, n2F);
-                    n2B = __fmaf_rn(bw, x22b, n2B);
-                }
-                if (even) {
-                    float x00f = N00 ? sq_ff(g0) : 0.0f, x00b = N00 ? sq_ff(h0) : 0.0f;
-                    float x02f = (N00 && N22) ? mul_ff(g0, g2c) : 0.0f, x02b = (N00 && N22) ? mul_ff(h0, h2c) : 0.0f;
-                    if (N00) {
-                        n0F = __fmaf_rn(fw, x00f, n0F);
-                        n0B = __fmaf_rn(bw, x00b, n0B);
-                    }
-#pragma unroll
-                    for (int k = 0; k < NWIN; ++k) {
-                        if (k < p.nwin && p.win[k].parity != PAR_ODD) {
-                            const int pr = p.win[k].product;
-                            float xf = pr == PROD_00_00 ? x00f : (pr == PROD_22_22 ? x22f : x02f);
-                            float xb = pr == PROD_00_00 ? x00b : (pr == PROD_22_22 ? x22b : x02b);
-                            cF[k] = __fmaf_rn(xf, sF[k * kSlots + sf], cF[k]);
-                            cB[k] = __fmaf_rn(xb, sB[k * kSlots + sb], cB[k]);
-                        }
-                    }
-                } else if (N22) {
-#pragma unroll
-                    for (int k = 0; k < NWIN; ++k) {
-                        if (k < p.nwin && p.win[k].product == PROD_22_22 && p.win[k].parity != PAR_EVEN) {
-                            cF[k] = __fmaf_rn(x22f, sF[k * kSlots + sf], cF[k]);
-                            cB[k] = __fmaf_rn(x22b, sB[k * kSlots + sb], cB[k]);
-                        }
-                    }
-                }
-            }
-            // ---- forward step: g(j+1) from g(j), g(j-1) ----
-            {
-                ff P = ff_mul_raw(two_prod(fA, fB), two_prod(fC, fD));  // P(j+1)
-                ff r = ff_rsqrt(P);
-                ff a1 = ff_mul(P, r);
-                if (N22) {
-                    ff g2n = ff_neg(ff_mul(ff_add(ff_mulf(g2c, 4.0f * fw), ff_mul(aj, g2p)), r));
-                    g2p = g2c;
-                    g2c = g2n;
-                }
-                if (N00 && !even) g0 = ff_neg(ff_mul(ff_mul(aj, r), g0));  // f00(j+1) = -a(j)/a(j+1) f00(j-1)
-                aj = a1;
-                fA += 1.0f; fB += 1.0f; fC -= 1.0f; fD += 1.0f;
-                fw += 2.0f;
-            }
-            // ---- backward step: h(j-1) from h(j), h(j+1) ----
-            {
-                ff P = ff_mul_raw(two_prod(bA, bB), two_prod(bC, bD));  // P(j)
-                ff r = ff_rsqrt(P);
-                ff a0 = ff_mul(P, r);
-                if (N22) {
-                    ff h2m = ff_neg(ff_mul(ff_add(ff_mulf(h2c, 4.0f * bw), ff_mul(an, h2n)), r));
-                    h2n = h2c;
-                    h2c = h2m;
-                }
-                if (N00 && !even) h0 = ff_neg(ff_mul(ff_mul(an, r), h0));  // f00(j-1) = -a(j+1)/a(j) f00(j+1)
-                an = a0;
-                bA -= 1.0f; bB -= 1.0f; bC += 1.0f; bD -= 1.0f;
-                bw -= 2.0f;
-            }
+        const int steps = min(kChunk, T - t0);  // t0 is even, so step s has the parity of s
+        int s = 0;
+        for (; s + 1 < steps; s += 2) {
+            sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
+            sweep_step<N00, N22, false>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
+            sweep_step<N00, N22, false>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
+            sweep_acc<NWIN, N00, N22, SPEC, false>(p, F, sF, lane + s + 1, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, false>(p, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
+            sweep_step<N00, N22, true>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
+            sweep_step<N00, N22, true>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
+        }
+        if (s < steps) {  // one even step left (T odd, last chunk)
+            sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
+            sweep_step<N00, N22, false>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
+            sweep_step<N00, N22, false>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
         }
         // ---- FP64 flush of the chunk sums ----
 #pragma unroll
@@ -208,14 +232,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
     const int jm = jmin + T;
     const bool evenT = (T & 1) == 0;
     {
-        double g2d = ff_to_double(g2c), g0d = (N00 && evenT) ? ff_to_double(g0) : 0.0;
+        double g2d = ff_to_double(F.f2), g0d = (N00 && evenT) ? ff_to_double(F.f0) : 0.0;
         double x22 = g2d * g2d, x00 = g0d * g0d, x02 = g0d * g2d, w = 2.0 * jm + 1.0;
         if (N22) FN2 = fma(w, x22, FN2);
         if (N00) FN0 = fma(w, x00, FN0);
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin) {
-                const int pr = p.win[k].product, pa = p.win[k].parity;
+            if (SPEC || k < p.nwin) {
+                const int pr = wprod<SPEC>(p, k), pa = wpar<SPEC>(p, k);
                 double ww = __ldg(p.win[k].wW + jm);
                 if (evenT && pa != PAR_ODD)
                     FW[k] = fma(pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02), ww, FW[k]);
@@ -224,15 +248,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
             }
         }
     }
-    // one more forward step for g(jm + 1)
-    double gm0 = ff_to_double(g2c), gm1 = 0.0, g0s;
+    // one more forward step for g(jm + 1) (and the 00 value at jm + 1 when T is odd)
+    const double gm0 = ff_to_double(F.f2);
+    double gm1 = 0.0, g0s;
     {
-        ff P = ff_mul_raw(two_prod(fA, fB), two_prod(fC, fD));
+        ff P = ff_mul_raw(two_prod(F.A, F.B), two_prod(F.C, F.D));
         ff r = ff_rsqrt(P);
-        if (N22) gm1 = ff_to_double(ff_neg(ff_mul(ff_add(ff_mulf(g2c, 4.0f * fw), ff_mul(aj, g2p)), r)));
-        g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(ff_mul(aj, r), g0))) : ff_to_double(g0);
+        if (N22) gm1 = ff_to_double(ff_neg(ff_mul(ff_add(ff_mul_raw(F.f2, ff_make(4.0f * F.w)), ff_mul_raw(F.a, F.f2o)), r)));
+        g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(ff_mul_raw(F.a, r), F.f0))) : ff_to_double(F.f0);
     }
-    const double hm0 = ff_to_double(h2c), hm1 = ff_to_double(h2n), h0s = ff_to_double(h0);
+    const double hm0 = ff_to_double(B.f2), hm1 = ff_to_double(B.f2o), h0s = ff_to_double(B.f0);
 
     // match, normalise, sign (FP64)
     const double lam0 = N00 ? g0s / h0s : 0.0;
@@ -246,8 +271,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
 #pragma unroll
     for (int k = 0; k < kMaxWin; ++k) {
         Xi[k] = 0.0;
-        if (k < NWIN && k < p.nwin) {
-            const int pr = p.win[k].product;
+        if (k < NWIN && (SPEC || k < p.nwin)) {
+            const int pr = wprod<SPEC>(p, k);
             if (pr == PROD_00_00)
                 Xi[k] = fma(lam0 * lam0, BW[k], FW[k]) * inv0;
             else if (!fam22)
@@ -261,32 +286,80 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_coupling_chosen(const C
     if (active) write_pair(p, l1, l2, Xi);
 }
 
-template <int NWIN>
-static cudaError_t launch_nwin(const CouplingParams& p, bool n00, bool n22, cudaStream_t s)
+// families a compile-time window set needs
+constexpr bool spec_needs(uint32_t spec, int nwin, bool fam00)
+{
+    bool need = false;
+    for (int k = 0; k < nwin; ++k) {
+        int pr = (int)((spec >> (4 * k)) & 3u) - 1;
+        need = need || (fam00 ? pr != PROD_22_22 : pr != PROD_00_00);
+    }
+    return need;
+}
+
+template <int NWIN, uint32_t SPEC>
+static cudaError_t launch_cfg(const CouplingParams& p, bool n00, bool n22, cudaStream_t s)
 {
     const int threads = kWarpsPerBlock * 32;
     const unsigned blocks = (unsigned)((p.ntasks + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    if (n00 && n22)
-        k_coupling_chosen<NWIN, true, true><<<blocks, threads, 0, s>>>(p);
-    else if (n22)
-        k_coupling_chosen<NWIN, false, true><<<blocks, threads, 0, s>>>(p);
-    else
-        k_coupling_chosen<NWIN, true, false><<<blocks, threads, 0, s>>>(p);
+    if constexpr (SPEC != 0) {
+        constexpr bool a = spec_needs(SPEC, NWIN, true), b = spec_needs(SPEC, NWIN, false);
+        (void)n00;
+        (void)n22;
+        k_coupling_chosen<NWIN, a, b, SPEC><<<blocks, threads, 0, s>>>(p);
+    } else {
+        if (n00 && n22)
+            k_coupling_chosen<NWIN, true, true, 0><<<blocks, threads, 0, s>>>(p);
+        else if (n22)
+            k_coupling_chosen<NWIN, false, true, 0><<<blocks, threads, 0, s>>>(p);
+        else
+            k_coupling_chosen<NWIN, true, false, 0><<<blocks, threads, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
+
+constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
+constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
+constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
+// the window sets of the mode-coupling and covariance entry points
+constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
+constexpr uint32_t S_PPMM = WPP | (WMM << 4);
+constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
 
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s)
 {
     bool n00 = false, n22 = false;
+    uint32_t spec = 0;
     for (int k = 0; k < p.nwin; ++k) {
         if (p.win[k].product != PROD_22_22) n00 = true;
         if (p.win[k].product != PROD_00_00) n22 = true;
+        spec |= wspec(p.win[k].product, p.win[k].parity) << (4 * k);
     }
     if (p.ntasks <= 0) return cudaSuccess;
-    if (p.nwin <= 1) return launch_nwin<1>(p, n00, n22, s);
-    if (p.nwin <= 2) return launch_nwin<2>(p, n00, n22, s);
-    if (p.nwin <= 4) return launch_nwin<4>(p, n00, n22, s);
-    return launch_nwin<8>(p, n00, n22, s);
+    switch (p.nwin) {
+    case 1:
+        if (spec == W00) return launch_cfg<1, W00>(p, n00, n22, s);
+        if (spec == W02) return launch_cfg<1, W02>(p, n00, n22, s);
+        if (spec == WPP) return launch_cfg<1, WPP>(p, n00, n22, s);
+        if (spec == WMM) return launch_cfg<1, WMM>(p, n00, n22, s);
+        return launch_cfg<1, 0>(p, n00, n22, s);
+    case 2:
+        if (spec == S_PPMM) return launch_cfg<2, S_PPMM>(p, n00, n22, s);
+        if (spec == rep(W00, 2)) return launch_cfg<2, rep(W00, 2)>(p, n00, n22, s);
+        return launch_cfg<2, 0>(p, n00, n22, s);
+    case 3:
+    case 4:
+        if (spec == S_MCM4) return launch_cfg<4, S_MCM4>(p, n00, n22, s);
+        if (spec == rep(W00, 4)) return launch_cfg<4, rep(W00, 4)>(p, n00, n22, s);
+        if (spec == rep(W02, 4)) return launch_cfg<4, rep(W02, 4)>(p, n00, n22, s);
+        if (spec == rep(WPP, 4)) return launch_cfg<4, rep(WPP, 4)>(p, n00, n22, s);
+        return launch_cfg<4, 0>(p, n00, n22, s);
+    default:
+        if (spec == S_TETE) return launch_cfg<5, S_TETE>(p, n00, n22, s);
+        if (p.nwin == 8 && spec == rep(W00, 8)) return launch_cfg<8, rep(W00, 8)>(p, n00, n22, s);
+        if (p.nwin == 8 && spec == rep(WPP, 8)) return launch_cfg<8, rep(WPP, 8)>(p, n00, n22, s);
+        return launch_cfg<8, 0>(p, n00, n22, s);
+    }
 }
 
 // (2 l3 + 1) W[l3] in FP64 -> (float mantissa in [0.5, 1), exponent); zeros -> (0, kZeroExp)
