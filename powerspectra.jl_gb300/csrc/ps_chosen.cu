@@ -12,11 +12,11 @@
 //    ~2^-46 relative error instead of FP32's 2^-24;
 //  * the forward (from jmin) and backward (from jmax) sweeps run interleaved
 //    in one loop: two independent dependency chains per lane;
-//  * windows are stored as (mantissa, exponent) pairs.  Every 32 steps each
+//  * windows are stored as (mantissa, exponent) pairs.  Every 64 steps each
 //    warp stages the slice of every window it is about to read into shared
 //    memory, scaled by 2^-E with E the largest exponent of the slice, so FP32
 //    keeps full relative precision whatever the windows' dynamic range
-//    (mask spectra span > 1e-45 at l ~ 8000).  The 32-step FP32 partial sums
+//    (mask spectra span > 1e-45 at l ~ 8000).  The 64-step FP32 partial sums
 //    are added into FP64 totals with the factor 2^E;
 //  * FP64 is kept where stability and range need it: the last forward point,
 //    the least-squares match of the two sweeps, the normalisation, the sign and
@@ -29,8 +29,9 @@
 
 namespace ps {
 
-constexpr int kChunk = 32;               // steps between window restaging / FP64 flushes
+constexpr int kChunk = 64;               // steps between window restaging / FP64 flushes
 constexpr int kSlots = kChunk + 32;      // staged window entries per warp, direction and window
+constexpr int kStagePerLane = kSlots / 32;
 
 __device__ __forceinline__ double pow2d(int e)
 {
@@ -46,17 +47,17 @@ __device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 belo
 // Stage window slots [base, base + kSlots) scaled by 2^-E into dst; returns E.
 __device__ __forceinline__ int stage_slice(float* dst, const int2* __restrict__ bf, int base, int wlen, int lane)
 {
-    int2 v[2];
+    int2 v[kStagePerLane];
     int emax = kZeroExp;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < kStagePerLane; ++q) {
         int j = base + lane + 32 * q;
         v[q] = (j >= 0 && j < wlen) ? __ldg(bf + j) : make_int2(0, kZeroExp);
         emax = max(emax, v[q].y);
     }
     emax = __reduce_max_sync(0xffffffffu, emax);
 #pragma unroll
-    for (int q = 0; q < 2; ++q) dst[lane + 32 * q] = __int_as_float(v[q].x) * pow2f_or_zero(v[q].y - emax);
+    for (int q = 0; q < kStagePerLane; ++q) dst[lane + 32 * q] = __int_as_float(v[q].x) * pow2f_or_zero(v[q].y - emax);
     return emax;
 }
 
