@@ -342,6 +342,149 @@ def run_ours(args):
     return 0
 
 
+SET_CONFIGS = ("batched_64", "large_8191", "cov_2508")
+
+
+def _set_problems(name):
+    """Host-side definition of the multi-matrix configurations.
+
+    batched_64: 64 problems, lmax drawn from {511, ..., 6143}, K in 1..16 seeded mask
+      spectra each, spin 0 (M00 per spectrum) or spin 2 (M++ and M-- per spectrum).
+    large_8191: lmax 8191, nW 16383, K = 20 spectra; spectrum k gives TT (k % 3 == 0),
+      EE = M++ (k % 3 == 1) or BB = M-- (k % 3 == 2): 20 matrices of 8192^2, 10.7 GB.
+    """
+    from powerspectra_gpu import synthetic as syn
+    if name == "batched_64":
+        out = []
+        for pr in syn.batched_problems():
+            out.append({"lmin": 0, "lmax": pr["lmax"], "cases": 0x1 if pr["spin"] == 0 else 0xC,
+                        "nW": pr["lmax"] + 1, "W": pr["W"]})
+        return out
+    if name == "large_8191":
+        big = syn.large_set()
+        groups = {0x1: [], 0x4: [], 0x8: []}
+        for k, W in enumerate(big["W"]):
+            groups[(0x1, 0x4, 0x8)[k % 3]].append(W)
+        return [{"lmin": 0, "lmax": big["lmax"], "cases": c, "nW": big["nW"], "W": Ws} for c, Ws in groups.items()]
+    raise SystemExit("unknown set config %s" % name)
+
+
+def run_set(args):
+    """Secondary configurations (parity-test cases, measured on request): the chosen path
+    against the plain FP64 path on the same device-resident inputs, plus the max relative
+    error of every chosen matrix against its FP64 counterpart."""
+    import numpy as np
+    import torch
+    import powerspectra_gpu as pg
+    from powerspectra_gpu import synthetic as syn
+
+    torch.cuda.set_device(0)
+    ctx = pg.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    keep = []
+
+    def dev(a):
+        t = torch.tensor(np.ascontiguousarray(a), device="cuda")
+        keep.append(t)
+        return t
+
+    def ev_time(fn, steps):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / steps
+
+    line = {"config": {"workload": args.config}, "unit": UNIT}
+    if args.config == "cov_2508":
+        L = 2508
+        ws, spectra, noise = syn.covariance_inputs(L)
+        blocks = syn.COV_BLOCKS
+        n = L + 1
+        jobs, outs_c, outs_p = [], [], []
+        windows = set()
+        for (a, b) in blocks:
+            kind, S, R, Ws = pg.covariance.gather(a, b, ws, spectra, noise)
+            windows.update(id(w) for w in Ws)
+            jobs.append((kind, [dev(x) for x in S], [dev(x) for x in R], [dev(x) for x in Ws]))
+            outs_c.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
+            outs_p.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
+
+        def run(mode, outs):
+            for (kind, S, R, Ws), C in zip(jobs, outs):
+                ctx.coupledcov_device(kind, [x.data_ptr() for x in S], [x.data_ptr() for x in R],
+                                      [x.data_ptr() for x in Ws], n, 0, L, C.data_ptr(), n, mode=mode)
+        elements = len(jobs) * n * n
+        line["config"].update({"lmax": L, "blocks": ["%s%s" % bl for bl in blocks],
+                               "windows": sum(len(j[3]) for j in jobs), "distinct_windows": len(windows)})
+        chosen = lambda: run("chosen", outs_c)
+        plain = lambda: run("plain", outs_p)
+        mats = list(zip(outs_c, outs_p))
+    else:
+        probs = _set_problems(args.config)
+        prob_dev, mats = [], []
+        for pr in probs:
+            n = pr["lmax"] - pr["lmin"] + 1
+            dW = [dev(w) for w in pr["W"]]
+            Mc, Mp, pc, pp = [], [], [], []
+            for k in range(len(dW)):
+                for s_ in range(4):
+                    if pr["cases"] & (1 << s_):
+                        c = torch.empty((n, n), dtype=torch.float64, device="cuda")
+                        q = torch.empty((n, n), dtype=torch.float64, device="cuda") if not args.no_plain else None
+                        Mc.append(c)
+                        mats.append((c, q))
+                        pc.append(c.data_ptr())
+                        pp.append(q.data_ptr() if q is not None else 0)
+                    else:
+                        pc.append(0)
+                        pp.append(0)
+            keep.extend(Mc)
+            prob_dev.append({"lmin": pr["lmin"], "lmax": pr["lmax"], "cases": pr["cases"], "nW": pr["nW"],
+                             "ldm": n, "W": [d.data_ptr() for d in dW], "M": pc, "Mp": pp})
+        elements = sum(int(c.shape[0]) ** 2 for c, _ in mats)
+        tune = ctx.batch_autotune(prob_dev[:min(len(prob_dev), 8)]) if args.config == "batched_64" else None
+        ctx.batch_prepare(prob_dev)
+        chosen = ctx.batch_graph_launch
+
+        def plain():
+            for pr in prob_dev:
+                ctx.mcm_set_device(pr["cases"], pr["W"], pr["nW"], pr["lmin"], pr["lmax"], pr["Mp"], pr["ldm"],
+                                   mode="plain")
+
+        def sequential_chosen():
+            for pr in prob_dev:
+                ctx.mcm_set_device(pr["cases"], pr["W"], pr["nW"], pr["lmin"], pr["lmax"], pr["M"], pr["ldm"],
+                                   mode="chosen")
+        line["config"].update({"problems": len(probs), "matrices": len(mats),
+                               "lmax": sorted(set(p["lmax"] for p in probs)), "autotune": tune})
+        for _ in range(args.warmup):
+            sequential_chosen()
+        line["sequential_chosen"] = {"value": elements / ev_time(sequential_chosen, args.steps), "unit": UNIT}
+    for _ in range(max(args.warmup, 3)):
+        chosen()
+    t_c = ev_time(chosen, args.steps)
+    line.update({"metric": METRIC, "value": elements / t_c, "ms_per_step": t_c * 1e3, "steps": args.steps,
+                 "elements_per_step": elements, "mode": "chosen"})
+    if not args.no_plain:
+        plain()
+        t_p = ev_time(plain, 1)
+        errs = []
+        for c, q in mats:
+            den = torch.maximum(q.abs(), 1e-9 * q.abs().max())
+            den = torch.where(den == 0, torch.ones_like(den), den)
+            errs.append(float(((c - q).abs() / den).max().item()))
+        line["plain_fp64"] = {"value": elements / t_p, "ms_per_step": t_p * 1e3, "steps": 1,
+                              "chosen_over_plain": t_p / t_c, "max_rel_err_chosen_vs_fp64": max(errs)}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,6 +499,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config in SET_CONFIGS:
+        return run_set(args)
     return run_ours(args)
 
 

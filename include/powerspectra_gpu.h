@@ -119,6 +119,46 @@ int ps_coupledcov(ps_ctx *ctx, int kind, const double *const *S, const double *c
 int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const double *const *dR,
                          const double *const *dW, int64_t nW, int lmin, int lmax, int mode, double *dC, int64_t ldc);
 
+/* Many mask spectra on one (l1, l2) grid: for window k and every spin case s
+ * selected in `cases`, dM[4*k + s] receives the matrix (entries of unselected
+ * cases are ignored).  This is `mcm` for a set of spectra (the reference calls
+ * inner_mcm*! once per spectrum and case, src/modecoupling.jl:192-246).  The
+ * (window, case) slots are processed in groups of up to 8 sharing one
+ * generation of the families per pair.  Device pointers; enqueued on the
+ * context stream. */
+int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
+                      int mode, double *const *dM, int64_t ldm);
+
+/* One coupling problem of a batch (device pointers): K spectra of nW entries,
+ * the spin cases to compute for each, and 4*K output slots (entry 4*k + s). */
+typedef struct ps_problem {
+    int lmin, lmax;
+    unsigned cases;
+    int K;
+    int64_t nW;
+    const double *const *W;
+    double *const *M;
+    int64_t ldm;
+} ps_problem;
+
+/* Batched uneven workload in one persistent launch (chosen arithmetic).
+ * The reference has no counterpart: it runs the problems one `mcm` call at a
+ * time.  prepare() splits every problem into window groups of `group_slots`
+ * (window, case) slots, builds one work queue over all problems ordered by
+ * decreasing family length, and uploads the tables; 0 for group_slots or
+ * blocks_per_sm picks the values ps_batch_autotune() found, else defaults.
+ * run() enqueues the window preparation, the queue reset and ONE persistent
+ * kernel.  graph_launch() captures run() into a CUDA graph on first use and
+ * replays it afterwards.  The problems' pointers must stay valid while the
+ * batch is in use. */
+int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);
+int ps_batch_run(ps_ctx *ctx);
+int ps_batch_graph_launch(ps_ctx *ctx);
+/* Times every (group_slots in {2, 4, 8}) x (blocks per SM) configuration on
+ * the given problems, keeps the fastest as the context's default and returns it. */
+int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best_group_slots,
+                      int *best_blocks_per_sm, double *best_ms);
+
 /* Instrumentation: device time of the last coupling kernel (CUDA events on the
  * launching stream), number of kernels this context has launched, and a
  * measured FMA-pipe peak (flop/s, FMA = 2 flops) of this GPU in FP64 (fp64=1)

@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "ps_internal.cuh"
@@ -37,6 +38,19 @@ struct ps_ctx {
     double* d_probe = nullptr;
     int2* d_bf = nullptr;  // split (mantissa, exponent) windows for the chosen kernel
     size_t bf_cap = 0;
+    // batched workload state (ps_batch_*)
+    struct Batch {
+        bool ready = false;
+        int nitems = 0, npreps = 0, max_wlen = 0, group_slots = 4, blocks = 0;
+        ps::CouplingParams* d_groups = nullptr;
+        int4* d_items = nullptr;
+        ps::WinPrep* d_preps = nullptr;
+        unsigned* d_counter = nullptr;
+        double* d_win = nullptr;
+        int2* d_bf = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    } batch;
+    int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
     double last_ms = 0.0;
@@ -230,6 +244,66 @@ static int stage_windows(ps_ctx* c, ps::CouplingParams& p, const double* const* 
     return PS_OK;
 }
 
+static void batch_release(ps_ctx* c)
+{
+    ps_ctx::Batch& b = c->batch;
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    cudaFree(b.d_groups);
+    cudaFree(b.d_items);
+    cudaFree(b.d_preps);
+    cudaFree(b.d_counter);
+    cudaFree(b.d_win);
+    cudaFree(b.d_bf);
+    b = ps_ctx::Batch();
+}
+
+template <typename T>
+static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
+{
+    if (v.empty()) return PS_OK;
+    cudaError_t e = cudaMalloc((void**)dst, v.size() * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *dst = nullptr;
+        return set_err(c, PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", v.size() * sizeof(T), cudaGetErrorString(e));
+    }
+    PS_CUDA(c, cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return PS_OK;
+}
+
+// Split (window, case) slots of one grid into groups of at most `gs` slots.
+struct Slot {
+    int k, s;
+};
+static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs)
+{
+    std::vector<Slot> all;
+    for (int k = 0; k < K; ++k)
+        for (int s = 0; s < 4; ++s)
+            if (cases & (1u << s)) all.push_back(Slot{k, s});
+    std::vector<std::vector<Slot>> out;
+    for (size_t i = 0; i < all.size(); i += (size_t)gs)
+        out.emplace_back(all.begin() + i, all.begin() + std::min(all.size(), i + (size_t)gs));
+    return out;
+}
+
+static int check_problem(ps_ctx* c, const ps_problem& p, int i)
+{
+    if (p.lmin < 0 || p.lmax < p.lmin || p.lmax > PS_MAX_LMAX)
+        return set_err(c, PS_ERR_ARG, "problem %d: need 0 <= lmin <= lmax <= %d", i, PS_MAX_LMAX);
+    if (p.cases == 0 || (p.cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "problem %d: cases mask 0x%x", i, p.cases);
+    if (p.K < 1 || !p.W || !p.M) return set_err(c, PS_ERR_ARG, "problem %d: K >= 1 and W, M arrays required", i);
+    if (p.nW < 1) return set_err(c, PS_ERR_ARG, "problem %d: nW must be >= 1", i);
+    if (p.ldm < p.lmax - p.lmin + 1) return set_err(c, PS_ERR_ARG, "problem %d: ldm too small", i);
+    for (int k = 0; k < p.K; ++k) {
+        if (!p.W[k]) return set_err(c, PS_ERR_ARG, "problem %d: W[%d] is NULL", i, k);
+        for (int s = 0; s < 4; ++s)
+            if ((p.cases & (1u << s)) && !p.M[4 * k + s])
+                return set_err(c, PS_ERR_ARG, "problem %d: M[%d] is NULL", i, 4 * k + s);
+    }
+    return PS_OK;
+}
+
 extern "C" {
 
 int ps_create(int device, ps_ctx** out)
@@ -267,6 +341,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_out);
     cudaFree(c->d_probe);
     cudaFree(c->d_bf);
+    batch_release(c);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -474,6 +549,257 @@ int ps_coupledcov_device(ps_ctx* c, int kind, const double* const* dS, const dou
                          const double* const* dW, int64_t nW, int lmin, int lmax, int mode, double* dC, int64_t ldc)
 {
     return cov_impl(c, kind, dS, dR, dW, nW, lmin, lmax, mode, dC, ldc, false);
+}
+
+int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K, int64_t nW, int lmin, int lmax,
+                      int mode, double* const* dM, int64_t ldm)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldm);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    if (cases == 0 || (cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "cases mask 0x%x must select bits 0..3", cases);
+    if (K < 1 || !dW || !dM) return set_err(c, PS_ERR_ARG, "K >= 1 and W, M arrays required");
+    for (int k = 0; k < K; ++k) {
+        if (!dW[k]) return set_err(c, PS_ERR_ARG, "W[%d] is NULL", k);
+        for (int s = 0; s < 4; ++s)
+            if ((cases & (1u << s)) && !dM[4 * k + s]) return set_err(c, PS_ERR_ARG, "M[%d] is NULL", 4 * k + s);
+    }
+    PS_CUDA(c, cudaSetDevice(c->device));
+    // all K windows are padded (and split) once; each group points into them
+    ps::CouplingParams base;
+    memset(&base, 0, sizeof(base));
+    base.lmin = lmin;
+    base.lmax = lmax;
+    base.epilogue = ps::EPI_MCM;
+    base.nwin = K;
+    {
+        // stage_windows fills base.win[k] for k < K; it needs room for K descriptors
+        std::vector<ps::WinDesc> descs(K);
+        int wlen = 2 * lmax + 2;
+        long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+        if ((st = ensure(c, &c->d_win, &c->win_cap, (size_t)K * wlen))) return st;
+        if (mode == PS_MODE_CHOSEN && (st = ensure_int2(c, &c->d_bf, &c->bf_cap, (size_t)K * wlen))) return st;
+        for (int k = 0; k < K; ++k) {
+            PS_CUDA(c, ps::launch_pad_windows(c->d_win + (size_t)k * wlen, dW[k], nuse, wlen, c->stream));
+            c->launches++;
+            descs[k].wW = c->d_win + (size_t)k * wlen;
+            if (mode == PS_MODE_CHOSEN) {
+                PS_CUDA(c, ps::launch_split_windows(c->d_bf + (size_t)k * wlen, descs[k].wW, wlen, c->stream));
+                c->launches++;
+                descs[k].bf = c->d_bf + (size_t)k * wlen;
+            }
+        }
+        base.wlen = wlen;
+        const int gs = mode == PS_MODE_CHOSEN ? 4 : ps::kMaxWin;
+        for (const auto& grp : group_slots(cases, K, gs)) {
+            ps::CouplingParams p = base;
+            p.nwin = (int)grp.size();
+            for (size_t i = 0; i < grp.size(); ++i) {
+                p.win[i] = descs[grp[i].k];
+                spin_window(grp[i].s, &p.win[i].product, &p.win[i].parity);
+                p.out[i] = dM[4 * grp[i].k + grp[i].s];
+            }
+            p.ldo = ldm;
+            if ((st = run_coupling(c, p, mode))) return st;
+        }
+    }
+    return PS_OK;
+}
+
+int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int bps)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!probs || nprob < 1) return set_err(c, PS_ERR_ARG, "need at least one problem");
+    int st;
+    for (int i = 0; i < nprob; ++i)
+        if ((st = check_problem(c, probs[i], i))) return st;
+    if (gs == 0) gs = c->tuned_group_slots ? c->tuned_group_slots : 4;
+    if (gs != 2 && gs != 4 && gs != 8) return set_err(c, PS_ERR_ARG, "group_slots must be 2, 4 or 8 (got %d)", gs);
+    PS_CUDA(c, cudaSetDevice(c->device));
+    batch_release(c);
+    ps_ctx::Batch& b = c->batch;
+    // window rows
+    std::vector<size_t> row0(nprob);
+    size_t rows = 0;
+    int max_wlen = 0;
+    for (int i = 0; i < nprob; ++i) {
+        row0[i] = rows;
+        int wlen = 2 * probs[i].lmax + 2;
+        rows += (size_t)probs[i].K * wlen;
+        max_wlen = std::max(max_wlen, wlen);
+    }
+    cudaError_t e = cudaMalloc((void**)&b.d_win, rows * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_bf, rows * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b.d_counter, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        batch_release(c);
+        return set_err(c, PS_ERR_OOM, "batch buffers: %s", cudaGetErrorString(e));
+    }
+    std::vector<ps::WinPrep> preps;
+    std::vector<ps::CouplingParams> groups;
+    std::vector<int4> items;
+    std::vector<float> cost;
+    for (int i = 0; i < nprob; ++i) {
+        const ps_problem& P = probs[i];
+        int wlen = 2 * P.lmax + 2;
+        long long nuse = P.nW < (int64_t)(2 * P.lmax + 1) ? P.nW : (int64_t)(2 * P.lmax + 1);
+        std::vector<ps::WinDesc> descs(P.K);
+        for (int k = 0; k < P.K; ++k) {
+            ps::WinPrep w;
+            w.src = P.W[k];
+            w.nW = nuse;
+            w.wW = b.d_win + row0[i] + (size_t)k * wlen;
+            w.bf = b.d_bf + row0[i] + (size_t)k * wlen;
+            w.wlen = wlen;
+            preps.push_back(w);
+            descs[k].wW = w.wW;
+            descs[k].bf = w.bf;
+        }
+        for (const auto& grp : group_slots(P.cases, P.K, gs)) {
+            ps::CouplingParams g;
+            memset(&g, 0, sizeof(g));
+            g.lmin = P.lmin;
+            g.lmax = P.lmax;
+            g.epilogue = ps::EPI_MCM;
+            g.nwin = (int)grp.size();
+            g.wlen = wlen;
+            g.ldo = P.ldm;
+            bool f00 = false, f22 = false;
+            for (size_t q = 0; q < grp.size(); ++q) {
+                g.win[q] = descs[grp[q].k];
+                spin_window(grp[q].s, &g.win[q].product, &g.win[q].parity);
+                g.out[q] = P.M[4 * grp[q].k + grp[q].s];
+                if (g.win[q].product != ps::PROD_22_22) f00 = true;
+                if (g.win[q].product != ps::PROD_00_00) f22 = true;
+            }
+            const int fam = (f00 ? 1 : 0) | (f22 ? 2 : 0);
+            const int gid = (int)groups.size();
+            groups.push_back(g);
+            // items: up to 8 warp tasks (256 consecutive l2) of one row
+            for (int l1 = P.lmin; l1 <= P.lmax; ++l1) {
+                for (int l2 = l1; l2 <= P.lmax; l2 += 256) {
+                    int ntask = std::min(8, (P.lmax - l2) / 32 + 1);
+                    items.push_back(make_int4(gid, l1, l2, ntask | (fam << 8)));
+                    cost.push_back((float)ntask * (2.0f * l1 + 1.0f) * (f22 ? 1.0f : 0.5f));
+                }
+            }
+        }
+    }
+    // longest first
+    std::vector<int> order(items.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int bb) { return cost[a] > cost[bb]; });
+    std::vector<int4> sorted(items.size());
+    for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+    if ((st = dev_upload(c, &b.d_groups, groups)) || (st = dev_upload(c, &b.d_items, sorted)) ||
+        (st = dev_upload(c, &b.d_preps, preps))) {
+        batch_release(c);
+        return st;
+    }
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    int nsm = 0;
+    PS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    int occ = ps::batch_blocks_per_sm(gs);
+    if (bps == 0) bps = c->tuned_blocks_per_sm ? c->tuned_blocks_per_sm : occ;
+    if (bps < 1 || bps > occ) bps = occ;
+    b.nitems = (int)sorted.size();
+    b.npreps = (int)preps.size();
+    b.max_wlen = max_wlen;
+    b.group_slots = gs;
+    b.blocks = nsm * bps;
+    b.ready = true;
+    return PS_OK;
+}
+
+static int batch_enqueue(ps_ctx* c, cudaStream_t s)
+{
+    ps_ctx::Batch& b = c->batch;
+    PS_CUDA(c, ps::launch_prep_windows(b.d_preps, b.npreps, b.max_wlen, s));
+    PS_CUDA(c, cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s));
+    ps::BatchParams bp;
+    bp.groups = b.d_groups;
+    bp.items = b.d_items;
+    bp.nitems = b.nitems;
+    bp.counter = b.d_counter;
+    PS_CUDA(c, cudaEventRecord(c->ev0, s));
+    PS_CUDA(c, ps::launch_batch_chosen(bp, b.group_slots, b.blocks, s));
+    PS_CUDA(c, cudaEventRecord(c->ev1, s));
+    return PS_OK;
+}
+
+int ps_batch_run(ps_ctx* c)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!c->batch.ready) return set_err(c, PS_ERR_ARG, "ps_batch_prepare has not been called");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    int st = batch_enqueue(c, c->stream);
+    if (st) return st;
+    c->launches += 2;
+    c->timed = true;
+    return PS_OK;
+}
+
+int ps_batch_graph_launch(ps_ctx* c)
+{
+    if (!c) return PS_ERR_ARG;
+    ps_ctx::Batch& b = c->batch;
+    if (!b.ready) return set_err(c, PS_ERR_ARG, "ps_batch_prepare has not been called");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    if (!b.exec) {
+        // capture on the context's own stream (a capturable, non-default stream)
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));
+        PS_CUDA(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
+        int st = batch_enqueue(c, c->own_stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return set_err(c, PS_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b.exec = nullptr;
+            return set_err(c, PS_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+    }
+    PS_CUDA(c, cudaGraphLaunch(b.exec, c->stream));
+    c->launches += 2;
+    c->timed = true;
+    return PS_OK;
+}
+
+int ps_batch_autotune(ps_ctx* c, const ps_problem* probs, int nprob, int* best_gs, int* best_bps, double* best_ms)
+{
+    if (!c) return PS_ERR_ARG;
+    const int cand_gs[3] = {2, 4, 8};
+    double best = 1e300;
+    int bg = 4, bb = 0, st;
+    for (int gi = 0; gi < 3; ++gi) {
+        int occ = ps::batch_blocks_per_sm(cand_gs[gi]);
+        for (int bps = 1; bps <= occ; ++bps) {
+            if ((st = ps_batch_prepare(c, probs, nprob, cand_gs[gi], bps))) return st;
+            if ((st = ps_batch_run(c))) return st;  // warm-up
+            if ((st = ps_batch_run(c))) return st;
+            PS_CUDA(c, cudaEventSynchronize(c->ev1));
+            float ms = 0.f;
+            PS_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+            if (ms < best) {
+                best = ms;
+                bg = cand_gs[gi];
+                bb = bps;
+            }
+        }
+    }
+    c->tuned_group_slots = bg;
+    c->tuned_blocks_per_sm = bb;
+    batch_release(c);
+    if (best_gs) *best_gs = bg;
+    if (best_bps) *best_bps = bb;
+    if (best_ms) *best_ms = best;
+    return PS_OK;
 }
 
 int ps_probe_fma_peak(ps_ctx* c, int fp64, double* flops)

@@ -12,11 +12,11 @@
 //    ~2^-46 relative error instead of FP32's 2^-24;
 //  * the forward (from jmin) and backward (from jmax) sweeps run interleaved
 //    in one loop: two independent dependency chains per lane;
-//  * windows are stored as (mantissa, exponent) pairs.  Every 64 steps each
+//  * windows are stored as (mantissa, exponent) pairs.  Every 32 steps each
 //    warp stages the slice of every window it is about to read into shared
 //    memory, scaled by 2^-E with E the largest exponent of the slice, so FP32
 //    keeps full relative precision whatever the windows' dynamic range
-//    (mask spectra span > 1e-45 at l ~ 8000).  The 64-step FP32 partial sums
+//    (mask spectra span > 1e-45 at l ~ 8000).  The 32-step FP32 partial sums
 //    are added into FP64 totals with the factor 2^E;
 //  * FP64 is kept where stability and range need it: the last forward point,
 //    the least-squares match of the two sweeps, the normalisation, the sign and
@@ -29,7 +29,7 @@
 
 namespace ps {
 
-constexpr int kChunk = 64;               // steps between window restaging / FP64 flushes
+constexpr int kChunk = 32;               // steps between window restaging / FP64 flushes
 constexpr int kSlots = kChunk + 32;      // staged window entries per warp, direction and window
 constexpr int kStagePerLane = kSlots / 32;
 
@@ -141,24 +141,20 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
     }
 }
 
+// One warp task: 32 consecutive l2 from l2_0 of row l1.  sF / sB are the
+// warp's shared-memory staging areas ([NWIN][kSlots] floats each).
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
+__device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
+                                            float* sB, const int lane)
 {
-    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
-    const int warp = threadIdx.x >> 5;
-    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    if (gw >= p.ntasks) return;  // warp-uniform
-    const int lane = threadIdx.x & 31;
-    const int2 task = p.tasks[gw];
-    const int l1 = task.x;
-    const int l2raw = task.y + lane;
+    const int l2raw = l2_0 + lane;
     const bool active = l2raw <= p.lmax;
     const int l2 = active ? l2raw : p.lmax;
     const int d = l2 - l1;
     const int jmin = d, jmax = l1 + l2;
     const int T = l1;
     const bool fam22 = N22 && (l1 >= 2);
-    const int jmin0 = task.y - l1, jmax0 = task.y + l1;  // lane 0's ends: lane i reads slot i + step
+    const int jmin0 = l2_0 - l1, jmax0 = l2_0 + l1;  // lane 0's ends: lane i reads slot i + step
 
     double Xi[kMaxWin];
     if (T == 0) {
@@ -178,9 +174,6 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coup
 #pragma unroll
     for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
     double FN0 = 0.0, FN2 = 0.0, BN0 = 0.0, BN2 = 0.0;
-
-    float* sF = &sW[warp][0][0][0];
-    float* sB = &sW[warp][1][0][0];
 
     for (int t0 = 0; t0 < T; t0 += kChunk) {
         int eF[NWIN], eB[NWIN];
@@ -287,6 +280,80 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coup
     if (active) write_pair(p, l1, l2, Xi);
 }
 
+template <int NWIN, bool N00, bool N22, uint32_t SPEC>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
+{
+    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    const int warp = threadIdx.x >> 5;
+    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+    if (gw >= p.ntasks) return;  // warp-uniform
+    const int2 task = p.tasks[gw];
+    chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], threadIdx.x & 31);
+}
+
+// Persistent batched kernel: every warp takes the next item of a work queue
+// ordered by decreasing family length (longest first), across all problems
+// and window groups of the batch, until the queue is empty.  An item is up to
+// 8 warp tasks (256 consecutive l2) of one row of one window group; the
+// group's CouplingParams live in global memory.
+template <int NWIN>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batch_chosen(const BatchParams bp)
+{
+    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    float* sF = &sW[warp][0][0][0];
+    float* sB = &sW[warp][1][0][0];
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = (int)atomicAdd(bp.counter, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= bp.nitems) break;  // every warp leaves once the queue is drained; nothing waits
+        const int4 item = bp.items[it];  // (group, l1, first l2, tasks | families << 8)
+        const CouplingParams& g = bp.groups[item.x];
+        const int ntask = item.w & 0xff, fam = item.w >> 8;
+        for (int q = 0; q < ntask; ++q) {
+            const int l2_0 = item.z + 32 * q;
+            if (fam == 1)
+                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, lane);
+            else if (fam == 2)
+                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, lane);
+            else
+                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, lane);
+            __syncwarp();
+        }
+    }
+}
+
+cudaError_t launch_batch_chosen(const BatchParams& bp, int group_slots, int blocks, cudaStream_t s)
+{
+    if (bp.nitems <= 0) return cudaSuccess;
+    if (group_slots <= 2)
+        k_batch_chosen<2><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
+    else if (group_slots <= 4)
+        k_batch_chosen<4><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
+    else
+        k_batch_chosen<8><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
+    return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(int group_slots)
+{
+    int n = 0;
+    cudaError_t e;
+    if (group_slots <= 2)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<2>, kWarpsPerBlock * 32, 0);
+    else if (group_slots <= 4)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<4>, kWarpsPerBlock * 32, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<8>, kWarpsPerBlock * 32, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
 // families a compile-time window set needs
 constexpr bool spec_needs(uint32_t spec, int nwin, bool fam00)
 {
@@ -372,6 +439,29 @@ __global__ void k_split_windows(int2* __restrict__ dst, const double* __restrict
         double m = (v == 0.0) ? 0.0 : frexp(v, &e);
         dst[j] = (v == 0.0) ? make_int2(0, kZeroExp) : make_int2(__float_as_int((float)m), e);
     }
+}
+
+// All windows of a batch in one launch: pad + premultiply + split.
+__global__ void k_prep_windows(const WinPrep* __restrict__ list, int n)
+{
+    const WinPrep w = list[blockIdx.y];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.wlen; j += gridDim.x * blockDim.x) {
+        double v = (j < w.nW) ? (2.0 * j + 1.0) * w.src[j] : 0.0;
+        w.wW[j] = v;
+        int e = 0;
+        double m = (v == 0.0) ? 0.0 : frexp(v, &e);
+        w.bf[j] = (v == 0.0) ? make_int2(0, kZeroExp) : make_int2(__float_as_int((float)m), e);
+    }
+}
+
+cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    int threads = 256;
+    int bx = (max_wlen + threads - 1) / threads;
+    if (bx > 64) bx = 64;
+    k_prep_windows<<<dim3(bx, n), threads, 0, s>>>(list, n);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_split_windows(int2* dst, const double* wW, int wlen, cudaStream_t s)

@@ -52,7 +52,28 @@ struct CouplingParams {
     const double* R[4];  // covariance noise ratios
 };
 
+// One window of a batch: user spectrum -> padded (2l+1)W row and its split copy.
+struct WinPrep {
+    const double* src;
+    long long nW;
+    double* wW;
+    int2* bf;
+    int wlen;
+};
+
+// Persistent batched launch: groups[item.x] holds the coupling parameters of
+// an item (group, l1, l2_0, families: 1 = 00 only, 2 = 22 only, 3 = both).
+struct BatchParams {
+    const CouplingParams* groups;
+    const int4* items;
+    int nitems;
+    unsigned* counter;  // work-queue head, zeroed before every launch
+};
+
 // Launchers (ps_plain_fp64.cu, ps_chosen.cu).
+cudaError_t launch_batch_chosen(const BatchParams& bp, int group_slots, int blocks, cudaStream_t s);
+int batch_blocks_per_sm(int group_slots);
+cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s);
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_pad_windows(double* dst, const double* src, long long nW, int wlen, cudaStream_t s);

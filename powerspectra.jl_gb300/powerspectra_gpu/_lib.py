@@ -25,7 +25,8 @@ MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_M
 
 # every symbol declared in include/powerspectra_gpu.h
 EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
-           "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_last_kernel_ms",
+           "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
+           "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak")
 
 
@@ -45,6 +46,12 @@ _lib = None
 _lock = threading.RLock()
 _DP = ctypes.POINTER(ctypes.c_double)
 _DPP = ctypes.POINTER(_DP)
+
+
+class PSProblem(ctypes.Structure):
+    """struct ps_problem of include/powerspectra_gpu.h"""
+    _fields_ = [("lmin", ctypes.c_int), ("lmax", ctypes.c_int), ("cases", ctypes.c_uint), ("K", ctypes.c_int),
+                ("nW", ctypes.c_int64), ("W", _DPP), ("M", _DPP), ("ldm", ctypes.c_int64)]
 
 
 def load(path=None):
@@ -81,6 +88,17 @@ def load(path=None):
         lib.ps_coupledcov.restype = ci
         lib.ps_coupledcov_device.argtypes = [vp, ci, _DPP, _DPP, _DPP, i64, ci, ci, ci, _DP, i64]
         lib.ps_coupledcov_device.restype = ci
+        lib.ps_mcm_set_device.argtypes = [vp, ctypes.c_uint, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
+        lib.ps_mcm_set_device.restype = ci
+        lib.ps_batch_prepare.argtypes = [vp, ctypes.POINTER(PSProblem), ci, ci, ci]
+        lib.ps_batch_prepare.restype = ci
+        lib.ps_batch_run.argtypes = [vp]
+        lib.ps_batch_run.restype = ci
+        lib.ps_batch_graph_launch.argtypes = [vp]
+        lib.ps_batch_graph_launch.restype = ci
+        lib.ps_batch_autotune.argtypes = [vp, ctypes.POINTER(PSProblem), ci, ctypes.POINTER(ci), ctypes.POINTER(ci),
+                                          ctypes.POINTER(ctypes.c_double)]
+        lib.ps_batch_autotune.restype = ci
         lib.ps_last_kernel_ms.argtypes = [vp]
         lib.ps_last_kernel_ms.restype = ctypes.c_double
         lib.ps_launch_count.argtypes = [vp]
@@ -199,6 +217,51 @@ class Context:
             ml[s] = int(dMs[s])
         self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
                                                 mode_code(mode), dptr_array(ml), int(ldm)))
+
+    def coupledcov_device(self, kind, dS, dR, dW, nW, lmin, lmax, dC, ldc, mode="chosen"):
+        """Device-pointer covariance block (addresses as ints)."""
+        k = COV_KINDS[kind] if isinstance(kind, str) else int(kind)
+        self.check(self.lib.ps_coupledcov_device(self.handle, k, dptr_array([int(x) for x in dS]),
+                                                 dptr_array([int(x) for x in dR]), dptr_array([int(x) for x in dW]),
+                                                 int(nW), lmin, lmax, mode_code(mode), dptr(int(dC)), int(ldc)))
+
+    def mcm_set_device(self, cases, dW, nW, lmin, lmax, dM, ldm, mode="chosen"):
+        """Many spectra on one grid: dW list of K device addresses, dM list of 4K
+        device addresses (entry 4k+s for spin case s; 0 where unused)."""
+        self.check(self.lib.ps_mcm_set_device(self.handle, int(cases), dptr_array([int(x) for x in dW]), len(dW),
+                                              int(nW), lmin, lmax, mode_code(mode),
+                                              dptr_array([int(x) for x in dM]), int(ldm)))
+
+    def _problems(self, problems):
+        arr = (PSProblem * len(problems))()
+        keep = []
+        for i, pr in enumerate(problems):
+            W = dptr_array([int(x) for x in pr["W"]])
+            M = dptr_array([int(x) for x in pr["M"]])
+            keep += [W, M]
+            arr[i] = PSProblem(int(pr.get("lmin", 0)), int(pr["lmax"]), int(pr["cases"]), len(pr["W"]),
+                               int(pr["nW"]), ctypes.cast(W, _DPP), ctypes.cast(M, _DPP), int(pr["ldm"]))
+        return arr, keep
+
+    def batch_prepare(self, problems, group_slots=0, blocks_per_sm=0):
+        """problems: dicts with lmin, lmax, cases, nW, ldm, W (K device addresses),
+        M (4K device addresses).  Builds the persistent kernel's work queue."""
+        arr, keep = self._problems(problems)
+        self._batch_keep = (arr, keep)  # the library keeps pointers only during prepare, but be safe
+        self.check(self.lib.ps_batch_prepare(self.handle, arr, len(problems), int(group_slots), int(blocks_per_sm)))
+
+    def batch_run(self):
+        self.check(self.lib.ps_batch_run(self.handle))
+
+    def batch_graph_launch(self):
+        self.check(self.lib.ps_batch_graph_launch(self.handle))
+
+    def batch_autotune(self, problems):
+        arr, keep = self._problems(problems)
+        g, b, ms = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_double(0)
+        self.check(self.lib.ps_batch_autotune(self.handle, arr, len(problems), ctypes.byref(g), ctypes.byref(b),
+                                              ctypes.byref(ms)))
+        return {"group_slots": g.value, "blocks_per_sm": b.value, "ms": ms.value}
 
     def xi(self, product, parity, Ws, lmin, lmax, mode="plain"):
         Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]

@@ -100,62 +100,75 @@ def loop_covTTEE(C, TEip, TEiq, TEjq, TEjp, W1, W2, mode="plain", ctx=None):
 
 
 # ---- coupledcov*! wrappers (src/covariance.jl:64-418) ----
-def coupledcovTTTT(C, ws, spectra, nr, mode="plain", ctx=None):
+def gather(ch1, ch2, ws, spectra, nr, planck=True):
+    """(kind, spectra, noise ratios, windows) of the block (ch1, ch2), in the
+    order the reference's coupledcov*! wrapper passes them to its loop_cov*!."""
     i, j, p, q = ws.field_names
     W = ws.window_function_W
-    return loop_covTTTT(C, spectra["TT", i, p], spectra["TT", j, q], spectra["TT", i, q], spectra["TT", j, p],
-                        nr["TT", i, p], nr["TT", j, q], nr["TT", i, q], nr["TT", j, p],
-                        W(NN, NN, i, p, "TT", j, q, "TT"), W(NN, NN, i, q, "TT", j, p, "TT"),
-                        W(NN, "TT", i, p, "TT", j, q, "TT"), W(NN, "TT", j, q, "TT", i, p, "TT"),
-                        W(NN, "TT", i, q, "TT", j, p, "TT"), W(NN, "TT", j, p, "TT", i, q, "TT"),
-                        W("TT", "TT", i, p, "TT", j, q, "TT"), W("TT", "TT", i, q, "TT", j, p, "TT"), mode=mode, ctx=ctx)
+    if (ch1, ch2) == ("TT", "TT"):  # src/covariance.jl:64-88
+        return ("TTTT", [spectra["TT", i, p], spectra["TT", j, q], spectra["TT", i, q], spectra["TT", j, p]],
+                [nr["TT", i, p], nr["TT", j, q], nr["TT", i, q], nr["TT", j, p]],
+                [W(NN, NN, i, p, "TT", j, q, "TT"), W(NN, NN, i, q, "TT", j, p, "TT"),
+                 W(NN, "TT", i, p, "TT", j, q, "TT"), W(NN, "TT", j, q, "TT", i, p, "TT"),
+                 W(NN, "TT", i, q, "TT", j, p, "TT"), W(NN, "TT", j, p, "TT", i, q, "TT"),
+                 W("TT", "TT", i, p, "TT", j, q, "TT"), W("TT", "TT", i, q, "TT", j, p, "TT")])
+    if (ch1, ch2) == ("EE", "EE"):  # src/covariance.jl:125-149
+        return ("EEEE", [spectra["EE", i, p], spectra["EE", j, q], spectra["EE", i, q], spectra["EE", j, p]],
+                [nr["EE", i, p], nr["EE", j, q], nr["EE", i, q], nr["EE", j, p]],
+                [W(NN, NN, i, p, "PP", j, q, "PP"), W(NN, NN, i, q, "PP", j, p, "PP"),
+                 W(NN, "PP", i, p, "PP", j, q, "PP"), W(NN, "PP", j, q, "PP", i, p, "PP"),
+                 W(NN, "PP", i, q, "PP", j, p, "PP"), W(NN, "PP", j, p, "PP", i, q, "PP"),
+                 W("PP", "PP", i, p, "PP", j, q, "PP"), W("PP", "PP", i, q, "PP", j, p, "PP")])
+    if (ch1, ch2) == ("TT", "TE"):  # src/covariance.jl:186-204
+        return ("TTTE", [spectra["TT", i, p], spectra["TT", j, p], spectra["TE", i, q], spectra["TE", j, q]],
+                [nr["TT", i, p], nr["TT", j, p]],
+                [W(NN, NN, i, p, "TT", j, q, "TP"), W(NN, NN, i, q, "TP", j, p, "TT"),
+                 W(NN, "TT", j, q, "TP", i, p, "TT"), W(NN, "TT", i, q, "TP", j, p, "TT")])
+    if (ch1, ch2) == ("TE", "TE"):  # src/covariance.jl:238-257
+        return ("TETE", [spectra["TT", i, p], spectra["EE", j, q], spectra["TE", i, q], spectra["TE", j, p]],
+                [nr["TT", i, p], nr["EE", j, q]],
+                [W(NN, NN, i, p, "TT", j, q, "PP"), W(NN, NN, i, q, "TP", j, p, "PT"),
+                 W(NN, "PP", i, p, "TT", j, q, "PP"), W(NN, "TT", j, q, "PP", i, p, "TT"),
+                 W("TT", "PP", i, p, "TT", j, q, "PP")])
+    if (ch1, ch2) == ("TE", "EE"):  # src/covariance.jl:305-333
+        return ("TEEE_PLANCK" if planck else "TEEE",
+                [spectra["EE", j, q], spectra["EE", j, p], spectra["TE", i, p], spectra["TE", i, q]],
+                [nr["EE", j, q], nr["EE", j, p]],
+                [W(NN, NN, i, p, "TP", j, q, "PP"), W(NN, NN, i, q, "TP", j, p, "PP"),
+                 W(NN, "PP", i, p, "TP", j, q, "PP"), W(NN, "PP", i, q, "TP", j, p, "PP")])
+    if (ch1, ch2) == ("TT", "EE"):  # src/covariance.jl:405-418
+        return ("TTEE", [spectra["TE", i, p], spectra["TE", i, q], spectra["TE", j, q], spectra["TE", j, p]], [],
+                [W(NN, NN, i, p, "TP", j, q, "TP"), W(NN, NN, i, q, "TP", j, p, "TP")])
+    return None
+
+
+def coupledcovTTTT(C, ws, spectra, nr, mode="plain", ctx=None):
+    return _run(*_kind_args(gather("TT", "TT", ws, spectra, nr), C), mode, ctx)
 
 
 def coupledcovEEEE(C, ws, spectra, nr, mode="plain", ctx=None):
-    i, j, p, q = ws.field_names
-    W = ws.window_function_W
-    return loop_covEEEE(C, spectra["EE", i, p], spectra["EE", j, q], spectra["EE", i, q], spectra["EE", j, p],
-                        nr["EE", i, p], nr["EE", j, q], nr["EE", i, q], nr["EE", j, p],
-                        W(NN, NN, i, p, "PP", j, q, "PP"), W(NN, NN, i, q, "PP", j, p, "PP"),
-                        W(NN, "PP", i, p, "PP", j, q, "PP"), W(NN, "PP", j, q, "PP", i, p, "PP"),
-                        W(NN, "PP", i, q, "PP", j, p, "PP"), W(NN, "PP", j, p, "PP", i, q, "PP"),
-                        W("PP", "PP", i, p, "PP", j, q, "PP"), W("PP", "PP", i, q, "PP", j, p, "PP"), mode=mode, ctx=ctx)
+    return _run(*_kind_args(gather("EE", "EE", ws, spectra, nr), C), mode, ctx)
 
 
 def coupledcovTTTE(C, ws, spectra, nr, mode="plain", ctx=None):
-    i, j, p, q = ws.field_names
-    W = ws.window_function_W
-    return loop_covTTTE(C, spectra["TT", i, p], spectra["TT", j, p], spectra["TE", i, q], spectra["TE", j, q],
-                        nr["TT", i, p], nr["TT", j, p],
-                        W(NN, NN, i, p, "TT", j, q, "TP"), W(NN, NN, i, q, "TP", j, p, "TT"),
-                        W(NN, "TT", j, q, "TP", i, p, "TT"), W(NN, "TT", i, q, "TP", j, p, "TT"), mode=mode, ctx=ctx)
+    return _run(*_kind_args(gather("TT", "TE", ws, spectra, nr), C), mode, ctx)
 
 
 def coupledcovTETE(C, ws, spectra, nr, mode="plain", ctx=None):
-    i, j, p, q = ws.field_names
-    W = ws.window_function_W
-    return loop_covTETE(C, spectra["TT", i, p], spectra["EE", j, q], spectra["TE", i, q], spectra["TE", j, p],
-                        nr["TT", i, p], nr["EE", j, q],
-                        W(NN, NN, i, p, "TT", j, q, "PP"), W(NN, NN, i, q, "TP", j, p, "PT"),
-                        W(NN, "PP", i, p, "TT", j, q, "PP"), W(NN, "TT", j, q, "PP", i, p, "TT"),
-                        W("TT", "PP", i, p, "TT", j, q, "PP"), mode=mode, ctx=ctx)
+    return _run(*_kind_args(gather("TE", "TE", ws, spectra, nr), C), mode, ctx)
 
 
 def coupledcovTEEE(C, ws, spectra, nr, planck=True, mode="plain", ctx=None):
-    i, j, p, q = ws.field_names
-    W = ws.window_function_W
-    loop = loop_covTEEE_planck if planck else loop_covTEEE
-    return loop(C, spectra["EE", j, q], spectra["EE", j, p], spectra["TE", i, p], spectra["TE", i, q],
-                nr["EE", j, q], nr["EE", j, p],
-                W(NN, NN, i, p, "TP", j, q, "PP"), W(NN, NN, i, q, "TP", j, p, "PP"),
-                W(NN, "PP", i, p, "TP", j, q, "PP"), W(NN, "PP", i, q, "TP", j, p, "PP"), mode=mode, ctx=ctx)
+    return _run(*_kind_args(gather("TE", "EE", ws, spectra, nr, planck=planck), C), mode, ctx)
 
 
 def coupledcovTTEE(C, ws, spectra, nr, mode="plain", ctx=None):
-    i, j, p, q = ws.field_names
-    W = ws.window_function_W
-    return loop_covTTEE(C, spectra["TE", i, p], spectra["TE", i, q], spectra["TE", j, q], spectra["TE", j, p],
-                        W(NN, NN, i, p, "TP", j, q, "TP"), W(NN, NN, i, q, "TP", j, p, "TP"), mode=mode, ctx=ctx)
+    return _run(*_kind_args(gather("TT", "EE", ws, spectra, nr), C), mode, ctx)
+
+
+def _kind_args(g, C):
+    kind, S, R, Ws = g
+    return kind, C, S, R, Ws
 
 
 def coupledcov(ch1, ch2, workspace, spectra, noiseratios=None, lmin=0, lmax=None, mode="plain", ctx=None):

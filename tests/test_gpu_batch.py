@@ -1,0 +1,121 @@
+"""Many-spectra sets and the persistent batched kernel against the oracle.
+
+ps_mcm_set_device: K windows x spin cases on one grid, in window groups.
+ps_batch_*: uneven problems (different lmax, K, spin cases) in one persistent
+launch, directly and replayed from a CUDA graph; and the autotuner.
+"""
+import numpy as np
+import pytest
+
+from gpu_util import cond_scale, max_err_scaled
+from oracle import oracle as o
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _W(nW, seed, cutoff=None):
+    from powerspectra_gpu import synthetic as syn
+    return syn.mask_spectrum(nW, 0.4 + 0.05 * (seed % 8), cutoff or max(nW / 3.0, 5.0), seed=seed)
+
+
+def _dev(a):
+    return torch.tensor(np.ascontiguousarray(a), device="cuda")
+
+
+@pytest.mark.parametrize("mode,tol", [("plain", 1e-12), ("chosen", 1e-6)])
+def test_mcm_set_device(ctx, mode, tol):
+    L, K = 90, 5
+    Ws = [_W(2 * L + 1, seed=k) for k in range(K)]
+    dW = [_dev(w) for w in Ws]
+    n = L + 1
+    dM = {(k, s): torch.zeros((n, n), dtype=torch.float64, device="cuda") for k in range(K) for s in range(4)}
+    ptrs = [dM[k, s].data_ptr() for k in range(K) for s in range(4)]
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        ctx.mcm_set_device(0xF, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, ptrs, n, mode=mode)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_stream(0)
+    for k in range(K):
+        for s in range(4):
+            got = dM[k, s].cpu().numpy().T
+            ref = o.inner_mcm(s, Ws[k], 0, L)
+            assert max_err_scaled(got, ref, cond_scale(s, Ws[k], 0, L)) < tol, (k, s)
+
+
+def _batch_problems(seed=3):
+    rng = np.random.default_rng(seed)
+    probs, refs = [], []
+    for i in range(7):
+        L = int(rng.choice([40, 77, 128, 200, 255]))
+        K = int(rng.integers(1, 6))
+        cases = [0x1, 0xC, 0xF, 0x2][i % 4]
+        lmin = [0, 0, 2, 0, 5, 0, 0][i]
+        n = L - lmin + 1
+        Ws = [_W(2 * L + 1, seed=100 * i + k) for k in range(K)]
+        dW = [_dev(w) for w in Ws]
+        dM = [torch.zeros((n, n), dtype=torch.float64, device="cuda") if cases & (1 << s) else None
+              for k in range(K) for s in range(4)]
+        probs.append({"lmin": lmin, "lmax": L, "cases": cases, "nW": 2 * L + 1, "ldm": n,
+                      "W": [d.data_ptr() for d in dW], "M": [m.data_ptr() if m is not None else 0 for m in dM],
+                      "_keep": (dW, dM)})
+        refs.append((Ws, lmin, L, cases, dM))
+    return probs, refs
+
+
+def _check(refs, tol=1e-6):
+    for Ws, lmin, L, cases, dM in refs:
+        for k, W in enumerate(Ws):
+            for s in range(4):
+                if cases & (1 << s):
+                    got = dM[4 * k + s].cpu().numpy().T
+                    ref = o.inner_mcm(s, W, lmin, L)
+                    assert max_err_scaled(got, ref, cond_scale(s, W, lmin, L)) < tol, (L, k, s)
+
+
+def test_batch_run_and_graph(ctx):
+    probs, refs = _batch_problems()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        ctx.batch_prepare(probs)
+        ctx.batch_run()
+        torch.cuda.synchronize()
+        _check(refs)
+        for _, _, _, _, dM in refs:
+            for m in dM:
+                if m is not None:
+                    m.zero_()
+        ctx.batch_graph_launch()  # capture + replay
+        ctx.batch_graph_launch()  # replay
+        torch.cuda.synchronize()
+        _check(refs)
+    finally:
+        ctx.set_stream(0)
+
+
+def test_batch_autotune_and_group_sizes(ctx):
+    probs, refs = _batch_problems(seed=9)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        best = ctx.batch_autotune(probs)
+        assert best["group_slots"] in (2, 4, 8) and best["blocks_per_sm"] >= 1 and best["ms"] > 0
+        for gs in (2, 8):
+            ctx.batch_prepare(probs, group_slots=gs)
+            ctx.batch_run()
+            torch.cuda.synchronize()
+            _check(refs)
+    finally:
+        ctx.set_stream(0)
+
+
+def test_batch_argument_errors(ctx):
+    import powerspectra_gpu as pg
+    with pytest.raises(pg.PowerSpectraArgumentError):
+        ctx.batch_run() if False else ctx.batch_prepare([{"lmin": 5, "lmax": 3, "cases": 1, "nW": 10, "ldm": 10,
+                                                           "W": [1], "M": [1, 0, 0, 0]}])
+    with pytest.raises(pg.PowerSpectraArgumentError):
+        ctx.batch_prepare([{"lmin": 0, "lmax": 10, "cases": 1, "nW": 10, "ldm": 11, "W": [0], "M": [1, 0, 0, 0]}])
+    with pytest.raises(pg.PowerSpectraArgumentError):
+        ctx.batch_prepare([{"lmin": 0, "lmax": 10, "cases": 1, "nW": 21, "ldm": 11, "W": [1], "M": [1, 0, 0, 0]}],
+                          group_slots=3)
