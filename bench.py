@@ -225,7 +225,10 @@ def run_ours(args):
     spins = sorted(wl["Ws"])
     mode = args.mode
     ctx = pg.Context(local)
-    stream = torch.cuda.current_stream()
+    # one real (non-default) stream shared by torch and the library, so the CUDA
+    # events below bracket the library's kernels
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
     dW = {s: torch.tensor(wl["Ws"][s], device="cuda") for s in spins}
@@ -380,7 +383,8 @@ def run_set(args):
 
     torch.cuda.set_device(0)
     ctx = pg.Context(0)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     keep = []
 

@@ -129,6 +129,18 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
 
+/* decouple_covmat (src/covariance.jl:8-14): out = B1^-1 * Y * B2^-T for n x n
+ * column-major host matrices Y, B1, B2 (leading dimension ld), by two FP64 LU
+ * factorisations on the GPU (the reference's rdiv! with lu(parent(B)')).  A
+ * singular B1 or B2 returns PS_ERR_ARG. */
+int ps_decouple_covmat(ps_ctx *ctx, const double *Y, const double *B1, const double *B2, int64_t n, int64_t ld,
+                       double *out, int64_t ldout);
+/* x = M \ b for an n x n coupling matrix and nrhs right-hand sides (host,
+ * column-major): the decoupling `M \ pCl` of master (src/modecoupling.jl:358,
+ * src/blockspectralmatrix.jl:124-129), by FP64 LU on the GPU. */
+int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double *b, int nrhs, int64_t ldb, double *x,
+             int64_t ldx);
+
 /* One coupling problem of a batch (device pointers): K spectra of nW entries,
  * the spin cases to compute for each, and 4*K output slots (entry 4*k + s). */
 typedef struct ps_problem {

@@ -13,6 +13,15 @@
 
 #include "ps_internal.cuh"
 
+// Dense solves (ps_linalg.cu)
+struct ps_linalg;
+ps_linalg* ps_linalg_new();
+void ps_linalg_free(ps_linalg* L);
+int ps_linalg_decouple(ps_linalg* L, const double* Y, const double* B1, const double* B2, int n, int64_t ldin,
+                       double* out, int64_t ldout, cudaStream_t s, char* err, size_t errn);
+int ps_linalg_solve(ps_linalg* L, const double* M, int n, int64_t ldm, const double* b, int nrhs, int64_t ldb,
+                    double* x, int64_t ldx, cudaStream_t s, char* err, size_t errn);
+
 // Largest lmax the kernels accept: the integer products in P(j) stay below 2^63
 // and every index stays in 32 bits.
 #define PS_MAX_LMAX 16383
@@ -51,6 +60,7 @@ struct ps_ctx {
         cudaGraphExec_t exec = nullptr;
     } batch;
     int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
+    ps_linalg* la = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
     double last_ms = 0.0;
@@ -342,6 +352,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_probe);
     cudaFree(c->d_bf);
     batch_release(c);
+    ps_linalg_free(c->la);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -800,6 +811,33 @@ int ps_batch_autotune(ps_ctx* c, const ps_problem* probs, int nprob, int* best_g
     if (best_bps) *best_bps = bb;
     if (best_ms) *best_ms = best;
     return PS_OK;
+}
+
+int ps_decouple_covmat(ps_ctx* c, const double* Y, const double* B1, const double* B2, int64_t n, int64_t ld,
+                       double* out, int64_t ldout)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!Y || !B1 || !B2 || !out) return set_err(c, PS_ERR_ARG, "Y, B1, B2 and out must not be NULL");
+    if (n < 1 || n > 65535 || ld < n || ldout < n) return set_err(c, PS_ERR_ARG, "need 1 <= n <= 65535, ld >= n");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->la) c->la = ps_linalg_new();
+    int st = ps_linalg_decouple(c->la, Y, B1, B2, (int)n, ld, out, ldout, c->stream, c->err, sizeof(c->err));
+    if (!st) c->launches += 6;
+    return st;
+}
+
+int ps_solve(ps_ctx* c, const double* M, int64_t n, int64_t ldm, const double* b, int nrhs, int64_t ldb, double* x,
+             int64_t ldx)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!M || !b || !x) return set_err(c, PS_ERR_ARG, "M, b and x must not be NULL");
+    if (n < 1 || n > 65535 || nrhs < 1 || ldm < n || ldb < n || ldx < n)
+        return set_err(c, PS_ERR_ARG, "need 1 <= n <= 65535, nrhs >= 1, leading dimensions >= n");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->la) c->la = ps_linalg_new();
+    int st = ps_linalg_solve(c->la, M, (int)n, ldm, b, nrhs, ldb, x, ldx, c->stream, c->err, sizeof(c->err));
+    if (!st) c->launches += 2;
+    return st;
 }
 
 int ps_probe_fma_peak(ps_ctx* c, int fp64, double* flops)

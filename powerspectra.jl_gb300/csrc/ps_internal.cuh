@@ -82,6 +82,7 @@ cudaError_t launch_split_windows(int2* dst, const double* wW, int wlen, cudaStre
 // Exponent marking an exact zero in the split window arrays.
 constexpr int kZeroExp = -100000;
 cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cudaStream_t s);
+cudaError_t launch_transpose(double* dst, const double* src, int n, cudaStream_t s);
 
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);

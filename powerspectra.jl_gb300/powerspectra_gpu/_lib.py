@@ -27,7 +27,7 @@ MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_M
 EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
            "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
-           "ps_launch_count", "ps_probe_fma_peak")
+           "ps_launch_count", "ps_probe_fma_peak", "ps_decouple_covmat", "ps_solve")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -99,6 +99,10 @@ def load(path=None):
         lib.ps_batch_autotune.argtypes = [vp, ctypes.POINTER(PSProblem), ci, ctypes.POINTER(ci), ctypes.POINTER(ci),
                                           ctypes.POINTER(ctypes.c_double)]
         lib.ps_batch_autotune.restype = ci
+        lib.ps_decouple_covmat.argtypes = [vp, _DP, _DP, _DP, i64, i64, _DP, i64]
+        lib.ps_decouple_covmat.restype = ci
+        lib.ps_solve.argtypes = [vp, _DP, i64, i64, _DP, ci, i64, _DP, i64]
+        lib.ps_solve.restype = ci
         lib.ps_last_kernel_ms.argtypes = [vp]
         lib.ps_last_kernel_ms.restype = ctypes.c_double
         lib.ps_launch_count.argtypes = [vp]
@@ -217,6 +221,28 @@ class Context:
             ml[s] = int(dMs[s])
         self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
                                                 mode_code(mode), dptr_array(ml), int(ldm)))
+
+    def decouple_covmat(self, Y, B1, B2):
+        """B1^-1 Y B2^-T (decouple_covmat, src/covariance.jl:8-14) for square float64 matrices."""
+        Y, B1, B2 = (np.asfortranarray(x, dtype=np.float64) for x in (Y, B1, B2))
+        n = Y.shape[0]
+        if Y.shape != (n, n) or B1.shape != (n, n) or B2.shape != (n, n):
+            raise PowerSpectraArgumentError(PS_ERR_ARG, "decouple_covmat needs three n x n matrices")
+        out = np.empty((n, n), dtype=np.float64, order="F")
+        self.check(self.lib.ps_decouple_covmat(self.handle, dptr(Y), dptr(B1), dptr(B2), n, n, dptr(out), n))
+        return out
+
+    def solve(self, M, b):
+        """M \\ b by LU on the GPU (b: vector or n x nrhs)."""
+        M = np.asfortranarray(M, dtype=np.float64)
+        vec = np.ndim(b) == 1
+        B = np.asfortranarray(np.reshape(b, (len(b), -1)) if vec else b, dtype=np.float64)
+        n = M.shape[0]
+        if M.shape != (n, n) or B.shape[0] != n:
+            raise PowerSpectraArgumentError(PS_ERR_ARG, "solve needs an n x n matrix and n rows of right-hand sides")
+        x = np.empty_like(B, order="F")
+        self.check(self.lib.ps_solve(self.handle, dptr(M), n, n, dptr(B), B.shape[1], n, dptr(x), n))
+        return x[:, 0] if vec else x
 
     def coupledcov_device(self, kind, dS, dR, dW, nW, lmin, lmax, dC, ldc, mode="chosen"):
         """Device-pointer covariance block (addresses as ints)."""

@@ -7,6 +7,9 @@
   w3j_exact.json      arbitrary-precision 3j values (mpmath Racah sum) for the
                       (0 0 0) and (-2 2 0) families at random (l1, l2, l3) up to
                       l = 8191, plus family-edge points.
+  decouple_3x3.json   the 3x3 known answer of the reference's decouple_covmat test
+                      (test/test_covmat.jl:11-17: A, B1, B2 and inv(B1) A inv(B2)'),
+                      parsed from the reference test file.
   oracle_small.npz    oracle matrices (mode coupling, all spin cases, two window
                       lengths; all seven covariance kinds) at small lmax, to pin
                       the oracle against accidental change.
@@ -31,6 +34,21 @@ def make_namaster(ref):
     out = {k: np.loadtxt(os.path.join(d, "mcm_%s_diag.txt" % k)) for k in ("TT", "EE", "TE")}
     np.savez(os.path.join(HERE, "namaster_diag.npz"), **out)
     print("namaster_diag.npz", {k: v.shape for k, v in out.items()})
+
+
+def make_decouple(ref):
+    import re
+    src = open(os.path.join(ref, "test", "test_covmat.jl")).read()
+    mats = {}
+    for name in ("A", "B1", "B2"):
+        m = re.search(r"^\s*%s = \[([^\]]*)\]" % name, src, flags=re.M)
+        rows = [[float(x) for x in r.split()] for r in m.group(1).split(";")]
+        mats[name] = rows
+    A, B1, B2 = (np.array(mats[k]) for k in ("A", "B1", "B2"))
+    want = np.linalg.inv(B1) @ A @ np.linalg.inv(B2).T  # Cref = inv(B1) * (A) * (inv(B2)'), test_covmat.jl:15
+    with open(os.path.join(HERE, "decouple_3x3.json"), "w") as f:
+        json.dump({"A": mats["A"], "B1": mats["B1"], "B2": mats["B2"], "expected": want.tolist()}, f, indent=1)
+    print("decouple_3x3.json")
 
 
 def make_exact():
@@ -102,6 +120,8 @@ if __name__ == "__main__":
     a = ap.parse_args()
     if a.only in ("all", "namaster"):
         make_namaster(a.ref)
+    if a.only in ("all", "decouple"):
+        make_decouple(a.ref)
     if a.only in ("all", "oracle"):
         make_oracle_small()
     if a.only in ("all", "exact"):
