@@ -171,6 +171,24 @@ int ps_batch_graph_launch(ps_ctx *ctx);
 int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best_group_slots,
                       int *best_blocks_per_sm, double *best_ms);
 
+/* No counterpart in the reference: an entry point for callers that may not
+ * allocate device memory -- code whose GPU memory belongs to another allocator
+ * (a framework's pool or a fixed budget) and pipelines that cannot take the
+ * device-wide synchronisation cudaMalloc/cudaFree may cause.  It computes the
+ * same matrices as ps_mcm_multi_device with PS_MODE_CHOSEN (same kernel, same
+ * results) on the caller's current device and `stream` (a cudaStream_t), with
+ * no context and no allocation: its scratch (padded windows and the work list,
+ * 2.6 MB) is a fixed array in the library's device image, which every GPU that
+ * loads the library keeps until the process exits.  Limits: lmax <= 4095 (a
+ * larger lmax returns PS_ERR_ARG); all arguments are checked as for
+ * ps_mcm_multi_device.  The first call on a device looks up the array's device
+ * address, so make that first call before any stream capture.  Every call
+ * rewrites the whole scratch; calls whose GPU work overlaps (other streams or
+ * host threads) share it and race, so serialise them.  Returns a PS_* code
+ * only (there is no context to hold a message). */
+int ps_mcm_multi_device_noalloc(unsigned cases, const double *const dW[4], int64_t nW, int lmin, int lmax,
+                                double *const dM[4], int64_t ldm, void *stream);
+
 /* Instrumentation: device time of the last coupling kernel (CUDA events on the
  * launching stream), number of kernels this context has launched, and a
  * measured FMA-pipe peak (flop/s, FMA = 2 flops) of this GPU in FP64 (fp64=1)

@@ -27,7 +27,7 @@ MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_M
 EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
            "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
-           "ps_launch_count", "ps_probe_fma_peak", "ps_decouple_covmat", "ps_solve")
+           "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve")
 
 
 class PowerSpectraGPUError(RuntimeError):
