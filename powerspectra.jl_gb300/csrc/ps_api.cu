@@ -685,13 +685,14 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
                 if (g.win[q].product != ps::PROD_00_00) f22 = true;
             }
             const int fam = (f00 ? 1 : 0) | (f22 ? 2 : 0);
+            const int tmpl = gs == 4 ? ps::chosen_batch_template(g) : 0;
             const int gid = (int)groups.size();
             groups.push_back(g);
             // items: up to 8 warp tasks (256 consecutive l2) of one row
             for (int l1 = P.lmin; l1 <= P.lmax; ++l1) {
                 for (int l2 = l1; l2 <= P.lmax; l2 += 256) {
                     int ntask = std::min(8, (P.lmax - l2) / 32 + 1);
-                    items.push_back(make_int4(gid, l1, l2, ntask | (fam << 8)));
+                    items.push_back(make_int4(gid, l1, l2, ntask | (fam << 8) | (tmpl << 12)));
                     cost.push_back((float)ntask * (2.0f * l1 + 1.0f) * (f22 ? 1.0f : 0.5f));
                 }
             }

@@ -70,8 +70,10 @@ __device__ __forceinline__ float mul_ff(ff a, ff b)
 
 // Window configuration: 4 bits per window, product + 1 in bits 0-1 (so a used
 // window is never 0) and parity in bits 2-3.  A non-zero SPEC fixes the
-// configuration at compile time (the common mode-coupling and covariance
-// sets); SPEC == 0 reads it from the launch parameters.
+// product and parity of every window slot at compile time (the common
+// mode-coupling and covariance sets); the number of used slots stays a launch
+// parameter (p.nwin <= NWIN), so one instantiation serves every prefix of its
+// slot list.  SPEC == 0 reads the configuration from the launch parameters.
 constexpr uint32_t wspec(int prod, int par) { return (uint32_t)((prod + 1) | (par << 2)); }
 template <uint32_t SPEC>
 __device__ __forceinline__ int wprod(const CouplingParams& p, int k)
@@ -126,7 +128,7 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
         if (N00) n0 = __fmaf_rn(s.w, x00, n0);
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if ((SPEC || k < p.nwin) && wpar<SPEC>(p, k) != PAR_ODD) {
+            if (k < p.nwin && wpar<SPEC>(p, k) != PAR_ODD) {
                 const int pr = wprod<SPEC>(p, k);
                 float x = pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02);
                 c[k] = __fmaf_rn(x, sw[k * kSlots + slot], c[k]);
@@ -135,7 +137,7 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
     } else if (N22) {
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if ((SPEC || k < p.nwin) && wprod<SPEC>(p, k) == PROD_22_22 && wpar<SPEC>(p, k) != PAR_EVEN)
+            if (k < p.nwin && wprod<SPEC>(p, k) == PROD_22_22 && wpar<SPEC>(p, k) != PAR_EVEN)
                 c[k] = __fmaf_rn(x22, sw[k * kSlots + slot], c[k]);
         }
     }
@@ -179,7 +181,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
         int eF[NWIN], eB[NWIN];
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (SPEC || k < p.nwin) {
+            if (k < p.nwin) {
                 eF[k] = stage_slice(sF + k * kSlots, p.win[k].bf, jmin0 + t0, p.wlen, lane);
                 eB[k] = stage_slice(sB + k * kSlots, p.win[k].bf, jmax0 - t0 - kChunk + 1, p.wlen, lane);
             } else {
@@ -232,7 +234,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
         if (N00) FN0 = fma(w, x00, FN0);
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (SPEC || k < p.nwin) {
+            if (k < p.nwin) {
                 const int pr = wprod<SPEC>(p, k), pa = wpar<SPEC>(p, k);
                 double ww = __ldg(p.win[k].wW + jm);
                 if (evenT && pa != PAR_ODD)
@@ -265,7 +267,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
 #pragma unroll
     for (int k = 0; k < kMaxWin; ++k) {
         Xi[k] = 0.0;
-        if (k < NWIN && (SPEC || k < p.nwin)) {
+        if (k < NWIN && k < p.nwin) {
             const int pr = wprod<SPEC>(p, k);
             if (pr == PROD_00_00)
                 Xi[k] = fma(lam0 * lam0, BW[k], FW[k]) * inv0;
@@ -279,6 +281,14 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     }
     if (active) write_pair(p, l1, l2, Xi);
 }
+
+constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
+constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
+constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
+// the window sets of the mode-coupling and covariance entry points
+constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
+constexpr uint32_t S_PPMM = WPP | (WMM << 4);
+constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
 
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
@@ -309,12 +319,22 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
         if (lane == 0) it = (int)atomicAdd(bp.counter, 1u);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= bp.nitems) break;  // every warp leaves once the queue is drained; nothing waits
-        const int4 item = bp.items[it];  // (group, l1, first l2, tasks | families << 8)
+        const int4 item = bp.items[it];  // (group, l1, first l2, tasks | families << 8 | template << 12)
         const CouplingParams& g = bp.groups[item.x];
-        const int ntask = item.w & 0xff, fam = item.w >> 8;
+        const int ntask = item.w & 0xff, fam = (item.w >> 8) & 0xf, tmpl = item.w >> 12;
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
-            if (fam == 1)
+            if (NWIN == 4 && tmpl == 1)
+                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, lane);
+            else if (NWIN == 4 && tmpl == 2)
+                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, lane);
+            else if (NWIN == 4 && tmpl == 3)
+                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, lane);
+            else if (NWIN == 4 && tmpl == 4)
+                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, lane);
+            else if (NWIN == 4 && tmpl == 5)
+                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, lane);
+            else if (fam == 1)
                 chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, lane);
             else if (fam == 2)
                 chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, lane);
@@ -386,48 +406,63 @@ static cudaError_t launch_cfg(const CouplingParams& p, bool n00, bool n22, cudaS
     return cudaGetLastError();
 }
 
-constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
-constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
-constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
-// the window sets of the mode-coupling and covariance entry points
-constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
-constexpr uint32_t S_PPMM = WPP | (WMM << 4);
-constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
+
+// True when the first `nwin` slots of `spec` equal those of the template T.
+static bool spec_fits(uint32_t spec, int nwin, uint32_t T, int TN)
+{
+    if (nwin > TN) return false;
+    for (int k = 0; k < nwin; ++k)
+        if (((spec >> (4 * k)) & 0xfu) != ((T >> (4 * k)) & 0xfu)) return false;
+    return true;
+}
+
+static uint32_t spec_of(const CouplingParams& p)
+{
+    uint32_t spec = 0;
+    for (int k = 0; k < p.nwin && k < 8; ++k) spec |= wspec(p.win[k].product, p.win[k].parity) << (4 * k);
+    return spec;
+}
+
+int chosen_batch_template(const CouplingParams& p)
+{
+    const uint32_t spec = spec_of(p);
+    if (spec_fits(spec, p.nwin, rep(W00, 4), 4)) return 1;
+    if (spec_fits(spec, p.nwin, rep(S_PPMM, 2), 4)) return 2;
+    if (spec_fits(spec, p.nwin, S_MCM4, 4)) return 3;
+    if (spec_fits(spec, p.nwin, rep(WPP, 4), 4)) return 4;
+    if (spec_fits(spec, p.nwin, rep(WMM, 4), 4)) return 5;
+    return 0;
+}
 
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s)
 {
     bool n00 = false, n22 = false;
-    uint32_t spec = 0;
     for (int k = 0; k < p.nwin; ++k) {
         if (p.win[k].product != PROD_22_22) n00 = true;
         if (p.win[k].product != PROD_00_00) n22 = true;
-        spec |= wspec(p.win[k].product, p.win[k].parity) << (4 * k);
     }
+    const uint32_t spec = spec_of(p);
+    const int nw = p.nwin;
     if (p.ntasks <= 0) return cudaSuccess;
-    switch (p.nwin) {
-    case 1:
-        if (spec == W00) return launch_cfg<1, W00>(p, n00, n22, s);
-        if (spec == W02) return launch_cfg<1, W02>(p, n00, n22, s);
-        if (spec == WPP) return launch_cfg<1, WPP>(p, n00, n22, s);
-        if (spec == WMM) return launch_cfg<1, WMM>(p, n00, n22, s);
-        return launch_cfg<1, 0>(p, n00, n22, s);
-    case 2:
-        if (spec == S_PPMM) return launch_cfg<2, S_PPMM>(p, n00, n22, s);
-        if (spec == rep(W00, 2)) return launch_cfg<2, rep(W00, 2)>(p, n00, n22, s);
-        return launch_cfg<2, 0>(p, n00, n22, s);
-    case 3:
-    case 4:
-        if (spec == S_MCM4) return launch_cfg<4, S_MCM4>(p, n00, n22, s);
-        if (spec == rep(W00, 4)) return launch_cfg<4, rep(W00, 4)>(p, n00, n22, s);
-        if (spec == rep(W02, 4)) return launch_cfg<4, rep(W02, 4)>(p, n00, n22, s);
-        if (spec == rep(WPP, 4)) return launch_cfg<4, rep(WPP, 4)>(p, n00, n22, s);
-        return launch_cfg<4, 0>(p, n00, n22, s);
-    default:
-        if (spec == S_TETE) return launch_cfg<5, S_TETE>(p, n00, n22, s);
-        if (p.nwin == 8 && spec == rep(W00, 8)) return launch_cfg<8, rep(W00, 8)>(p, n00, n22, s);
-        if (p.nwin == 8 && spec == rep(WPP, 8)) return launch_cfg<8, rep(WPP, 8)>(p, n00, n22, s);
-        return launch_cfg<8, 0>(p, n00, n22, s);
-    }
+    // the smallest instantiation whose slot list starts with this configuration
+    if (spec_fits(spec, nw, W00, 1)) return launch_cfg<1, W00>(p, n00, n22, s);
+    if (spec_fits(spec, nw, W02, 1)) return launch_cfg<1, W02>(p, n00, n22, s);
+    if (spec_fits(spec, nw, WPP, 1)) return launch_cfg<1, WPP>(p, n00, n22, s);
+    if (spec_fits(spec, nw, WMM, 1)) return launch_cfg<1, WMM>(p, n00, n22, s);
+    if (spec_fits(spec, nw, S_PPMM, 2)) return launch_cfg<2, S_PPMM>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(W00, 4), 4)) return launch_cfg<4, rep(W00, 4)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(S_PPMM, 2), 4)) return launch_cfg<4, rep(S_PPMM, 2)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, S_MCM4, 4)) return launch_cfg<4, S_MCM4>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(W02, 4), 4)) return launch_cfg<4, rep(W02, 4)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(WPP, 4), 4)) return launch_cfg<4, rep(WPP, 4)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(WMM, 4), 4)) return launch_cfg<4, rep(WMM, 4)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, S_TETE, 5)) return launch_cfg<5, S_TETE>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(W00, 8), 8)) return launch_cfg<8, rep(W00, 8)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, rep(WPP, 8), 8)) return launch_cfg<8, rep(WPP, 8)>(p, n00, n22, s);
+    if (nw <= 1) return launch_cfg<1, 0>(p, n00, n22, s);
+    if (nw <= 2) return launch_cfg<2, 0>(p, n00, n22, s);
+    if (nw <= 4) return launch_cfg<4, 0>(p, n00, n22, s);
+    return launch_cfg<8, 0>(p, n00, n22, s);
 }
 
 // (2 l3 + 1) W[l3] in FP64 -> (float mantissa in [0.5, 1), exponent); zeros -> (0, kZeroExp)

@@ -73,6 +73,7 @@ struct BatchParams {
 // Launchers (ps_plain_fp64.cu, ps_chosen.cu).
 cudaError_t launch_batch_chosen(const BatchParams& bp, int group_slots, int blocks, cudaStream_t s);
 int batch_blocks_per_sm(int group_slots);
+int chosen_batch_template(const CouplingParams& p);  // compile-time slot set of a batch group (0: generic)
 cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s);
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s);
