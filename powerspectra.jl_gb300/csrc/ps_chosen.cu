@@ -74,7 +74,7 @@ __device__ __forceinline__ float mul_ff(ff a, ff b)
 // mode-coupling and covariance sets); the number of used slots stays a launch
 // parameter (p.nwin <= NWIN), so one instantiation serves every prefix of its
 // slot list.  SPEC == 0 reads the configuration from the launch parameters.
-constexpr uint32_t wspec(int prod, int par) { return (uint32_t)((prod + 1) | (par << 2)); }
+__host__ __device__ constexpr uint32_t wspec(int prod, int par) { return (uint32_t)((prod + 1) | (par << 2)); }
 template <uint32_t SPEC>
 __device__ __forceinline__ int wprod(const CouplingParams& p, int k)
 {
@@ -282,7 +282,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     if (active) write_pair(p, l1, l2, Xi);
 }
 
-constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
+__host__ __device__ constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
 constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
 constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
 // the window sets of the mode-coupling and covariance entry points
@@ -310,17 +310,28 @@ template <int NWIN>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batch_chosen(const BatchParams bp)
 {
     __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    // each warp's copy of its current group's parameters: read in the inner
+    // loops, so they live in shared memory rather than behind global loads
+    __shared__ CouplingParams sG[kWarpsPerBlock];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     float* sF = &sW[warp][0][0][0];
     float* sB = &sW[warp][1][0][0];
+    int cur = -1;
     for (;;) {
         int it = 0;
         if (lane == 0) it = (int)atomicAdd(bp.counter, 1u);
         it = __shfl_sync(0xffffffffu, it, 0);
         if (it >= bp.nitems) break;  // every warp leaves once the queue is drained; nothing waits
         const int4 item = bp.items[it];  // (group, l1, first l2, tasks | families << 8 | template << 12)
-        const CouplingParams& g = bp.groups[item.x];
+        if (item.x != cur) {
+            const int* src = reinterpret_cast<const int*>(bp.groups + item.x);
+            int* dst = reinterpret_cast<int*>(&sG[warp]);
+            for (int q = lane; q < (int)(sizeof(CouplingParams) / sizeof(int)); q += 32) dst[q] = src[q];
+            cur = item.x;
+            __syncwarp();
+        }
+        const CouplingParams& g = sG[warp];
         const int ntask = item.w & 0xff, fam = (item.w >> 8) & 0xf, tmpl = item.w >> 12;
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
