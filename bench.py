@@ -318,9 +318,14 @@ def run_ours(args):
     kms = statistics.mean(kernel_ms)
     peak = peak64 if mode == "plain" else peak32
     achieved = fl / (kms * 1e-3)
+    # DRAM bytes per launch from one ncu capture of this kernel at this size
+    # (profiles/coupling_chosen_all_spins_3071_dram.md); bench.py cannot run ncu itself
+    traffic = 2.504e8 if (wl["name"] == "all_spins_3071" and mode == "chosen") else None
     roofline = {"bound": "fp64_fma_pipe" if mode == "plain" else "fp32_fma_pipe",
                 "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture of the same kernel "
+                                  "and workload" if traffic else None,
                 "peak_source": "measured live by the library's FMA-chain probe kernel (MEASURED_PEAKS.json has no "
                                "CUDA-core FP64/FP32 figure)",
                 "algorithmic_flops_per_launch": fl, "l3_terms_per_family": terms,

@@ -44,15 +44,35 @@ __device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 belo
     return d < -126 ? 0.0f : __int_as_float((d + 127) << 23);
 }
 
-// Stage window slots [base, base + kSlots) scaled by 2^-E into dst; returns E.
-__device__ __forceinline__ int stage_slice(float* dst, const int2* __restrict__ bf, int base, int wlen, int lane)
+// Window slices move in two stages.  fetch_slice issues asynchronous copies
+// (cp.async, 8 bytes per lane and slot) of the raw (mantissa, exponent) slots
+// [base, base + kSlots) into shared memory; they land while the previous chunk
+// computes.  scale_slice then rescales the raw slice by 2^-E, with E the
+// slice's largest exponent, into the FP32 slots the steps read, and returns E.
+__device__ __forceinline__ void fetch_slice(int2* raw, const int2* __restrict__ bf, int base, int wlen, int lane)
+{
+#pragma unroll
+    for (int q = 0; q < kStagePerLane; ++q) {
+        const int j = base + lane + 32 * q;
+        int2* d = raw + lane + 32 * q;
+        if (j >= 0 && j < wlen) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(d);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(bf + j) : "memory");
+        } else {
+            *d = make_int2(0, kZeroExp);
+        }
+    }
+}
+__device__ __forceinline__ void fetch_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void fetch_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane)
 {
     int2 v[kStagePerLane];
     int emax = kZeroExp;
 #pragma unroll
     for (int q = 0; q < kStagePerLane; ++q) {
-        int j = base + lane + 32 * q;
-        v[q] = (j >= 0 && j < wlen) ? __ldg(bf + j) : make_int2(0, kZeroExp);
+        v[q] = raw[lane + 32 * q];
         emax = max(emax, v[q].y);
     }
     emax = __reduce_max_sync(0xffffffffu, emax);
@@ -147,7 +167,7 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
 // warp's shared-memory staging areas ([NWIN][kSlots] floats each).
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
-                                            float* sB, const int lane)
+                                            float* sB, int2* raw, const int lane)
 {
     const int l2raw = l2_0 + lane;
     const bool active = l2raw <= p.lmax;
@@ -177,18 +197,40 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
     double FN0 = 0.0, FN2 = 0.0, BN0 = 0.0, BN2 = 0.0;
 
+    int2* rF = raw;                  // raw forward slices, [NWIN][kSlots]
+    int2* rB = raw + NWIN * kSlots;  // raw backward slices
+#pragma unroll
+    for (int k = 0; k < NWIN; ++k) {
+        if (k < p.nwin) {
+            fetch_slice(rF + k * kSlots, p.win[k].bf, jmin0, p.wlen, lane);
+            fetch_slice(rB + k * kSlots, p.win[k].bf, jmax0 - kChunk + 1, p.wlen, lane);
+        }
+    }
+    fetch_commit();
     for (int t0 = 0; t0 < T; t0 += kChunk) {
         int eF[NWIN], eB[NWIN];
+        fetch_wait_all();
+        __syncwarp();
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
             if (k < p.nwin) {
-                eF[k] = stage_slice(sF + k * kSlots, p.win[k].bf, jmin0 + t0, p.wlen, lane);
-                eB[k] = stage_slice(sB + k * kSlots, p.win[k].bf, jmax0 - t0 - kChunk + 1, p.wlen, lane);
+                eF[k] = scale_slice(sF + k * kSlots, rF + k * kSlots, lane);
+                eB[k] = scale_slice(sB + k * kSlots, rB + k * kSlots, lane);
             } else {
                 eF[k] = eB[k] = kZeroExp;
             }
         }
         __syncwarp();
+        if (t0 + kChunk < T) {  // the next chunk's slices land while this one computes
+#pragma unroll
+            for (int k = 0; k < NWIN; ++k) {
+                if (k < p.nwin) {
+                    fetch_slice(rF + k * kSlots, p.win[k].bf, jmin0 + t0 + kChunk, p.wlen, lane);
+                    fetch_slice(rB + k * kSlots, p.win[k].bf, jmax0 - t0 - 2 * kChunk + 1, p.wlen, lane);
+                }
+            }
+        }
+        fetch_commit();
         float cF[NWIN], cB[NWIN];
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) cF[k] = cB[k] = 0.0f;
@@ -294,11 +336,13 @@ template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
 {
     __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
     const int warp = threadIdx.x >> 5;
     const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
     if (gw >= p.ntasks) return;  // warp-uniform
     const int2 task = p.tasks[gw];
-    chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], threadIdx.x & 31);
+    chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], &sR[warp][0][0][0],
+                                      threadIdx.x & 31);
 }
 
 // Persistent batched kernel: every warp takes the next item of a work queue
@@ -313,6 +357,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
     // each warp's copy of its current group's parameters: read in the inner
     // loops, so they live in shared memory rather than behind global loads
     __shared__ CouplingParams sG[kWarpsPerBlock];
+    __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     float* sF = &sW[warp][0][0][0];
@@ -336,21 +381,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
             if (NWIN == 4 && tmpl == 1)
-                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (NWIN == 4 && tmpl == 2)
-                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (NWIN == 4 && tmpl == 3)
-                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (NWIN == 4 && tmpl == 4)
-                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (NWIN == 4 && tmpl == 5)
-                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (fam == 1)
-                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else if (fam == 2)
-                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             else
-                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, lane);
+                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
             __syncwarp();
         }
     }
