@@ -425,3 +425,49 @@ int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, co
     free(buf);
     return st;
 }
+
+/* quickpolXi! (src/beam.jl:72-109): for l'' = 2..lmax and l in the band
+ * max(2, l''-bl) .. min(lmax, l''+bu), Xi[l'', l] = sgn * sum_l' W[l'] f1(l') f2(l')
+ * with f_k(l') = (l' l l''; s_k+nu_k, -s_k, -nu_k) over the common support of the
+ * two families (Xisum, src/beam.jl:17-28), W[l'] = 0 for l' >= nW, and
+ * sgn = (-1)^(s1+s2+nu1+nu2).  Xi is dense column-major (lmax+1)^2; entries
+ * outside the band are left untouched. */
+int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
+                   long ldx, int nthreads)
+{
+    if (lmax < 0 || bl < 0 || bu < 0 || ldx < lmax + 1) return 1;
+    int nt = nthreads_or_default(nthreads);
+    int blen = 2 * lmax + 2;
+    int err = 0;
+    const double sgn = ((s1 + s2 + nu1 + nu2) % 2 == 0) ? 1.0 : -1.0;
+#pragma omp parallel num_threads(nt)
+    {
+        double *f1 = (double *)malloc(sizeof(double) * (size_t)blen);
+        double *f2 = (double *)malloc(sizeof(double) * (size_t)blen);
+        if (!f1 || !f2) {
+#pragma omp atomic write
+            err = 2;
+        }
+#pragma omp for schedule(dynamic, 1)
+        for (int lpp = 2; lpp <= lmax; ++lpp) {
+            if (!f1 || !f2) continue;
+            int lo = lpp - bl > 2 ? lpp - bl : 2, hi = lpp + bu < lmax ? lpp + bu : lmax;
+            for (int l = lo; l <= hi; ++l) {
+                /* (l' l l''; s+nu, -s, -nu) = (l l'' l'; -s, -nu, s+nu): the family over the third column */
+                int j1, j2;
+                int n1 = or_w3j_family(l, lpp, -s1, -nu1, f1, &j1);
+                int n2 = or_w3j_family(l, lpp, -s2, -nu2, f2, &j2);
+                int a = j1 > j2 ? j1 : j2;
+                int b1 = j1 + n1 - 1, b2 = j2 + n2 - 1;
+                int b = b1 < b2 ? b1 : b2;
+                if (b > nW - 1) b = (int)(nW - 1);
+                double acc = 0.0;
+                for (int lp = a; lp <= b; ++lp) acc += W[lp] * f1[lp - j1] * f2[lp - j2];
+                Xi[(long)lpp + (long)l * ldx] = sgn * acc;
+            }
+        }
+        free(f1);
+        free(f2);
+    }
+    return err;
+}

@@ -36,6 +36,11 @@ int or_inner_mcm_abs(int spin, const double *W, long nW, int lmin, int lmax, dou
 int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, const double *const *W, long nW,
                     int lmin, int lmax, double *C, long ldc, const int *rows, int nrows, int nthreads);
 
+/* quickpolXi! (src/beam.jl:72-109) into a dense column-major (lmax+1)^2 Xi,
+ * rows l'' = 2..lmax, columns l within the band [l''-bl, l''+bu], l >= 2. */
+int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
+                   long ldx, int nthreads);
+
 int or_cov_nwindows(int kind);
 int or_max_threads(void);
 double or_l3_terms(int lmin, int lmax, long nW, const int *rows, int nrows);

@@ -53,6 +53,8 @@ def _load():
         lib.or_loop_cov_abs.argtypes = [ci, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp), cl, ci, ci, dp,
                                         cl, ip, ci, ci]
         lib.or_loop_cov_abs.restype = ci
+        lib.or_quickpol_xi.argtypes = [ci, ci, ci, ci, dp, cl, ci, ci, ci, dp, cl, ci]
+        lib.or_quickpol_xi.restype = ci
         lib.or_xi.argtypes = [ci, ci, dp, cl, ci, ci, dp, cl, ci]
         lib.or_xi.restype = ci
         lib.or_loop_cov.argtypes = [ci, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp), cl, ci, ci, dp, cl,
@@ -151,3 +153,16 @@ def l3_terms(lmin, lmax, nW, rows=None):
     """l3-terms of one family summed over the (l1 <= l2) pairs of the rows, l3 <= nW-1."""
     r, rp, nr = _rows(rows)
     return _load().or_l3_terms(lmin, lmax, nW, rp, nr)
+
+
+def quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, nthreads=0):
+    """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band."""
+    lib = _load()
+    W = np.ascontiguousarray(W, dtype=np.float64)
+    n = lmax + 1
+    X = np.zeros((n, n), dtype=np.float64, order="F")
+    st = lib.or_quickpol_xi(int(nu1), int(nu2), int(s1), int(s2), _dptr(W), len(W), lmax, bl, bu, _dptr(X), n,
+                            nthreads)
+    if st:
+        raise RuntimeError("oracle quickpol_xi failed (%d)" % st)
+    return X

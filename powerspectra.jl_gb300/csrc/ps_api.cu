@@ -698,10 +698,15 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
             }
         }
     }
-    // longest first
+    // items of one kernel body together (warps of an SM then share their
+    // instruction stream), longest first within each body
     std::vector<int> order(items.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int bb) { return cost[a] > cost[bb]; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int bb) {
+        const int ta = items[a].w >> 8, tb = items[bb].w >> 8;  // template and families
+        if (ta != tb) return ta < tb;
+        return cost[a] > cost[bb];
+    });
     std::vector<int4> sorted(items.size());
     for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
     if ((st = dev_upload(c, &b.d_groups, groups)) || (st = dev_upload(c, &b.d_items, sorted)) ||

@@ -6,10 +6,13 @@
 // contracted on the fly; see ps_plain_fp64.cu for the recurrence), with the
 // arithmetic moved off the FP64 pipe:
 //
-//  * recurrence state and coefficients are float-float values (ps_ff.cuh):
-//    P(j) is formed exactly from its four integer factors, 1/sqrt(P) by an
-//    FP32 estimate plus one compensated Newton step, so each step carries
-//    ~2^-46 relative error instead of FP32's 2^-24;
+//  * recurrence state and coefficients are float-float values (ps_ff.cuh), so
+//    each step carries ~2^-46 relative error instead of FP32's 2^-24.  The
+//    step factors a(j)/a(j+1) and 1/a(j+1) split into a lane-uniform part and
+//    a part shared along u = 2i + t (see "coefficient tables" below); each
+//    chunk the warp tabulates both as float-float square-root ratios formed
+//    from exact integer products (FP32 1/sqrt estimate plus one compensated
+//    Newton step), and every step multiplies two table entries;
 //  * the forward (from jmin) and backward (from jmax) sweeps run interleaved
 //    in one loop: two independent dependency chains per lane;
 //  * windows are stored as (mantissa, exponent) pairs.  Every 32 steps each
@@ -165,9 +168,115 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
 
 // One warp task: 32 consecutive l2 from l2_0 of row l1.  sF / sB are the
 // warp's shared-memory staging areas ([NWIN][kSlots] floats each).
+// ---- coefficient tables ----------------------------------------------------
+// For lane i of a warp task (l1, l2_0 + i) the recurrence coefficient at
+// forward step t factorises as P = G(t) F(u), u = 2i + t, with
+//   G(t) = t (2 l1 + 1 - t)             (the same for every lane)
+//   F(u) = (2 d0 + u)(2 l2_0 + 1 + u)   (d0 = l2_0 - l1, shared along u)
+// and at backward step t as P' = G'(t) F'(v), v = 2i - t, with
+//   G'(t) = (2 l1 - t)(1 + t),  F'(v) = (2 l2_0 + v)(2 l1 + 2 l2_0 + 1 + v).
+// So the step factors rho = a(j)/a(j+1) and 1/a(j+1) are products of a
+// lane-uniform G factor and a shared F factor.  Once per chunk the warp
+// tabulates these square-root ratios in shared memory (each lane a few
+// entries), and every step then costs two float-float products instead of a
+// float-float P, 1/sqrt(P) and a(j).
+constexpr int kFEnt = kChunk / 2 + 32;  // F entries per parity of u (or v)
+struct CoefTab {
+    ff gF_rho[kChunk], gF_r[kChunk];    // forward: sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))
+    ff fF_rho[2][kFEnt], fF_r[2][kFEnt];  // forward: sqrt(F(u)/F(u+1)), 1/sqrt(F(u+1))
+    ff gB_rho[kChunk], gB_r[kChunk];    // backward: sqrt(G'(t-1)/G'(t)), 1/sqrt(G'(t))
+    ff fB_rho[2][kFEnt], fB_r[2][kFEnt];  // backward: sqrt(F'(v+1)/F'(v)), 1/sqrt(F'(v))
+};
+
+// rho = sqrt(X / Y) and r = 1 / sqrt(Y) for X >= 0, Y > 0 (float-float)
+__device__ __forceinline__ void sqrt_ratio(ff X, ff Y, ff& rho, ff& r)
+{
+    r = ff_rsqrt(Y);
+    rho = X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
+}
+
+__device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1, int l2_0, int lane)
+{
+    const ff zero = ff_make(0.0f);
+    {
+        const int ti = t0 + lane;
+        const float t = (float)ti;
+        ff a, b;
+        if (ti < T) {
+            sqrt_ratio(two_prod(t, (float)(2 * l1 + 1) - t), two_prod(t + 1.0f, (float)(2 * l1) - t), a, b);
+            tb.gF_rho[lane] = a;
+            tb.gF_r[lane] = b;
+            sqrt_ratio(two_prod((float)(2 * l1 + 1) - t, t), two_prod((float)(2 * l1) - t, 1.0f + t), a, b);
+            tb.gB_rho[lane] = a;
+            tb.gB_r[lane] = b;
+        } else {
+            tb.gF_rho[lane] = tb.gF_r[lane] = tb.gB_rho[lane] = tb.gB_r[lane] = zero;
+        }
+    }
+    const int d0 = l2_0 - l1;
+#pragma unroll
+    for (int q = 0; q < (2 * kFEnt + 31) / 32; ++q) {
+        const int e = lane + 32 * q;
+        if (e >= 2 * kFEnt) break;
+        ff a = zero, b = zero;
+        {   // forward, u = t0 + e
+            const float u = (float)(t0 + e);
+            sqrt_ratio(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
+                       two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u), a, b);
+            tb.fF_rho[e & 1][e >> 1] = a;
+            tb.fF_r[e & 1][e >> 1] = b;
+        }
+        {   // backward, v = e - t0 - 31
+            const int v = e - t0 - (kChunk - 1);
+            if (2 * l2_0 + v > 0) {
+                const float fv = (float)v;
+                sqrt_ratio(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
+                           two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv), a, b);
+            } else {
+                a = b = zero;
+            }
+            tb.fB_rho[e & 1][e >> 1] = a;
+            tb.fB_r[e & 1][e >> 1] = b;
+        }
+    }
+}
+
+// One table-driven step: f(next) = -(c (2j+1) f(cur) r + rho f(prev)), c = 4.
+template <bool N00, bool N22, bool ODD_STEP>
+__device__ __forceinline__ void tab_step(Sweep& s, ff rho, ff r, float dw)
+{
+    if (N22) {
+        ff u = ff_mul_raw(ff_mul_raw(s.f2, ff_make(4.0f * s.w)), r);
+        ff v = ff_mul_raw(rho, s.f2o);
+        ff nf = ff_neg(ff_add(u, v));
+        s.f2o = s.f2;
+        s.f2 = nf;
+    }
+    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul(rho, s.f0));
+    s.w += dw;
+}
+
+template <bool N00, bool N22, bool ODD_STEP>
+__device__ __forceinline__ void tab_fwd(Sweep& s, const CoefTab& tb, int st, int lane)
+{
+    const int e = 2 * lane + st;  // u - t0
+    ff rho = ff_mul_raw(tb.gF_rho[st], tb.fF_rho[e & 1][e >> 1]);
+    ff r = ff_mul_raw(tb.gF_r[st], tb.fF_r[e & 1][e >> 1]);
+    tab_step<N00, N22, ODD_STEP>(s, rho, r, 2.0f);
+}
+
+template <bool N00, bool N22, bool ODD_STEP>
+__device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int lane)
+{
+    const int e = 2 * lane - st + (kChunk - 1);  // v - (-t0 - 31)
+    ff rho = ff_mul_raw(tb.gB_rho[st], tb.fB_rho[e & 1][e >> 1]);
+    ff r = ff_mul_raw(tb.gB_r[st], tb.fB_r[e & 1][e >> 1]);
+    tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
+}
+
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
-                                            float* sB, int2* raw, const int lane)
+                                            float* sB, int2* raw, CoefTab& tb, const int lane)
 {
     const int l2raw = l2_0 + lane;
     const bool active = l2raw <= p.lmax;
@@ -220,6 +329,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
                 eF[k] = eB[k] = kZeroExp;
             }
         }
+        build_tables(tb, t0, T, l1, l2_0, lane);
         __syncwarp();
         if (t0 + kChunk < T) {  // the next chunk's slices land while this one computes
 #pragma unroll
@@ -240,18 +350,18 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
         for (; s + 1 < steps; s += 2) {
             sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            sweep_step<N00, N22, false>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
-            sweep_step<N00, N22, false>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
+            tab_fwd<N00, N22, false>(F, tb, s, lane);
+            tab_bwd<N00, N22, false>(B, tb, s, lane);
             sweep_acc<NWIN, N00, N22, SPEC, false>(p, F, sF, lane + s + 1, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, false>(p, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
-            sweep_step<N00, N22, true>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
-            sweep_step<N00, N22, true>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
+            tab_fwd<N00, N22, true>(F, tb, s + 1, lane);
+            tab_bwd<N00, N22, true>(B, tb, s + 1, lane);
         }
         if (s < steps) {  // one even step left (T odd, last chunk)
             sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            sweep_step<N00, N22, false>(F, 1.0f, 1.0f, -1.0f, 1.0f, 2.0f);
-            sweep_step<N00, N22, false>(B, -1.0f, -1.0f, 1.0f, -1.0f, -2.0f);
+            tab_fwd<N00, N22, false>(F, tb, s, lane);
+            tab_bwd<N00, N22, false>(B, tb, s, lane);
         }
         // ---- FP64 flush of the chunk sums ----
 #pragma unroll
@@ -290,11 +400,16 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     const double gm0 = ff_to_double(F.f2);
     double gm1 = 0.0, g0s;
     {
-        ff P = ff_mul_raw(two_prod(F.A, F.B), two_prod(F.C, F.D));
-        ff r = ff_rsqrt(P);
-        if (N22) gm1 = ff_to_double(ff_neg(ff_mul(ff_add(ff_mul_raw(F.f2, ff_make(4.0f * F.w)), ff_mul_raw(F.a, F.f2o)), r)));
-        g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(ff_mul_raw(F.a, r), F.f0))) : ff_to_double(F.f0);
+        // P(jm) = T(2d+T)(2l1+1-T)(2l2+1+T), P(jm+1) = (T+1)(2d+T+1)(2l1-T)(2l2+2+T)
+        const float fT = (float)T;
+        ff P0 = ff_mul_raw(two_prod(fT, (float)(2 * d) + fT), two_prod((float)(2 * l1 + 1) - fT, (float)(2 * l2 + 1) + fT));
+        ff P1 = ff_mul_raw(two_prod(fT + 1.0f, (float)(2 * d + 1) + fT), two_prod((float)(2 * l1) - fT, (float)(2 * l2 + 2) + fT));
+        ff rho, r;
+        sqrt_ratio(P0, P1, rho, r);
+        if (N22) gm1 = ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mul_raw(F.f2, ff_make(4.0f * F.w)), r), ff_mul_raw(rho, F.f2o))));
+        g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(rho, F.f0))) : ff_to_double(F.f0);
     }
+
     const double hm0 = ff_to_double(B.f2), hm1 = ff_to_double(B.f2o), h0s = ff_to_double(B.f0);
 
     // match, normalise, sign (FP64)
@@ -337,12 +452,13 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coup
 {
     __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
     __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
+    __shared__ CoefTab sT[kWarpsPerBlock];
     const int warp = threadIdx.x >> 5;
     const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
     if (gw >= p.ntasks) return;  // warp-uniform
     const int2 task = p.tasks[gw];
     chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], &sR[warp][0][0][0],
-                                      threadIdx.x & 31);
+                                      sT[warp], threadIdx.x & 31);
 }
 
 // Persistent batched kernel: every warp takes the next item of a work queue
@@ -358,6 +474,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
     // loops, so they live in shared memory rather than behind global loads
     __shared__ CouplingParams sG[kWarpsPerBlock];
     __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
+    __shared__ CoefTab sT[kWarpsPerBlock];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     float* sF = &sW[warp][0][0][0];
@@ -381,21 +498,21 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
             if (NWIN == 4 && tmpl == 1)
-                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (NWIN == 4 && tmpl == 2)
-                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (NWIN == 4 && tmpl == 3)
-                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (NWIN == 4 && tmpl == 4)
-                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (NWIN == 4 && tmpl == 5)
-                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (fam == 1)
-                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else if (fam == 2)
-                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             else
-                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], lane);
+                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
             __syncwarp();
         }
     }
