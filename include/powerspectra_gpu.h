@@ -141,6 +141,19 @@ int ps_decouple_covmat(ps_ctx *ctx, const double *Y, const double *B1, const dou
 int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double *b, int nrhs, int64_t ldb, double *x,
              int64_t ldx);
 
+/* QuickPol beam coupling (quickpolXi!, src/beam.jl:72-109): for l'' = 2..lmax
+ * and l in [max(2, l''-bl), min(lmax, l''+bu)],
+ *   Xi[l'', l] = (-1)^(s1+s2+nu1+nu2) sum_l' W[l'] (l' l l''; s1+nu1, -s1, -nu1)
+ *                                                 (l' l l''; s2+nu2, -s2, -nu2)
+ * over the two families' common support (Xisum, src/beam.jl:17-28), W[l'] = 0
+ * for l' >= nW.  W is the scan-pattern spectrum (quickpolW); Xi is a dense
+ * column-major (lmax+1) x (lmax+1) matrix (ld >= lmax+1) that receives the
+ * band and zeros elsewhere.  FP64, general spins; host pointers.  The
+ * reference stores Xi as a BandedMatrix; here the band is written into a dense
+ * matrix. */
+int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *W, int64_t nW, int lmax, int bl,
+                   int bu, double *Xi, int64_t ldx);
+
 /* One coupling problem of a batch (device pointers): K spectra of nW entries,
  * the spin cases to compute for each, and 4*K output slots (entry 4*k + s). */
 typedef struct ps_problem {
@@ -155,10 +168,12 @@ typedef struct ps_problem {
 
 /* Batched uneven workload in one persistent launch (chosen arithmetic).
  * The reference has no counterpart: it runs the problems one `mcm` call at a
- * time.  prepare() splits every problem into window groups of `group_slots`
- * (window, case) slots, builds one work queue over all problems ordered by
- * decreasing family length, and uploads the tables; 0 for group_slots or
- * blocks_per_sm picks the values ps_batch_autotune() found, else defaults.
+ * time.  prepare() splits every problem into window groups of up to
+ * `group_slots` (2 or 4) (window, case) slots -- whole windows per group, so
+ * the ++ and -- of one spectrum share their family -- builds one work queue
+ * over all problems ordered by kernel body and decreasing family length, and
+ * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
+ * ps_batch_autotune() found, else defaults.
  * run() enqueues the window preparation, the queue reset and ONE persistent
  * kernel.  graph_launch() captures run() into a CUDA graph on first use and
  * replays it afterwards.  The problems' pointers must stay valid while the
@@ -166,7 +181,7 @@ typedef struct ps_problem {
 int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);
 int ps_batch_run(ps_ctx *ctx);
 int ps_batch_graph_launch(ps_ctx *ctx);
-/* Times every (group_slots in {2, 4, 8}) x (blocks per SM) configuration on
+/* Times every (group_slots in {2, 4}) x (blocks per SM) configuration on
  * the given problems, keeps the fastest as the context's default and returns it. */
 int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best_group_slots,
                       int *best_blocks_per_sm, double *best_ms);

@@ -297,6 +297,31 @@ static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs)
     return out;
 }
 
+// Batch groups hold whole windows in one of the per-window slot patterns the
+// persistent kernel has a compile-time body for (TT, TE, ++, --, ++/-- pairs,
+// TT/TE/++/--); any other combination of cases is split case by case.
+static std::vector<std::vector<Slot>> batch_group_slots(unsigned cases, int K, int gs)
+{
+    std::vector<std::vector<Slot>> out;
+    auto pack = [&](unsigned cs) {
+        int per = __builtin_popcount(cs);
+        int wpg = per >= gs ? 1 : gs / per;  // windows per group
+        for (int k0 = 0; k0 < K; k0 += wpg) {
+            std::vector<Slot> g;
+            for (int k = k0; k < std::min(K, k0 + wpg); ++k)
+                for (int s = 0; s < 4; ++s)
+                    if (cs & (1u << s)) g.push_back(Slot{k, s});
+            out.push_back(g);
+        }
+    };
+    if (cases == 0x1 || cases == 0x2 || cases == 0x4 || cases == 0x8 || cases == 0xC || (cases == 0xF && gs >= 4))
+        pack(cases);
+    else
+        for (int s = 0; s < 4; ++s)
+            if (cases & (1u << s)) pack(1u << s);
+    return out;
+}
+
 static int check_problem(ps_ctx* c, const ps_problem& p, int i)
 {
     if (p.lmin < 0 || p.lmax < p.lmin || p.lmax > PS_MAX_LMAX)
@@ -625,7 +650,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     for (int i = 0; i < nprob; ++i)
         if ((st = check_problem(c, probs[i], i))) return st;
     if (gs == 0) gs = c->tuned_group_slots ? c->tuned_group_slots : 4;
-    if (gs != 2 && gs != 4 && gs != 8) return set_err(c, PS_ERR_ARG, "group_slots must be 2, 4 or 8 (got %d)", gs);
+    if (gs != 2 && gs != 4) return set_err(c, PS_ERR_ARG, "group_slots must be 2 or 4 (got %d)", gs);
     PS_CUDA(c, cudaSetDevice(c->device));
     batch_release(c);
     ps_ctx::Batch& b = c->batch;
@@ -667,7 +692,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
             descs[k].wW = w.wW;
             descs[k].bf = w.bf;
         }
-        for (const auto& grp : group_slots(P.cases, P.K, gs)) {
+        for (const auto& grp : batch_group_slots(P.cases, P.K, gs)) {
             ps::CouplingParams g;
             memset(&g, 0, sizeof(g));
             g.lmin = P.lmin;
@@ -685,7 +710,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
                 if (g.win[q].product != ps::PROD_00_00) f22 = true;
             }
             const int fam = (f00 ? 1 : 0) | (f22 ? 2 : 0);
-            const int tmpl = gs == 4 ? ps::chosen_batch_template(g) : 0;
+            const int tmpl = ps::chosen_batch_template(g);
             const int gid = (int)groups.size();
             groups.push_back(g);
             // items: up to 8 warp tasks (256 consecutive l2) of one row
@@ -717,7 +742,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     int nsm = 0;
     PS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    int occ = ps::batch_blocks_per_sm(gs);
+    int occ = ps::batch_blocks_per_sm();
     if (bps == 0) bps = c->tuned_blocks_per_sm ? c->tuned_blocks_per_sm : occ;
     if (bps < 1 || bps > occ) bps = occ;
     b.nitems = (int)sorted.size();
@@ -740,7 +765,7 @@ static int batch_enqueue(ps_ctx* c, cudaStream_t s)
     bp.nitems = b.nitems;
     bp.counter = b.d_counter;
     PS_CUDA(c, cudaEventRecord(c->ev0, s));
-    PS_CUDA(c, ps::launch_batch_chosen(bp, b.group_slots, b.blocks, s));
+    PS_CUDA(c, ps::launch_batch_chosen(bp, b.blocks, s));
     PS_CUDA(c, cudaEventRecord(c->ev1, s));
     return PS_OK;
 }
@@ -791,11 +816,11 @@ int ps_batch_graph_launch(ps_ctx* c)
 int ps_batch_autotune(ps_ctx* c, const ps_problem* probs, int nprob, int* best_gs, int* best_bps, double* best_ms)
 {
     if (!c) return PS_ERR_ARG;
-    const int cand_gs[3] = {2, 4, 8};
+    const int cand_gs[2] = {2, 4};
     double best = 1e300;
     int bg = 4, bb = 0, st;
-    for (int gi = 0; gi < 3; ++gi) {
-        int occ = ps::batch_blocks_per_sm(cand_gs[gi]);
+    for (int gi = 0; gi < 2; ++gi) {
+        int occ = ps::batch_blocks_per_sm();
         for (int bps = 1; bps <= occ; ++bps) {
             if ((st = ps_batch_prepare(c, probs, nprob, cand_gs[gi], bps))) return st;
             if ((st = ps_batch_run(c))) return st;  // warm-up
@@ -844,6 +869,34 @@ int ps_solve(ps_ctx* c, const double* M, int64_t n, int64_t ldm, const double* b
     int st = ps_linalg_solve(c->la, M, (int)n, ldm, b, nrhs, ldb, x, ldx, c->stream, c->err, sizeof(c->err));
     if (!st) c->launches += 2;
     return st;
+}
+
+int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W, int64_t nW, int lmax, int bl, int bu,
+                   double* Xi, int64_t ldx)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!W || !Xi) return set_err(c, PS_ERR_ARG, "W and Xi must not be NULL");
+    if (lmax < 0 || lmax > PS_MAX_LMAX || nW < 1 || bl < 0 || bu < 0 || ldx < (int64_t)lmax + 1)
+        return set_err(c, PS_ERR_ARG, "need 0 <= lmax <= %d, nW >= 1, bandwidths >= 0, ldx >= lmax+1", PS_MAX_LMAX);
+    if (abs(nu1) > 64 || abs(nu2) > 64 || abs(s1) > 64 || abs(s2) > 64)
+        return set_err(c, PS_ERR_ARG, "spins beyond +-64 are not supported");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    const size_t n = (size_t)lmax + 1;
+    const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+    int st;
+    if ((st = ensure(c, &c->d_raw, &c->raw_cap, (size_t)nuse))) return st;
+    if ((st = ensure(c, &c->d_out, &c->out_cap, n * n))) return st;
+    PS_CUDA(c, cudaMemcpyAsync(c->d_raw, W, (size_t)nuse * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    PS_CUDA(c, cudaMemsetAsync(c->d_out, 0, n * n * sizeof(double), c->stream));
+    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    PS_CUDA(c, ps::launch_quickpol(c->d_raw, nuse, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out, (long long)n, c->stream));
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->launches++;
+    c->timed = true;
+    PS_CUDA(c, cudaMemcpy2DAsync(Xi, (size_t)ldx * sizeof(double), c->d_out, n * sizeof(double), n * sizeof(double), n,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
 }
 
 int ps_probe_fma_peak(ps_ctx* c, int fp64, double* flops)

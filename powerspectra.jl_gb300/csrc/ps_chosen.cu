@@ -139,8 +139,31 @@ __device__ __forceinline__ void sweep_step(Sweep& s, float dA, float dB, float d
     s.w += dw;
 }
 
+// The window configuration one task uses, read from the parameters once: the
+// inner loops then never reload launch parameters (which, when they live in
+// shared memory, the compiler could not keep in registers across the loop's
+// shared-memory stores).
+template <int NWIN>
+struct WinCfg {
+    int nwin;
+    int prod[NWIN], par[NWIN];
+};
+
+template <int NWIN, uint32_t SPEC>
+__device__ __forceinline__ WinCfg<NWIN> win_cfg(const CouplingParams& p)
+{
+    WinCfg<NWIN> c;
+    c.nwin = p.nwin;
+#pragma unroll
+    for (int k = 0; k < NWIN; ++k) {
+        c.prod[k] = wprod<SPEC>(p, k);
+        c.par[k] = wpar<SPEC>(p, k);
+    }
+    return c;
+}
+
 template <int NWIN, bool N00, bool N22, uint32_t SPEC, bool EVEN>
-__device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& s, const float* sw, int slot,
+__device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s, const float* sw, int slot,
                                           float* c, float& n0, float& n2)
 {
     float x22 = N22 ? sq_ff(s.f2) : 0.0f;
@@ -151,8 +174,8 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
         if (N00) n0 = __fmaf_rn(s.w, x00, n0);
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin && wpar<SPEC>(p, k) != PAR_ODD) {
-                const int pr = wprod<SPEC>(p, k);
+            if (k < p.nwin && p.par[k] != PAR_ODD) {
+                const int pr = p.prod[k];
                 float x = pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02);
                 c[k] = __fmaf_rn(x, sw[k * kSlots + slot], c[k]);
             }
@@ -160,7 +183,7 @@ __device__ __forceinline__ void sweep_acc(const CouplingParams& p, const Sweep& 
     } else if (N22) {
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin && wprod<SPEC>(p, k) == PROD_22_22 && wpar<SPEC>(p, k) != PAR_EVEN)
+            if (k < p.nwin && p.prod[k] == PROD_22_22 && p.par[k] != PAR_EVEN)
                 c[k] = __fmaf_rn(x22, sw[k * kSlots + slot], c[k]);
         }
     }
@@ -286,6 +309,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     const int T = l1;
     const bool fam22 = N22 && (l1 >= 2);
     const int jmin0 = l2_0 - l1, jmax0 = l2_0 + l1;  // lane 0's ends: lane i reads slot i + step
+    const WinCfg<NWIN> wc = win_cfg<NWIN, SPEC>(p);
 
     double Xi[kMaxWin];
     if (T == 0) {
@@ -348,18 +372,18 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
         const int steps = min(kChunk, T - t0);  // t0 is even, so step s has the parity of s
         int s = 0;
         for (; s + 1 < steps; s += 2) {
-            sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
             tab_fwd<N00, N22, false>(F, tb, s, lane);
             tab_bwd<N00, N22, false>(B, tb, s, lane);
-            sweep_acc<NWIN, N00, N22, SPEC, false>(p, F, sF, lane + s + 1, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, false>(p, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
+            sweep_acc<NWIN, N00, N22, SPEC, false>(wc, F, sF, lane + s + 1, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, false>(wc, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
             tab_fwd<N00, N22, true>(F, tb, s + 1, lane);
             tab_bwd<N00, N22, true>(B, tb, s + 1, lane);
         }
         if (s < steps) {  // one even step left (T odd, last chunk)
-            sweep_acc<NWIN, N00, N22, SPEC, true>(p, F, sF, lane + s, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, true>(p, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
+            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
             tab_fwd<N00, N22, false>(F, tb, s, lane);
             tab_bwd<N00, N22, false>(B, tb, s, lane);
         }
@@ -467,7 +491,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coup
 // 8 warp tasks (256 consecutive l2) of one row of one window group; the
 // group's CouplingParams live in global memory.
 template <int NWIN>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batch_chosen(const BatchParams bp)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) k_batch_chosen(const BatchParams bp)
 {
     __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
     // each warp's copy of its current group's parameters: read in the inner
@@ -497,50 +521,31 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_batc
         const int ntask = item.w & 0xff, fam = (item.w >> 8) & 0xf, tmpl = item.w >> 12;
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
-            if (NWIN == 4 && tmpl == 1)
-                chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (NWIN == 4 && tmpl == 2)
-                chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (NWIN == 4 && tmpl == 3)
-                chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (NWIN == 4 && tmpl == 4)
-                chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (NWIN == 4 && tmpl == 5)
-                chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (fam == 1)
-                chosen_task<NWIN, true, false, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else if (fam == 2)
-                chosen_task<NWIN, false, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
-            else
-                chosen_task<NWIN, true, true, 0>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane);
+            (void)fam;
+            switch (tmpl) {  // the group's compile-time slot set (prepare never emits others)
+            case 1: chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 2: chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 3: chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 4: chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 5: chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            default: chosen_task<4, true, true, rep(W02, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            }
             __syncwarp();
         }
     }
 }
 
-cudaError_t launch_batch_chosen(const BatchParams& bp, int group_slots, int blocks, cudaStream_t s)
+cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, cudaStream_t s)
 {
     if (bp.nitems <= 0) return cudaSuccess;
-    if (group_slots <= 2)
-        k_batch_chosen<2><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
-    else if (group_slots <= 4)
-        k_batch_chosen<4><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
-    else
-        k_batch_chosen<8><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
+    k_batch_chosen<4><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
     return cudaGetLastError();
 }
 
-int batch_blocks_per_sm(int group_slots)
+int batch_blocks_per_sm()
 {
     int n = 0;
-    cudaError_t e;
-    if (group_slots <= 2)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<2>, kWarpsPerBlock * 32, 0);
-    else if (group_slots <= 4)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<4>, kWarpsPerBlock * 32, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<8>, kWarpsPerBlock * 32, 0);
-    if (e != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<4>, kWarpsPerBlock * 32, 0) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
@@ -604,6 +609,7 @@ int chosen_batch_template(const CouplingParams& p)
     if (spec_fits(spec, p.nwin, S_MCM4, 4)) return 3;
     if (spec_fits(spec, p.nwin, rep(WPP, 4), 4)) return 4;
     if (spec_fits(spec, p.nwin, rep(WMM, 4), 4)) return 5;
+    if (spec_fits(spec, p.nwin, rep(W02, 4), 4)) return 6;
     return 0;
 }
 

@@ -71,8 +71,8 @@ struct BatchParams {
 };
 
 // Launchers (ps_plain_fp64.cu, ps_chosen.cu).
-cudaError_t launch_batch_chosen(const BatchParams& bp, int group_slots, int blocks, cudaStream_t s);
-int batch_blocks_per_sm(int group_slots);
+cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, cudaStream_t s);
+int batch_blocks_per_sm();
 int chosen_batch_template(const CouplingParams& p);  // compile-time slot set of a batch group (0: generic)
 cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s);
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
@@ -84,6 +84,8 @@ cudaError_t launch_split_windows(int2* dst, const double* wW, int wlen, cudaStre
 constexpr int kZeroExp = -100000;
 cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cudaStream_t s);
 cudaError_t launch_transpose(double* dst, const double* src, int n, cudaStream_t s);
+cudaError_t launch_quickpol(const double* W, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1, int s2,
+                            double* Xi, long long ldx, cudaStream_t s);
 
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);

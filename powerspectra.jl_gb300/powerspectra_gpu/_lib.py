@@ -27,7 +27,8 @@ MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_M
 EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
            "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
-           "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve")
+           "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
+           "ps_quickpol_xi")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -103,6 +104,8 @@ def load(path=None):
         lib.ps_decouple_covmat.restype = ci
         lib.ps_solve.argtypes = [vp, _DP, i64, i64, _DP, ci, i64, _DP, i64]
         lib.ps_solve.restype = ci
+        lib.ps_quickpol_xi.argtypes = [vp, ci, ci, ci, ci, _DP, i64, ci, ci, ci, _DP, i64]
+        lib.ps_quickpol_xi.restype = ci
         lib.ps_last_kernel_ms.argtypes = [vp]
         lib.ps_last_kernel_ms.restype = ctypes.c_double
         lib.ps_launch_count.argtypes = [vp]
@@ -221,6 +224,15 @@ class Context:
             ml[s] = int(dMs[s])
         self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
                                                 mode_code(mode), dptr_array(ml), int(ldm)))
+
+    def quickpol_xi(self, nu1, nu2, s1, s2, W, lmax, bl, bu):
+        """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band."""
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        n = lmax + 1
+        X = np.empty((n, n), dtype=np.float64, order="F")
+        self.check(self.lib.ps_quickpol_xi(self.handle, int(nu1), int(nu2), int(s1), int(s2), dptr(W), len(W), lmax,
+                                           int(bl), int(bu), dptr(X), n))
+        return X
 
     def decouple_covmat(self, Y, B1, B2):
         """B1^-1 Y B2^-T (decouple_covmat, src/covariance.jl:8-14) for square float64 matrices."""

@@ -1,0 +1,41 @@
+"""QuickPol beam coupling Xi (quickpolXi!, src/beam.jl:72-109) against the oracle.
+
+General-spin families (l' l l''; s+nu, -s, -nu): the oracle's recurrence is
+checked against exact 3j values for such spins in tests/test_oracle.py."""
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("nu1,nu2,s1,s2", [(0, 0, 0, 0), (0, 0, 2, 2), (1, -1, 2, 0), (2, 2, -2, 2), (-3, 1, 2, -2),
+                                           (4, -4, 0, 2)])
+@pytest.mark.parametrize("lmax,bl,bu,nWk", [(120, 10, 10, "2L"), (200, 30, 5, "L"), (60, 100, 100, "short")])
+def test_quickpol_vs_oracle(ctx, nu1, nu2, s1, s2, lmax, bl, bu, nWk):
+    nW = {"2L": 2 * lmax + 1, "L": lmax + 1, "short": lmax // 2}[nWk]
+    rng = np.random.default_rng(lmax + 7 * nu1 + 3 * s1)
+    W = rng.random(nW) * np.exp(-np.arange(nW) / 40.0)
+    G = ctx.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu)
+    R = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu)
+    scale = np.abs(o.quickpol_xi(nu1, nu2, s1, s2, np.abs(W), lmax, bl, bu))  # positive W: no cancellation in W
+    err = np.abs(G - R) / np.maximum(np.maximum(np.abs(R), 1e-3 * scale), 1e-300)
+    band = np.zeros_like(G, dtype=bool)
+    for r in range(2, lmax + 1):
+        band[r, max(2, r - bl):min(lmax, r + bu) + 1] = True
+    assert not np.any(G[~band])
+    assert np.max(err[band]) < 1e-10
+
+
+def test_quickpol_known_identity(ctx):
+    """nu = s = 0 with W = 4 pi delta_l0 ... (l' l l''; 0 0 0)^2 summed against W_0 only
+    picks l' = 0, i.e. l = l'': Xi is diagonal with value W_0 / (2 l + 1)."""
+    lmax = 80
+    W = np.zeros(2 * lmax + 1)
+    W[0] = 3.0
+    X = ctx.quickpol_xi(0, 0, 0, 0, W, lmax, 5, 5)
+    l = np.arange(lmax + 1)
+    np.testing.assert_allclose(np.diag(X)[2:], 3.0 / (2 * l[2:] + 1), rtol=1e-13)
+    off = X - np.diag(np.diag(X))
+    assert np.max(np.abs(off)) < 1e-15

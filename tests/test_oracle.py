@@ -137,3 +137,25 @@ def test_covariance_symmetric_and_reference_formula():
     TEip, TEiq, TEjq, TEjp = S
     want = ((TEip[a] * TEjq[b] + TEjq[a] * TEip[b]) * X[0][a, b] + (TEiq[a] * TEjp[b] + TEjp[a] * TEiq[b]) * X[1][a, b]) / 2
     assert abs(C[a, b] - want) <= 1e-14 * abs(want)
+
+
+@pytest.mark.parametrize("l1,l2,m1,m2", [(40, 37, -2, -4), (100, 90, 3, -1), (200, 250, -2, 4), (1000, 1003, -6, 2),
+                                         (513, 600, 2, -6), (30, 30, -4, 4), (8, 9, -3, -3)])
+def test_general_spin_families_vs_exact(l1, l2, m1, m2):
+    """General (m1, m2, -m1-m2) families, as QuickPol uses, against the mpmath Racah sum."""
+    exact3j = pytest.importorskip("oracle.exact3j")
+    jmin, f = o.w3j_family(l1, l2, m1, m2)
+    amp = 1.0 / math.sqrt(max((l1 + l2 + 1) ** 2 - jmin ** 2, 1))
+    for k in np.unique(np.linspace(0, len(f) - 1, 10).astype(int)):
+        ex = float(exact3j.w3j(l1, l2, jmin + int(k), m1, m2, -m1 - m2))
+        assert abs(f[k] - ex) <= 1e-12 * max(abs(ex), amp)
+
+
+def test_quickpol_oracle_diagonal_known_answer():
+    lmax = 40
+    W = np.zeros(2 * lmax + 1)
+    W[0] = 3.0
+    X = o.quickpol_xi(0, 0, 0, 0, W, lmax, 4, 4)
+    l = np.arange(lmax + 1)
+    np.testing.assert_allclose(np.diag(X)[2:], 3.0 / (2 * l[2:] + 1), rtol=1e-14)
+    assert np.max(np.abs(X - np.diag(np.diag(X)))) < 1e-16
