@@ -474,9 +474,19 @@ def run_set(args):
         for _ in range(args.warmup):
             sequential_chosen()
         line["sequential_chosen"] = {"value": elements / ev_time(sequential_chosen, args.steps), "unit": UNIT}
+        # three rows of every matrix from the sequential launches, to check the batched results against
+        seq_rows = [c[[0, c.shape[0] // 2, c.shape[0] - 1]].clone() for c, _ in mats]
     for _ in range(max(args.warmup, 3)):
         chosen()
     t_c = ev_time(chosen, args.steps)
+    if args.config == "batched_64":
+        d = 0.0
+        for (c, _), r in zip(mats, seq_rows):
+            b = c[[0, c.shape[0] // 2, c.shape[0] - 1]]
+            den = torch.maximum(r.abs(), 1e-9 * r.abs().max())
+            den = torch.where(den == 0, torch.ones_like(den), den)
+            d = max(d, float(((b - r).abs() / den).max().item()))
+        line["sequential_chosen"]["max_rel_diff_batched_vs_sequential"] = d
     line.update({"metric": METRIC, "value": elements / t_c, "ms_per_step": t_c * 1e3, "steps": args.steps,
                  "elements_per_step": elements, "mode": "chosen"})
     if not args.no_plain:
@@ -489,6 +499,112 @@ def run_set(args):
             errs.append(float(((c - q).abs() / den).max().item()))
         line["plain_fp64"] = {"value": elements / t_p, "ms_per_step": t_p * 1e3, "steps": 1,
                               "chosen_over_plain": t_p / t_c, "max_rel_err_chosen_vs_fp64": max(errs)}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
+def run_window(args):
+    """window_W_8191: mask spectra W_l from harmonic coefficients (alm2cl, window_function_W!).
+
+    8 seeded coefficient sets at lmax = mmax = 8191 (33.6M complex coefficients, 537 MB each,
+    a mask-like envelope in l) and the 36 spectra of all pairs i <= j, one ps_window_W_device
+    call each: one step reads 8 auto sets once and 28 cross pairs twice, 34.4 GB.  The
+    reduction is HBM-bound; the roofline is coefficient bytes read / kernel time against the
+    measured HBM copy bandwidth."""
+    import numpy as np
+    import torch
+    import powerspectra_gpu as pg
+    from oracle import oracle as o
+
+    L, nsets = 8191, 8
+    torch.cuda.set_device(0)
+    ctx = pg.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    nalm = o.n_alms(L, L)
+    ls = torch.cat([torch.arange(m, L + 1, device="cuda", dtype=torch.float64) for m in range(L + 1)])
+    env = torch.exp(-ls / 3000.0) / (ls + 1.0)
+    gen = torch.Generator(device="cuda").manual_seed(8191)
+    sets = []
+    for _ in range(nsets):
+        a = torch.randn((nalm, 2), dtype=torch.float64, device="cuda", generator=gen) * env[:, None]
+        a[:L + 1, 1] = 0.0  # m = 0 coefficients of a real field are real
+        sets.append(a)
+    del ls, env
+    pairs = [(i, j) for i in range(nsets) for j in range(i, nsets)]
+    out = torch.empty((len(pairs), L + 1), dtype=torch.float64, device="cuda")
+    bytes_step = sum((1 if i == j else 2) * nalm * 16 for i, j in pairs)
+
+    def step():
+        for q, (i, j) in enumerate(pairs):
+            ctx.window_W_device([sets[i].data_ptr()], [sets[j].data_ptr()], L, L, L, out[q].data_ptr())
+
+    def ev_time(fn, steps):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / steps
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    clk = ClockSampler(0)
+    launches0 = ctx.launch_count()
+    t = ev_time(step, args.steps)
+    launches = (ctx.launch_count() - launches0) // args.steps
+    clocks = clk.stop()
+    # one partial-sum launch alone, for the roofline (its share is nearly all of a call)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ctx.window_W_device([sets[0].data_ptr()], [sets[1].data_ptr()], L, L, L, out[0].data_ptr())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t1 = ev0.elapsed_time(ev1) / 1e3
+    peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    ach = 2 * nalm * 16 / t1 / 1e9
+    # parity at full size: one auto and one cross spectrum against the oracle (numpy, host)
+    host = [sets[k].cpu().numpy().view(np.complex128).ravel() for k in (0, 1)]
+    got = out.cpu().numpy()
+    t0 = time.perf_counter()
+    ref_cross = o.alm2cl(host[0], host[1], L)
+    cpu_dt = time.perf_counter() - t0
+    ref_auto = o.alm2cl(host[0], host[0], L)
+    sc_cross = o.alm2cl(np.abs(host[0]).astype(complex), np.abs(host[1]).astype(complex), L)
+    err = max(float(np.max(np.abs(got[1] - ref_cross) / sc_cross)),
+              float(np.max(np.abs(got[0] - ref_auto) / np.abs(ref_auto))))
+    # e2e: the host-pointer entry point, pinned host sets in, spectra out (each call copies its sets)
+    hsets = [torch.empty((nalm, 2), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    for k in range(3):
+        hsets[k].copy_(sets[k])
+    hw = np.empty(L + 1)
+    e2e_pairs = [(0, 0), (0, 1), (1, 2)]
+    t0 = time.perf_counter()
+    for i, j in e2e_pairs:
+        ctx.window_W([hsets[i].numpy().view(np.complex128).ravel()], [hsets[j].numpy().view(np.complex128).ravel()],
+                     L)
+    e2e_dt = time.perf_counter() - t0
+    e2e_bytes = sum((1 if i == j else 2) * nalm * 16 for i, j in e2e_pairs)
+    line = {"metric": "alm2cl coefficient bytes/s (window_function_W! mask spectra)", "value": bytes_step / t / 1e9,
+            "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "window_W_8191", "lmax": L, "mmax": L, "sets": nsets,
+                                            "spectra_per_step": len(pairs), "bytes_per_step": bytes_step,
+                                            "l2": "inputs (537 MB per set) larger than L2"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "traffic": None, "kernel": "k_alm2cl_partial + k_alm2cl_reduce, one cross spectrum",
+                         "ms_per_call": t1 * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+            "e2e": {"value": e2e_bytes / e2e_dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": e2e_bytes,
+                    "d2h_bytes_per_step": 8 * (L + 1) * len(e2e_pairs),
+                    "what": "ps_window_W on pinned host sets: 1 auto and 2 cross spectra"},
+            "max_rel_err_vs_oracle": err, "clocks": clocks, "gpu_launches": launches,
+            "cpu_baseline": {"value": 2 * nalm * 16 / cpu_dt / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                             "sample": "one cross spectrum at lmax 8191 with the oracle's numpy alm2cl, %.1f s"
+                                       % cpu_dt}}
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -510,6 +626,8 @@ def main():
         return run_reference(args)
     if args.config in SET_CONFIGS:
         return run_set(args)
+    if args.config == "window_W_8191":
+        return run_window(args)
     return run_ours(args)
 
 

@@ -135,6 +135,12 @@ int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int 
  * singular B1 or B2 returns PS_ERR_ARG. */
 int ps_decouple_covmat(ps_ctx *ctx, const double *Y, const double *B1, const double *B2, int64_t n, int64_t ld,
                        double *out, int64_t ldout);
+/* The same on device matrices, so a covariance from ps_coupledcov_device is
+ * decoupled without leaving the GPU.  Runs on the context stream and waits for
+ * each factorisation's pivot status (to report a singular B1 or B2), so it
+ * returns once `out` is written. */
+int ps_decouple_covmat_device(ps_ctx *ctx, const double *dY, const double *dB1, const double *dB2, int64_t n,
+                              int64_t ld, double *dout, int64_t ldout);
 /* x = M \ b for an n x n coupling matrix and nrhs right-hand sides (host,
  * column-major): the decoupling `M \ pCl` of master (src/modecoupling.jl:358,
  * src/blockspectralmatrix.jl:124-129), by FP64 LU on the GPU. */
@@ -153,6 +159,25 @@ int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double 
  * matrix. */
 int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *W, int64_t nW, int lmax, int bl,
                    int bu, double *Xi, int64_t ldx);
+
+/* Mask spectra from harmonic coefficients (alm2cl): for l = 0..lout,
+ *   W[l] = (1/nterms) sum_t cl(A[t], B[t])[l],
+ *   cl(a, b)[l] = (Re(a_l0 conj b_l0) + 2 sum_{m=1}^{min(l,mmax)} Re(a_lm conj b_lm)) / (2l+1).
+ * Each set holds the complex coefficients of one real field as interleaved
+ * (re, im) doubles in the HEALPix m-major order, (l, m) at m(2 lmax+1-m)/2 + l
+ * (Healpix.jl's Alm).  A NULL set stands for all-zero coefficients: its term
+ * adds nothing but still counts in 1/nterms.  Replaces window_function_W!
+ * (src/workspace.jl:174-213), whose terms are the (wX, wY) effective-weight
+ * pairs, and with nterms = 1 the alm2cl calls of mcm (src/modecoupling.jl:197,
+ * :234) and master (src/modecoupling.jl:357-373).  1 <= nterms <= 16,
+ * 0 <= mmax <= lmax, lout <= lmax.  FP64; the summation order is fixed, so
+ * results are reproducible run to run.  ps_window_W takes host arrays and
+ * returns when W is filled; ps_window_W_device takes 16-byte aligned device
+ * sets and a device W and is enqueued on the context stream. */
+int ps_window_W(ps_ctx *ctx, const double *const *A, const double *const *B, int nterms, int lmax, int mmax,
+                int lout, double *W);
+int ps_window_W_device(ps_ctx *ctx, const double *const *dA, const double *const *dB, int nterms, int lmax, int mmax,
+                       int lout, double *dW);
 
 /* One coupling problem of a batch (device pointers): K spectra of nW entries,
  * the spin cases to compute for each, and 4*K output slots (entry 4*k + s). */

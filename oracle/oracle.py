@@ -4,6 +4,8 @@ TEST INFRASTRUCTURE ONLY.  The oracle restates, in plain FP64 C with OpenMP,
 the reference algorithm of PowerSpectra.jl for the mode-coupling hot path:
   src/modecoupling.jl:3-159   Xi projectors, fill_3j!, inner_mcm00!/02!/++!/--!
   src/covariance.jl:92-446    loop_cov{TTTT,EEEE,TTTE,TETE,TEEE,TEEE_planck,TTEE}!
+  src/beam.jl:17-109          Xisum / quickpolXi!
+  src/workspace.jl:174-213    window_function_W! (alm2cl of coefficient sets; plain numpy below)
 Matrices are column-major (Julia layout): element (l1, l2) of an (n x n)
 result with lmin offset lives at [l1 - lmin, l2 - lmin] of a Fortran-ordered
 numpy array.
@@ -166,3 +168,40 @@ def quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, nthreads=0):
     if st:
         raise RuntimeError("oracle quickpol_xi failed (%d)" % st)
     return X
+
+
+def alm_index(l, m, lmax):
+    """Position of a_lm in the HEALPix m-major coefficient order (Healpix.jl almIndex, 0-based)."""
+    return m * (2 * lmax + 1 - m) // 2 + l
+
+
+def n_alms(lmax, mmax):
+    return (mmax + 1) * (mmax + 2) // 2 + (mmax + 1) * (lmax - mmax)
+
+
+def alm2cl(a, b, lmax, mmax=None):
+    """Cross-spectrum of two coefficient sets of real fields (the HEALPix alm2cl definition that
+    src/modecoupling.jl:197 and src/workspace.jl:202 call, from the third-party Healpix.jl):
+    cl[l] = (Re a_l0 b*_l0 + 2 sum_{m=1}^{min(l,mmax)} Re a_lm b*_lm) / (2l+1).  Plain loops over m
+    in FP64, one l-vector per m."""
+    mmax = lmax if mmax is None else mmax
+    cl = np.zeros(lmax + 1)
+    for m in range(mmax + 1):
+        i0 = alm_index(m, m, lmax)
+        x = a[i0:i0 + lmax + 1 - m]
+        y = b[i0:i0 + lmax + 1 - m]
+        term = x.real * y.real + x.imag * y.imag
+        cl[m:] += term if m == 0 else 2.0 * term
+    return cl / (2.0 * np.arange(lmax + 1) + 1.0)
+
+
+def window_function_W(A, B, lmax, mmax=None, lout=None):
+    """window_function_W! (src/workspace.jl:174-213): the mean over the (wX, wY) terms of
+    alm2cl(A[t], B[t])[0:lout]; None is an all-zero set (effective_weight_alm!'s zero Alm,
+    src/workspace.jl:167-170), which still counts in the mean."""
+    lout = lmax if lout is None else lout
+    res = np.zeros(lout + 1)
+    for a, b in zip(A, B):
+        if a is not None and b is not None:
+            res += alm2cl(a, b, lmax, mmax)[:lout + 1]
+    return res * (1.0 / len(A))

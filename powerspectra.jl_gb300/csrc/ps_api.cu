@@ -18,7 +18,7 @@ struct ps_linalg;
 ps_linalg* ps_linalg_new();
 void ps_linalg_free(ps_linalg* L);
 int ps_linalg_decouple(ps_linalg* L, const double* Y, const double* B1, const double* B2, int n, int64_t ldin,
-                       double* out, int64_t ldout, cudaStream_t s, char* err, size_t errn);
+                       double* out, int64_t ldout, cudaStream_t s, char* err, size_t errn, bool on_device);
 int ps_linalg_solve(ps_linalg* L, const double* M, int n, int64_t ldm, const double* b, int nrhs, int64_t ldb,
                     double* x, int64_t ldx, cudaStream_t s, char* err, size_t errn);
 
@@ -47,6 +47,10 @@ struct ps_ctx {
     double* d_probe = nullptr;
     int2* d_bf = nullptr;  // split (mantissa, exponent) windows for the chosen kernel
     size_t bf_cap = 0;
+    double* d_alm = nullptr;  // harmonic coefficients copied in by ps_window_W (2 doubles each)
+    size_t alm_cap = 0;
+    double* d_part = nullptr;  // alm2cl partial sums
+    size_t part_cap = 0;
     // batched workload state (ps_batch_*)
     struct Batch {
         bool ready = false;
@@ -376,6 +380,8 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_out);
     cudaFree(c->d_probe);
     cudaFree(c->d_bf);
+    cudaFree(c->d_alm);
+    cudaFree(c->d_part);
     batch_release(c);
     ps_linalg_free(c->la);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -711,6 +717,10 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
             }
             const int fam = (f00 ? 1 : 0) | (f22 ? 2 : 0);
             const int tmpl = ps::chosen_batch_template(g);
+            if (tmpl == 0) {
+                batch_release(c);
+                return set_err(c, PS_ERR_UNSUPPORTED, "problem %d: no batched kernel body for a window group", i);
+            }
             const int gid = (int)groups.size();
             groups.push_back(g);
             // items: up to 8 warp tasks (256 consecutive l2) of one row
@@ -852,7 +862,20 @@ int ps_decouple_covmat(ps_ctx* c, const double* Y, const double* B1, const doubl
     if (n < 1 || n > 65535 || ld < n || ldout < n) return set_err(c, PS_ERR_ARG, "need 1 <= n <= 65535, ld >= n");
     PS_CUDA(c, cudaSetDevice(c->device));
     if (!c->la) c->la = ps_linalg_new();
-    int st = ps_linalg_decouple(c->la, Y, B1, B2, (int)n, ld, out, ldout, c->stream, c->err, sizeof(c->err));
+    int st = ps_linalg_decouple(c->la, Y, B1, B2, (int)n, ld, out, ldout, c->stream, c->err, sizeof(c->err), false);
+    if (!st) c->launches += 6;
+    return st;
+}
+
+int ps_decouple_covmat_device(ps_ctx* c, const double* dY, const double* dB1, const double* dB2, int64_t n, int64_t ld,
+                              double* dout, int64_t ldout)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!dY || !dB1 || !dB2 || !dout) return set_err(c, PS_ERR_ARG, "Y, B1, B2 and out must not be NULL");
+    if (n < 1 || n > 65535 || ld < n || ldout < n) return set_err(c, PS_ERR_ARG, "need 1 <= n <= 65535, ld >= n");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    if (!c->la) c->la = ps_linalg_new();
+    int st = ps_linalg_decouple(c->la, dY, dB1, dB2, (int)n, ld, dout, ldout, c->stream, c->err, sizeof(c->err), true);
     if (!st) c->launches += 6;
     return st;
 }
@@ -895,6 +918,90 @@ int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W,
     c->timed = true;
     PS_CUDA(c, cudaMemcpy2DAsync(Xi, (size_t)ldx * sizeof(double), c->d_out, n * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDeviceToHost, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+// Shared by ps_window_W and ps_window_W_device: dA/dB are device sets (null = zeros).
+static int window_run(ps_ctx* c, const double* const* dA, const double* const* dB, int nterms, int lmax, int mmax,
+                      int lout, double* dW)
+{
+    ps::AlmParams p = {};
+    p.nterms = nterms;
+    p.lmax = lmax;
+    p.mmax = mmax;
+    p.lout = lout;
+    p.mchunk = ps::kAlmChunk;
+    p.nmchunks = ps::alm2cl_chunks(mmax);
+    for (int t = 0; t < nterms; ++t) {
+        p.a[t] = (const double2*)dA[t];
+        p.b[t] = (const double2*)dB[t];
+    }
+    int st = ensure(c, &c->d_part, &c->part_cap, (size_t)nterms * p.nmchunks * ((size_t)lout + 1));
+    if (st) return st;
+    p.partial = c->d_part;
+    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    PS_CUDA(c, ps::launch_alm2cl(p, 1.0 / nterms, dW, c->stream));
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->launches += 2;
+    c->timed = true;
+    return PS_OK;
+}
+
+static int window_check(ps_ctx* c, const double* const* A, const double* const* B, int nterms, int lmax, int mmax,
+                        int lout, const double* W)
+{
+    if (!A || !B || !W) return set_err(c, PS_ERR_ARG, "A, B and W must not be NULL");
+    if (nterms < 1 || nterms > ps::kAlmMaxTerms)
+        return set_err(c, PS_ERR_ARG, "need 1 <= nterms <= %d, got %d", ps::kAlmMaxTerms, nterms);
+    if (lmax < 0 || lmax > 65535 || mmax < 0 || mmax > lmax || lout < 0 || lout > lmax)
+        return set_err(c, PS_ERR_ARG, "need 0 <= mmax <= lmax <= 65535 and 0 <= lout <= lmax");
+    return PS_OK;
+}
+
+int ps_window_W_device(ps_ctx* c, const double* const* dA, const double* const* dB, int nterms, int lmax, int mmax,
+                       int lout, double* dW)
+{
+    if (!c) return PS_ERR_ARG;
+    int st = window_check(c, dA, dB, nterms, lmax, mmax, lout, dW);
+    if (st) return st;
+    for (int t = 0; t < nterms; ++t)
+        if (((uintptr_t)dA[t] | (uintptr_t)dB[t]) & 15)
+            return set_err(c, PS_ERR_ARG, "coefficient set %d is not 16-byte aligned", t);
+    PS_CUDA(c, cudaSetDevice(c->device));
+    return window_run(c, dA, dB, nterms, lmax, mmax, lout, dW);
+}
+
+int ps_window_W(ps_ctx* c, const double* const* A, const double* const* B, int nterms, int lmax, int mmax, int lout,
+                double* W)
+{
+    if (!c) return PS_ERR_ARG;
+    int st = window_check(c, A, B, nterms, lmax, mmax, lout, W);
+    if (st) return st;
+    PS_CUDA(c, cudaSetDevice(c->device));
+    // copy each distinct host set once (an auto-spectrum term names the same set twice)
+    const size_t nalm = (size_t)(mmax + 1) * (mmax + 2) / 2 + (size_t)(mmax + 1) * (lmax - mmax);
+    std::vector<const double*> uniq;
+    for (int t = 0; t < nterms; ++t)
+        for (const double* q : {A[t], B[t]})
+            if (q && std::find(uniq.begin(), uniq.end(), q) == uniq.end()) uniq.push_back(q);
+    if ((st = ensure(c, &c->d_alm, &c->alm_cap, 2 * nalm * (uniq.size() ? uniq.size() : 1)))) return st;
+    if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)lout + 1))) return st;
+    for (size_t u = 0; u < uniq.size(); ++u)
+        PS_CUDA(c, cudaMemcpyAsync(c->d_alm + 2 * nalm * u, uniq[u], 2 * nalm * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->stream));
+    auto dev = [&](const double* q) -> const double* {
+        if (!q) return nullptr;
+        return c->d_alm + 2 * nalm * (size_t)(std::find(uniq.begin(), uniq.end(), q) - uniq.begin());
+    };
+    const double* dA[ps::kAlmMaxTerms];
+    const double* dB[ps::kAlmMaxTerms];
+    for (int t = 0; t < nterms; ++t) {
+        dA[t] = dev(A[t]);
+        dB[t] = dev(B[t]);
+    }
+    if ((st = window_run(c, dA, dB, nterms, lmax, mmax, lout, c->d_out))) return st;
+    PS_CUDA(c, cudaMemcpyAsync(W, c->d_out, ((size_t)lout + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PS_OK;
 }

@@ -463,12 +463,15 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     if (active) write_pair(p, l1, l2, Xi);
 }
 
+// n copies of one slot spec w (4 bits) in consecutive slots
 __host__ __device__ constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
 constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
 constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
 // the window sets of the mode-coupling and covariance entry points
 constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
 constexpr uint32_t S_PPMM = WPP | (WMM << 4);
+constexpr uint32_t S_PPMM2 = S_PPMM | (S_PPMM << 8);  // (++, --) of two windows
+static_assert(((S_PPMM2 >> 8) & 0xffu) == S_PPMM && ((S_PPMM2 >> 4) & 0xfu) == WMM, "slot layout of S_PPMM2");
 constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
 
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
@@ -524,11 +527,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) k_batch_chosen(const B
             (void)fam;
             switch (tmpl) {  // the group's compile-time slot set (prepare never emits others)
             case 1: chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 2: chosen_task<4, false, true, rep(S_PPMM, 2)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 2: chosen_task<4, false, true, S_PPMM2>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
             case 3: chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
             case 4: chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
             case 5: chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            default: chosen_task<4, true, true, rep(W02, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            case 6: chosen_task<4, true, true, rep(W02, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
+            default: break;  // prepare rejects groups without a body
             }
             __syncwarp();
         }
@@ -605,7 +609,7 @@ int chosen_batch_template(const CouplingParams& p)
 {
     const uint32_t spec = spec_of(p);
     if (spec_fits(spec, p.nwin, rep(W00, 4), 4)) return 1;
-    if (spec_fits(spec, p.nwin, rep(S_PPMM, 2), 4)) return 2;
+    if (spec_fits(spec, p.nwin, S_PPMM2, 4)) return 2;
     if (spec_fits(spec, p.nwin, S_MCM4, 4)) return 3;
     if (spec_fits(spec, p.nwin, rep(WPP, 4), 4)) return 4;
     if (spec_fits(spec, p.nwin, rep(WMM, 4), 4)) return 5;
@@ -630,7 +634,7 @@ cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s)
     if (spec_fits(spec, nw, WMM, 1)) return launch_cfg<1, WMM>(p, n00, n22, s);
     if (spec_fits(spec, nw, S_PPMM, 2)) return launch_cfg<2, S_PPMM>(p, n00, n22, s);
     if (spec_fits(spec, nw, rep(W00, 4), 4)) return launch_cfg<4, rep(W00, 4)>(p, n00, n22, s);
-    if (spec_fits(spec, nw, rep(S_PPMM, 2), 4)) return launch_cfg<4, rep(S_PPMM, 2)>(p, n00, n22, s);
+    if (spec_fits(spec, nw, S_PPMM2, 4)) return launch_cfg<4, S_PPMM2>(p, n00, n22, s);
     if (spec_fits(spec, nw, S_MCM4, 4)) return launch_cfg<4, S_MCM4>(p, n00, n22, s);
     if (spec_fits(spec, nw, rep(W02, 4), 4)) return launch_cfg<4, rep(W02, 4)>(p, n00, n22, s);
     if (spec_fits(spec, nw, rep(WPP, 4), 4)) return launch_cfg<4, rep(WPP, 4)>(p, n00, n22, s);

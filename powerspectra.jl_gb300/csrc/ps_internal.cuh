@@ -87,6 +87,21 @@ cudaError_t launch_transpose(double* dst, const double* src, int n, cudaStream_t
 cudaError_t launch_quickpol(const double* W, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1, int s2,
                             double* Xi, long long ldx, cudaStream_t s);
 
+// alm2cl reduction (ps_window.cu).  Term t pairs coefficient sets a[t], b[t]
+// (HEALPix m-major order, lmax / mmax); a null set stands for all zeros.
+constexpr int kAlmMaxTerms = 16;
+constexpr int kAlmChunk = 64;  // m values per block of the partial-sum kernel
+struct AlmParams {
+    const double2* a[kAlmMaxTerms];
+    const double2* b[kAlmMaxTerms];
+    int nterms;
+    int lmax, mmax, lout;
+    int mchunk, nmchunks;
+    double* partial;  // nterms * nmchunks * (lout + 1)
+};
+int alm2cl_chunks(int mmax);
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, double* W, cudaStream_t s);
+
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);
 int cov_nratios(int kind);

@@ -145,28 +145,31 @@ void ps_linalg_free(ps_linalg* L)
     delete L;
 }
 
-// Copy a column-major host matrix (ld) into a dense device matrix (ld = rows).
-static int la_in(double* dst, const double* src, int rows, int cols, int64_t ld, cudaStream_t s, char* err, size_t errn)
+// Copy a column-major host (or device) matrix (ld) into a dense device matrix (ld = rows).
+static int la_in(double* dst, const double* src, int rows, int cols, int64_t ld, cudaStream_t s, char* err, size_t errn,
+                 bool on_device = false)
 {
     LA_CUDA(cudaMemcpy2DAsync(dst, (size_t)rows * sizeof(double), src, (size_t)ld * sizeof(double),
-                              (size_t)rows * sizeof(double), (size_t)cols, cudaMemcpyHostToDevice, s));
+                              (size_t)rows * sizeof(double), (size_t)cols,
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
     return PS_OK;
 }
 
 int ps_linalg_decouple(ps_linalg* L, const double* Y, const double* B1, const double* B2, int n, int64_t ldin,
-                       double* out, int64_t ldout, cudaStream_t s, char* err, size_t errn)
+                       double* out, int64_t ldout, cudaStream_t s, char* err, size_t errn, bool on_device)
 {
     int st = la_reserve(L, (size_t)n * n, n, s, err, errn);
     if (st) return st;
-    if ((st = la_in(L->x, Y, n, n, ldin, s, err, errn))) return st;
-    if ((st = la_in(L->a, B1, n, n, ldin, s, err, errn))) return st;
+    if ((st = la_in(L->x, Y, n, n, ldin, s, err, errn, on_device))) return st;
+    if ((st = la_in(L->a, B1, n, n, ldin, s, err, errn, on_device))) return st;
     if ((st = la_lu_solve(L, n, n, L->x, s, "B1", err, errn))) return st;  // x = B1^-1 Y
     LA_CUDA(ps::launch_transpose(L->t, L->x, n, s));                        // t = x^T
-    if ((st = la_in(L->a, B2, n, n, ldin, s, err, errn))) return st;
+    if ((st = la_in(L->a, B2, n, n, ldin, s, err, errn, on_device))) return st;
     if ((st = la_lu_solve(L, n, n, L->t, s, "B2", err, errn))) return st;  // t = B2^-1 x^T
     LA_CUDA(ps::launch_transpose(L->x, L->t, n, s));                        // x = x B2^-T
     LA_CUDA(cudaMemcpy2DAsync(out, (size_t)ldout * sizeof(double), L->x, (size_t)n * sizeof(double),
-                              (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, s));
+                              (size_t)n * sizeof(double), (size_t)n,
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     LA_CUDA(cudaStreamSynchronize(s));
     return PS_OK;
 }

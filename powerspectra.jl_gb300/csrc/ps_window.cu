@@ -1,0 +1,92 @@
+// ps_window.cu -- mask power spectra W_l from harmonic coefficients (alm2cl) on the GPU.
+//
+// Replaces the alm2cl reductions that feed the coupling kernels:
+//   * window_function_W! (src/workspace.jl:174-213): the average over the
+//     (wX, wY) weight terms of alm2cl(w_X, w_Y)[0:lmax] (Planck 2015 eq. C.11-C.16);
+//   * the mask cross-spectrum of mcm (src/modecoupling.jl:197, :234) and the
+//     pseudo-spectra of master (src/modecoupling.jl:357-373), one term each.
+//
+// The cross-spectrum of two coefficient sets of a real field is the published
+// definition
+//     cl[l] = ( Re(a_l0 conj b_l0) + 2 sum_{m=1}^{min(l, mmax)} Re(a_lm conj b_lm) ) / (2l + 1),
+// with the coefficients in the HEALPix m-major order: (l, m) at
+// m (2 lmax + 1 - m) / 2 + l.
+//
+// The reduction is HBM-bound (16 bytes per coefficient and set, read once).
+// Thread l of a block reads (l, m) for the m of its block's m-chunk; the 32
+// lanes of a warp hold consecutive l at the same m, so each load is 512
+// contiguous bytes.  Partial sums per (term, m-chunk, l) go to a scratch array
+// and a second kernel adds them in a fixed order, so results do not depend on
+// scheduling (no atomics).
+#include "ps_internal.cuh"
+
+namespace ps {
+
+namespace {
+
+constexpr int kAlmThreads = 256;
+
+__global__ void __launch_bounds__(kAlmThreads) k_alm2cl_partial(AlmParams p)
+{
+    const int l = blockIdx.x * kAlmThreads + threadIdx.x;
+    const int c = blockIdx.y, t = blockIdx.z;
+    const double2* __restrict__ a = p.a[t];
+    const double2* __restrict__ b = p.b[t];
+    const int m0 = c * p.mchunk;
+    double acc = 0.0;
+    if (l <= p.lout && a && b) {
+        const int m1 = min(min(m0 + p.mchunk - 1, p.mmax), l);
+        long long idx = (long long)m0 * (2 * p.lmax + 1 - m0) / 2 + l;  // (l, m0)
+        if (a == b) {
+#pragma unroll 4
+            for (int m = m0; m <= m1; ++m) {
+                const double2 v = __ldg(a + idx);
+                const double x = fma(v.x, v.x, v.y * v.y);
+                acc += m == 0 ? x : 2.0 * x;
+                idx += p.lmax - m;  // (l, m + 1)
+            }
+        } else {
+#pragma unroll 4
+            for (int m = m0; m <= m1; ++m) {
+                const double2 v = __ldg(a + idx), w = __ldg(b + idx);
+                const double x = fma(v.x, w.x, v.y * w.y);
+                acc += m == 0 ? x : 2.0 * x;
+                idx += p.lmax - m;
+            }
+        }
+    }
+    if (l <= p.lout) p.partial[((long long)t * p.nmchunks + c) * (p.lout + 1) + l] = acc;
+}
+
+// W[l] = scale * sum_t (sum_c partial[t][c][l]) / (2l + 1), in a fixed order.
+__global__ void k_alm2cl_reduce(const double* __restrict__ partial, int nterms, int nmchunks, int lout, double scale,
+                                double* __restrict__ W)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l > lout) return;
+    const double inv = 1.0 / (2.0 * l + 1.0);
+    double s = 0.0;
+    for (int t = 0; t < nterms; ++t) {
+        double ct = 0.0;
+        const double* q = partial + (long long)t * nmchunks * (lout + 1) + l;
+        for (int c = 0; c < nmchunks; ++c) ct += q[(long long)c * (lout + 1)];
+        s += ct * inv;
+    }
+    W[l] = s * scale;
+}
+
+}  // namespace
+
+int alm2cl_chunks(int mmax) { return (mmax + kAlmChunk) / kAlmChunk; }
+
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, double* W, cudaStream_t s)
+{
+    dim3 grid((p.lout + kAlmThreads) / kAlmThreads, p.nmchunks, p.nterms);
+    k_alm2cl_partial<<<grid, kAlmThreads, 0, s>>>(p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_alm2cl_reduce<<<(p.lout + 256) / 256, 256, 0, s>>>(p.partial, p.nterms, p.nmchunks, p.lout, scale, W);
+    return cudaGetLastError();
+}
+
+}  // namespace ps

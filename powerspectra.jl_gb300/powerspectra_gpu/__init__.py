@@ -10,3 +10,4 @@ from .spectralarray import BlockSpectralMatrix, SpectralArray, SpectralVector, s
 from .modecoupling import (inner_mcm00, inner_mcm02, inner_mcmMM, inner_mcmPP, inner_mcmPPMM, mcm)  # noqa: F401
 from .covariance import (ConstantDict, WindowWorkspace, coupledcov, loop_covEEEE, loop_covTEEE,  # noqa: F401
                          loop_covTEEE_planck, loop_covTETE, loop_covTTEE, loop_covTTTE, loop_covTTTT)
+from .workspace import AlmWindowWorkspace, alm2cl, n_alms, wterms  # noqa: F401

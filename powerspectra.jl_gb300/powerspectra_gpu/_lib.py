@@ -28,7 +28,7 @@ EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_sync
            "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
-           "ps_quickpol_xi")
+           "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -106,6 +106,12 @@ def load(path=None):
         lib.ps_solve.restype = ci
         lib.ps_quickpol_xi.argtypes = [vp, ci, ci, ci, ci, _DP, i64, ci, ci, ci, _DP, i64]
         lib.ps_quickpol_xi.restype = ci
+        lib.ps_decouple_covmat_device.argtypes = [vp, _DP, _DP, _DP, i64, i64, _DP, i64]
+        lib.ps_decouple_covmat_device.restype = ci
+        lib.ps_window_W.argtypes = [vp, _DPP, _DPP, ci, ci, ci, ci, _DP]
+        lib.ps_window_W.restype = ci
+        lib.ps_window_W_device.argtypes = [vp, _DPP, _DPP, ci, ci, ci, ci, _DP]
+        lib.ps_window_W_device.restype = ci
         lib.ps_last_kernel_ms.argtypes = [vp]
         lib.ps_last_kernel_ms.restype = ctypes.c_double
         lib.ps_launch_count.argtypes = [vp]
@@ -233,6 +239,45 @@ class Context:
         self.check(self.lib.ps_quickpol_xi(self.handle, int(nu1), int(nu2), int(s1), int(s2), dptr(W), len(W), lmax,
                                            int(bl), int(bu), dptr(X), n))
         return X
+
+    def window_W(self, A, B, lmax, mmax=None, lout=None):
+        """(1/nterms) sum_t alm2cl(A[t], B[t])[0:lout] for host complex128 coefficient sets in the
+        HEALPix m-major order (None = all-zero set).  window_function_W!, src/workspace.jl:174-213."""
+        mmax = lmax if mmax is None else mmax
+        lout = lmax if lout is None else lout
+        if len(A) != len(B):
+            raise PowerSpectraArgumentError(PS_ERR_ARG, "A and B need the same number of terms")
+        nalm = (mmax + 1) * (mmax + 2) // 2 + (mmax + 1) * (lmax - mmax)
+        keep, pa, pb = [], [], []
+        for lst, out in ((A, pa), (B, pb)):
+            for a in lst:
+                if a is None:
+                    out.append(None)
+                    continue
+                a = np.ascontiguousarray(a, dtype=np.complex128)
+                if a.shape != (nalm,):
+                    raise PowerSpectraArgumentError(PS_ERR_ARG, "a coefficient set needs %d entries" % nalm)
+                keep.append(a)
+                out.append(a.view(np.float64))
+        # an auto-spectrum term names one array twice: pass the same pointer so it is copied once
+        for t in range(len(A)):
+            if A[t] is not None and A[t] is B[t]:
+                pb[t] = pa[t]
+        W = np.empty(lout + 1, dtype=np.float64)
+        self.check(self.lib.ps_window_W(self.handle, dptr_array(pa), dptr_array(pb), len(A), lmax, mmax, lout,
+                                        dptr(W)))
+        return W
+
+    def window_W_device(self, dA, dB, lmax, mmax, lout, dW):
+        """Device variant: dA / dB are lists of device addresses (int, or None for a zero set)."""
+        self.check(self.lib.ps_window_W_device(self.handle, dptr_array([None if a is None else int(a) for a in dA]),
+                                               dptr_array([None if b is None else int(b) for b in dB]), len(dA),
+                                               lmax, mmax, lout, dptr(int(dW))))
+
+    def decouple_covmat_device(self, dY, dB1, dB2, n, ld, dout, ldout):
+        """decouple_covmat on device matrices (addresses as ints)."""
+        self.check(self.lib.ps_decouple_covmat_device(self.handle, dptr(int(dY)), dptr(int(dB1)), dptr(int(dB2)), n,
+                                                      ld, dptr(int(dout)), ldout))
 
     def decouple_covmat(self, Y, B1, B2):
         """B1^-1 Y B2^-T (decouple_covmat, src/covariance.jl:8-14) for square float64 matrices."""

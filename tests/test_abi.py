@@ -15,7 +15,7 @@ def _header_symbols():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         txt = open(h).read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-        for m in re.finditer(r"\b(ps_[a-z0-9_]+)\s*\(", txt):
+        for m in re.finditer(r"\b(ps_[A-Za-z0-9_]+)\s*\(", txt):
             syms.add(m.group(1))
     return syms
 

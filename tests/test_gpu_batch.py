@@ -23,8 +23,9 @@ def _dev(a):
     return torch.tensor(np.ascontiguousarray(a), device="cuda")
 
 
-@pytest.mark.parametrize("mode,tol", [("plain", 1e-12), ("chosen", 1e-6)])
-def test_mcm_set_device(ctx, mode, tol):
+@pytest.mark.parametrize("mode,tol,cases", [("plain", 1e-12, 0xF), ("chosen", 1e-6, 0xF), ("chosen", 1e-6, 0xC),
+                                            ("chosen", 1e-6, 0x4), ("chosen", 1e-6, 0x2), ("chosen", 1e-6, 0x9)])
+def test_mcm_set_device(ctx, mode, tol, cases):
     L, K = 90, 5
     Ws = [_W(2 * L + 1, seed=k) for k in range(K)]
     dW = [_dev(w) for w in Ws]
@@ -33,12 +34,14 @@ def test_mcm_set_device(ctx, mode, tol):
     ptrs = [dM[k, s].data_ptr() for k in range(K) for s in range(4)]
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     try:
-        ctx.mcm_set_device(0xF, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, ptrs, n, mode=mode)
+        ctx.mcm_set_device(cases, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, ptrs, n, mode=mode)
         torch.cuda.synchronize()
     finally:
         ctx.set_stream(0)
     for k in range(K):
         for s in range(4):
+            if not cases & (1 << s):
+                continue
             got = dM[k, s].cpu().numpy().T
             ref = o.inner_mcm(s, Ws[k], 0, L)
             assert max_err_scaled(got, ref, cond_scale(s, Ws[k], 0, L)) < tol, (k, s)
@@ -50,7 +53,7 @@ def _batch_problems(seed=3):
     for i in range(7):
         L = int(rng.choice([40, 77, 128, 200, 255]))
         K = int(rng.integers(1, 6))
-        cases = [0x1, 0xC, 0xF, 0x2][i % 4]
+        cases = [0x1, 0xC, 0xF, 0x2, 0x4, 0x8, 0x3][i]  # every batch body, and a split combination
         lmin = [0, 0, 2, 0, 5, 0, 0][i]
         n = L - lmin + 1
         Ws = [_W(2 * L + 1, seed=100 * i + k) for k in range(K)]

@@ -53,3 +53,21 @@ def test_singular_is_an_argument_error(ctx):
     with pytest.raises(pg.PowerSpectraArgumentError, match="singular"):
         ctx.decouple_covmat(np.eye(4), Z, np.eye(4))
     assert np.allclose(ctx.solve(np.eye(3) * 2, np.ones(3)), 0.5)  # context still usable
+
+
+def test_decouple_device_matches_host(ctx):
+    """ps_decouple_covmat_device on a covariance that stays on the GPU."""
+    import torch
+    from powerspectra_gpu import synthetic as syn
+    L = 256
+    W = syn.mask_spectrum(L + 1, 0.6, 100.0, seed=3)
+    M = ctx.mcm(0, W, 2, L, mode="plain")
+    rng = np.random.default_rng(4)
+    X = rng.random(M.shape)
+    C = X.T @ X
+    n = M.shape[0]
+    dC, dM = (torch.from_numpy(np.asfortranarray(x).ravel(order="F")).cuda() for x in (C, M))
+    dout = torch.empty(n * (n + 3), dtype=torch.float64, device="cuda")  # ldout = n + 3
+    ctx.decouple_covmat_device(dC.data_ptr(), dM.data_ptr(), dM.data_ptr(), n, n, dout.data_ptr(), n + 3)
+    got = dout.cpu().numpy().reshape((n + 3, n), order="F")[:n]
+    np.testing.assert_allclose(got, ctx.decouple_covmat(C, M, M), rtol=1e-12, atol=1e-14 * np.abs(got).max())

@@ -159,3 +159,39 @@ def test_quickpol_oracle_diagonal_known_answer():
     l = np.arange(lmax + 1)
     np.testing.assert_allclose(np.diag(X)[2:], 3.0 / (2 * l[2:] + 1), rtol=1e-14)
     assert np.max(np.abs(X - np.diag(np.diag(X)))) < 1e-16
+
+
+def test_alm2cl_oracle_against_direct_sum_over_m():
+    """The oracle's alm2cl (vectorised over l) against the definition written as a sum over
+    m = -l..l, with a_{l,-m} = (-1)^m conj(a_lm) for a real field."""
+    lmax, mmax = 40, 25
+    rng = np.random.default_rng(11)
+    n = o.n_alms(lmax, mmax)
+    a = rng.normal(size=n) + 1j * rng.normal(size=n)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    a[:lmax + 1] = a[:lmax + 1].real
+    b[:lmax + 1] = b[:lmax + 1].real
+    cl = o.alm2cl(a, b, lmax, mmax)
+    for l in range(lmax + 1):
+        s = 0.0 + 0.0j
+        for m in range(-min(l, mmax), min(l, mmax) + 1):
+            i = o.alm_index(l, abs(m), lmax)
+            am = a[i] if m >= 0 else (-1) ** m * np.conj(a[i])
+            bm = b[i] if m >= 0 else (-1) ** m * np.conj(b[i])
+            s += am * np.conj(bm)
+        assert abs(s.imag) < 1e-12
+        assert abs(cl[l] - s.real / (2 * l + 1)) < 1e-13 * max(1.0, abs(s.real))
+
+
+def test_alm2cl_known_answers():
+    lmax, mmax = 60, 20
+    ones = np.ones(o.n_alms(lmax, mmax), dtype=complex)
+    l = np.arange(lmax + 1)
+    np.testing.assert_allclose(o.alm2cl(ones, ones, lmax, mmax), (1 + 2 * np.minimum(l, mmax)) / (2 * l + 1.0))
+    # a field with one axisymmetric mode: a_l0 = c at l = 7 only -> cl[7] = c^2 / 15
+    a = np.zeros(o.n_alms(lmax, lmax), dtype=complex)
+    a[o.alm_index(7, 0, lmax)] = 3.0
+    cl = o.alm2cl(a, a, lmax)
+    assert cl[7] == 9.0 / 15 and np.count_nonzero(cl) == 1
+    # window_function_W! mean: a zero (None) term counts
+    np.testing.assert_allclose(o.window_function_W([a, None], [a, a], lmax), 0.5 * cl)
