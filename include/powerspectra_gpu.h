@@ -123,8 +123,8 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * selected in `cases`, dM[4*k + s] receives the matrix (entries of unselected
  * cases are ignored).  This is `mcm` for a set of spectra (the reference calls
  * inner_mcm*! once per spectrum and case, src/modecoupling.jl:192-246).  The
- * (window, case) slots are processed in groups of up to 8 sharing one
- * generation of the families per pair.  Device pointers; enqueued on the
+ * (window, case) slots are processed in groups (up to 4 in chosen mode, 8 in
+ * plain FP64) sharing one generation of the families per pair.  Device pointers; enqueued on the
  * context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
@@ -159,6 +159,15 @@ int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double 
  * matrix. */
 int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *W, int64_t nW, int lmax, int bl,
                    int bu, double *Xi, int64_t ldx);
+/* quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2) (src/beam.jl:72-109) from the
+ * effective scan weights themselves: W = quickpolW(omega1, omega2)
+ * (src/beam.jl:40-53), W[l'] = sum_m omega1_l'm conj(omega2_l'm) over m = -l'..l'
+ * (m = 0 once, m > 0 twice), is formed on the GPU and then used as in
+ * ps_quickpol_xi, with W[l'] = 0 beyond alm_lmax.  omega1 / omega2 are host
+ * coefficient sets (interleaved re, im; HEALPix m-major order, alm_lmax /
+ * alm_mmax). */
+int ps_quickpol_xi_alm(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *omega1, const double *omega2,
+                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, double *Xi, int64_t ldx);
 
 /* Mask spectra from harmonic coefficients (alm2cl): for l = 0..lout,
  *   W[l] = (1/nterms) sum_t cl(A[t], B[t])[l],

@@ -205,3 +205,9 @@ def window_function_W(A, B, lmax, mmax=None, lout=None):
         if a is not None and b is not None:
             res += alm2cl(a, b, lmax, mmax)[:lout + 1]
     return res * (1.0 / len(A))
+
+
+def quickpolW(a, b, lmax, mmax=None):
+    """quickpolW (src/beam.jl:40-53): sum over m = -l..l of a_lm conj(b_lm), i.e. alm2cl without
+    the 1/(2l+1)."""
+    return alm2cl(a, b, lmax, mmax) * (2.0 * np.arange(lmax + 1) + 1.0)

@@ -924,7 +924,7 @@ int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W,
 
 // Shared by ps_window_W and ps_window_W_device: dA/dB are device sets (null = zeros).
 static int window_run(ps_ctx* c, const double* const* dA, const double* const* dB, int nterms, int lmax, int mmax,
-                      int lout, double* dW)
+                      int lout, double* dW, bool per_l = true)
 {
     ps::AlmParams p = {};
     p.nterms = nterms;
@@ -941,7 +941,7 @@ static int window_run(ps_ctx* c, const double* const* dA, const double* const* d
     if (st) return st;
     p.partial = c->d_part;
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    PS_CUDA(c, ps::launch_alm2cl(p, 1.0 / nterms, dW, c->stream));
+    PS_CUDA(c, ps::launch_alm2cl(p, 1.0 / nterms, per_l, dW, c->stream));
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->launches += 2;
     c->timed = true;
@@ -1002,6 +1002,46 @@ int ps_window_W(ps_ctx* c, const double* const* A, const double* const* B, int n
     }
     if ((st = window_run(c, dA, dB, nterms, lmax, mmax, lout, c->d_out))) return st;
     PS_CUDA(c, cudaMemcpyAsync(W, c->d_out, ((size_t)lout + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
+int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* omega1, const double* omega2,
+                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, double* Xi, int64_t ldx)
+{
+    if (!c) return PS_ERR_ARG;
+    if (!omega1 || !omega2 || !Xi) return set_err(c, PS_ERR_ARG, "omega1, omega2 and Xi must not be NULL");
+    if (alm_lmax < 0 || alm_lmax > 65535 || alm_mmax < 0 || alm_mmax > alm_lmax)
+        return set_err(c, PS_ERR_ARG, "need 0 <= alm_mmax <= alm_lmax <= 65535");
+    if (lmax < 0 || lmax > PS_MAX_LMAX || bl < 0 || bu < 0 || ldx < (int64_t)lmax + 1)
+        return set_err(c, PS_ERR_ARG, "need 0 <= lmax <= %d, bandwidths >= 0, ldx >= lmax+1", PS_MAX_LMAX);
+    if (abs(nu1) > 64 || abs(nu2) > 64 || abs(s1) > 64 || abs(s2) > 64)
+        return set_err(c, PS_ERR_ARG, "spins beyond +-64 are not supported");
+    PS_CUDA(c, cudaSetDevice(c->device));
+    // quickpolW on the GPU: sum_m omega1_lm conj(omega2_lm), no 1 / (2l + 1)
+    const size_t nalm = (size_t)(alm_mmax + 1) * (alm_mmax + 2) / 2 + (size_t)(alm_mmax + 1) * (alm_lmax - alm_mmax);
+    const bool same = omega1 == omega2;
+    int st;
+    if ((st = ensure(c, &c->d_alm, &c->alm_cap, 2 * nalm * (same ? 1 : 2)))) return st;
+    if ((st = ensure(c, &c->d_spec, &c->spec_cap, (size_t)alm_lmax + 1))) return st;
+    const size_t n = (size_t)lmax + 1;
+    if ((st = ensure(c, &c->d_out, &c->out_cap, n * n))) return st;
+    PS_CUDA(c, cudaMemcpyAsync(c->d_alm, omega1, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const double* dA = c->d_alm;
+    const double* dB = c->d_alm;
+    if (!same) {
+        PS_CUDA(c, cudaMemcpyAsync(c->d_alm + 2 * nalm, omega2, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->stream));
+        dB = c->d_alm + 2 * nalm;
+    }
+    if ((st = window_run(c, &dA, &dB, 1, alm_lmax, alm_mmax, alm_lmax, c->d_spec, false))) return st;
+    PS_CUDA(c, cudaMemsetAsync(c->d_out, 0, n * n * sizeof(double), c->stream));
+    PS_CUDA(c, ps::launch_quickpol(c->d_spec, (long long)alm_lmax + 1, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out,
+                                   (long long)n, c->stream));
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->launches++;
+    PS_CUDA(c, cudaMemcpy2DAsync(Xi, (size_t)ldx * sizeof(double), c->d_out, n * sizeof(double), n * sizeof(double), n,
+                                 cudaMemcpyDeviceToHost, c->stream));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PS_OK;
 }

@@ -73,7 +73,7 @@ struct BatchParams {
 // Launchers (ps_plain_fp64.cu, ps_chosen.cu).
 cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, cudaStream_t s);
 int batch_blocks_per_sm();
-int chosen_batch_template(const CouplingParams& p);  // compile-time slot set of a batch group (0: generic)
+int chosen_batch_template(const CouplingParams& p);  // compile-time slot set of a batch group (0: none fits)
 cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s);
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s);
@@ -100,7 +100,7 @@ struct AlmParams {
     double* partial;  // nterms * nmchunks * (lout + 1)
 };
 int alm2cl_chunks(int mmax);
-cudaError_t launch_alm2cl(const AlmParams& p, double scale, double* W, cudaStream_t s);
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s);
 
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);

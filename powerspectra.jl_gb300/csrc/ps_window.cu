@@ -4,7 +4,8 @@
 //   * window_function_W! (src/workspace.jl:174-213): the average over the
 //     (wX, wY) weight terms of alm2cl(w_X, w_Y)[0:lmax] (Planck 2015 eq. C.11-C.16);
 //   * the mask cross-spectrum of mcm (src/modecoupling.jl:197, :234) and the
-//     pseudo-spectra of master (src/modecoupling.jl:357-373), one term each.
+//     pseudo-spectra of master (src/modecoupling.jl:357-373), one term each;
+//   * quickpolW (src/beam.jl:40-53), the same sum without the 1 / (2l + 1).
 //
 // The cross-spectrum of two coefficient sets of a real field is the published
 // definition
@@ -58,18 +59,20 @@ __global__ void __launch_bounds__(kAlmThreads) k_alm2cl_partial(AlmParams p)
     if (l <= p.lout) p.partial[((long long)t * p.nmchunks + c) * (p.lout + 1) + l] = acc;
 }
 
-// W[l] = scale * sum_t (sum_c partial[t][c][l]) / (2l + 1), in a fixed order.
+// W[l] = scale * sum_t (sum_c partial[t][c][l]) / (2l + 1), in a fixed order
+// (without the 1 / (2l + 1) when per_l is 0: the scan-pattern spectrum of quickpolW).
 __global__ void k_alm2cl_reduce(const double* __restrict__ partial, int nterms, int nmchunks, int lout, double scale,
-                                double* __restrict__ W)
+                                int per_l, double* __restrict__ W)
 {
     const int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l > lout) return;
-    const double inv = 1.0 / (2.0 * l + 1.0);
+    const double inv = per_l ? 1.0 / (2.0 * l + 1.0) : 1.0;
     double s = 0.0;
     for (int t = 0; t < nterms; ++t) {
         double ct = 0.0;
         const double* q = partial + (long long)t * nmchunks * (lout + 1) + l;
-        for (int c = 0; c < nmchunks; ++c) ct += q[(long long)c * (lout + 1)];
+#pragma unroll 16
+        for (int c = 0; c < nmchunks; ++c) ct += __ldg(q + (long long)c * (lout + 1));  // loads issue ahead of the adds
         s += ct * inv;
     }
     W[l] = s * scale;
@@ -79,13 +82,13 @@ __global__ void k_alm2cl_reduce(const double* __restrict__ partial, int nterms, 
 
 int alm2cl_chunks(int mmax) { return (mmax + kAlmChunk) / kAlmChunk; }
 
-cudaError_t launch_alm2cl(const AlmParams& p, double scale, double* W, cudaStream_t s)
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s)
 {
     dim3 grid((p.lout + kAlmThreads) / kAlmThreads, p.nmchunks, p.nterms);
     k_alm2cl_partial<<<grid, kAlmThreads, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_alm2cl_reduce<<<(p.lout + 256) / 256, 256, 0, s>>>(p.partial, p.nterms, p.nmchunks, p.lout, scale, W);
+    k_alm2cl_reduce<<<(p.lout + 128) / 128, 128, 0, s>>>(p.partial, p.nterms, p.nmchunks, p.lout, scale, per_l ? 1 : 0, W);
     return cudaGetLastError();
 }
 

@@ -6,6 +6,9 @@
 #     inner_mcm⁰⁰!, inner_mcm⁰²!, inner_mcm⁺⁺!, inner_mcm⁻⁻!   (src/modecoupling.jl:78-159)
 #     loop_covTTTT!, loop_covEEEE!, loop_covTTTE!, loop_covTETE!,
 #     loop_covTEEE!, loop_covTEEE_planck!, loop_covTTEE!        (src/covariance.jl:92-446)
+#     decouple_covmat                                            (src/covariance.jl:8-14)
+#     quickpolΞ!                                                 (src/beam.jl:72-109)
+#     window_function_W!                                         (src/workspace.jl:174-213)
 # so `mcm`, `coupledcov` and `master` keep their signatures and return types
 # while the (l1, l2) loops run on the GPU.  There is no CPU fallback: a missing
 # library or device raises.
@@ -13,6 +16,7 @@ module PowerSpectraGPU
 
 using PowerSpectra
 import PowerSpectra: SpectralArray, SpectralVector
+import Healpix
 
 const libps = get(ENV, "POWERSPECTRA_GPU_LIB",
                   joinpath(@__DIR__, "..", "lib", "libpowerspectra_gpu.so"))
@@ -113,6 +117,71 @@ PowerSpectra.loop_covTEEE_planck!(𝐂::FMat, EEjq::SV, EEjp::SV, TEip::SV, TEiq
     gpu_cov!(:TEEE_planck, 𝐂, (EEjq, EEjp, TEip, TEiq), (r_EE_jq, r_EE_jp), (W1, W2, W3, W4))
 PowerSpectra.loop_covTTEE!(𝐂::FMat, TEip::SV, TEiq::SV, TEjq::SV, TEjp::SV, W1, W2) =
     gpu_cov!(:TTEE, 𝐂, (TEip, TEiq, TEjq, TEjp), (), (W1, W2))
+
+# ---- rows downstream and upstream of the loops ----------------------------------------------
+
+# decouple_covmat (src/covariance.jl:8-14): B1^-1 Y B2^-T by two FP64 LU solves on the GPU
+function PowerSpectra.decouple_covmat(Y::FMat, B1::FMat, B2::FMat)
+    M = deepcopy(Y)
+    C = parent(M)
+    n = size(C, 1)
+    Yp, B1p, B2p = collect(parent(Y)), collect(parent(B1)), collect(parent(B2))  # dense, ld = n
+    c = ctx()
+    st = ccall((:ps_decouple_covmat, libps), Cint,
+               (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64, Int64, Ptr{Float64}, Int64),
+               c, Yp, B1p, B2p, n, n, C, stride(C, 2))
+    check(st, c)
+    return M
+end
+
+# quickpolΞ! (src/beam.jl:72-109): quickpolW and the banded Ξ on the GPU; the band is copied
+# into the caller's BandedMatrix-backed SpectralArray
+function PowerSpectra.quickpolΞ!(𝚵::SpectralArray{Float64,2}, ν₁, ν₂, s₁, s₂,
+                                 ω₁::Healpix.Alm{ComplexF64}, ω₂::Healpix.Alm{ComplexF64})
+    size(𝚵, 1) != size(𝚵, 2) && throw(ArgumentError("𝚵 is not square."))
+    lmax = lastindex(𝚵, 1)
+    bl, bu = PowerSpectra.BandedMatrices.bandwidths(parent(𝚵))
+    X = Matrix{Float64}(undef, lmax + 1, lmax + 1)
+    c = ctx()
+    st = ccall((:ps_quickpol_xi_alm, libps), Cint,
+               (Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Cint, Cint,
+                Ptr{Float64}, Int64),
+               c, ν₁, ν₂, s₁, s₂, Ptr{Float64}(pointer(ω₁.alm)), Ptr{Float64}(pointer(ω₂.alm)),
+               min(ω₁.lmax, ω₂.lmax), min(ω₁.mmax, ω₂.mmax), lmax, bl, bu, X, lmax + 1)
+    check(st, c)
+    for ℓ″ in 2:lmax, ℓ in PowerSpectra.specrowrange(𝚵, ℓ″)
+        𝚵[ℓ″, ℓ] = X[ℓ″ + 1, ℓ + 1]
+    end
+    return 𝚵
+end
+
+# window_function_W! (src/workspace.jl:174-213): the alm2cl mean over the weight terms on the
+# GPU; the effective-weight coefficients still come from effective_weight_alm! (map2alm)
+function PowerSpectra.window_function_W!(workspace::PowerSpectra.CovarianceWorkspace{Float64},
+                                         X, Y, i, j, α, p, q, β)
+    key = (X, Y, i, j, α, p, q, β)
+    haskey(workspace.W_spectra, key) && return workspace.W_spectra[key]
+    wterms(Z) = Z == :TT ? (:II,) : (Z == :PP ? (:QQ, :UU) : (Z,))
+    A, B = Healpix.Alm{ComplexF64,Vector{ComplexF64}}[], Healpix.Alm{ComplexF64,Vector{ComplexF64}}[]
+    for wX in wterms(X), wY in wterms(Y)
+        push!(A, PowerSpectra.effective_weight_alm!(workspace, wX, i, j, α))
+        push!(B, PowerSpectra.effective_weight_alm!(workspace, wY, p, q, β))
+    end
+    lmax = workspace.lmax
+    result = zeros(Float64, lmax + 1)
+    c = ctx()
+    GC.@preserve A B begin
+        pa = [Ptr{Float64}(pointer(a.alm)) for a in A]
+        pb = [Ptr{Float64}(pointer(b.alm)) for b in B]
+        st = ccall((:ps_window_W, libps), Cint,
+                   (Ptr{Cvoid}, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Cint, Cint, Cint, Cint, Ptr{Float64}),
+                   c, pa, pb, length(A), A[1].lmax, A[1].mmax, lmax, result)
+        check(st, c)
+    end
+    W = SpectralVector(result)
+    workspace.W_spectra[key] = W
+    return W
+end
 
 function __init__()
     atexit() do

@@ -28,7 +28,8 @@ EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_sync
            "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
-           "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device")
+           "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device",
+           "ps_quickpol_xi_alm")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -106,6 +107,8 @@ def load(path=None):
         lib.ps_solve.restype = ci
         lib.ps_quickpol_xi.argtypes = [vp, ci, ci, ci, ci, _DP, i64, ci, ci, ci, _DP, i64]
         lib.ps_quickpol_xi.restype = ci
+        lib.ps_quickpol_xi_alm.argtypes = [vp, ci, ci, ci, ci, _DP, _DP, ci, ci, ci, ci, ci, _DP, i64]
+        lib.ps_quickpol_xi_alm.restype = ci
         lib.ps_decouple_covmat_device.argtypes = [vp, _DP, _DP, _DP, i64, i64, _DP, i64]
         lib.ps_decouple_covmat_device.restype = ci
         lib.ps_window_W.argtypes = [vp, _DPP, _DPP, ci, ci, ci, ci, _DP]
@@ -238,6 +241,22 @@ class Context:
         X = np.empty((n, n), dtype=np.float64, order="F")
         self.check(self.lib.ps_quickpol_xi(self.handle, int(nu1), int(nu2), int(s1), int(s2), dptr(W), len(W), lmax,
                                            int(bl), int(bu), dptr(X), n))
+        return X
+
+    def quickpol_xi_alm(self, nu1, nu2, s1, s2, omega1, omega2, alm_lmax, lmax, bl, bu, alm_mmax=None):
+        """quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2) (src/beam.jl:72-109): W = quickpolW(omega1,
+        omega2) and Xi on the GPU, from complex128 scan-weight coefficient sets (HEALPix order)."""
+        alm_mmax = alm_lmax if alm_mmax is None else alm_mmax
+        nalm = (alm_mmax + 1) * (alm_mmax + 2) // 2 + (alm_mmax + 1) * (alm_lmax - alm_mmax)
+        o1 = np.ascontiguousarray(omega1, dtype=np.complex128)
+        o2 = o1 if omega2 is omega1 else np.ascontiguousarray(omega2, dtype=np.complex128)
+        if o1.shape != (nalm,) or o2.shape != (nalm,):
+            raise PowerSpectraArgumentError(PS_ERR_ARG, "a coefficient set needs %d entries" % nalm)
+        n = lmax + 1
+        X = np.empty((n, n), dtype=np.float64, order="F")
+        self.check(self.lib.ps_quickpol_xi_alm(self.handle, int(nu1), int(nu2), int(s1), int(s2),
+                                               dptr(o1.view(np.float64)), dptr(o2.view(np.float64)), alm_lmax,
+                                               alm_mmax, lmax, int(bl), int(bu), dptr(X), n))
         return X
 
     def window_W(self, A, B, lmax, mmax=None, lout=None):

@@ -39,3 +39,22 @@ def test_quickpol_known_identity(ctx):
     np.testing.assert_allclose(np.diag(X)[2:], 3.0 / (2 * l[2:] + 1), rtol=1e-13)
     off = X - np.diag(np.diag(X))
     assert np.max(np.abs(off)) < 1e-15
+
+
+@pytest.mark.parametrize("alm_lmax,alm_mmax,lmax,bl,bu", [(64, 64, 40, 6, 9), (100, 30, 50, 50, 50)])
+def test_quickpol_from_scan_weights(ctx, alm_lmax, alm_mmax, lmax, bl, bu):
+    """quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2): W = quickpolW(omega1, omega2) on the GPU,
+    then Xi, against the oracle's quickpolW and Xi."""
+    rng = np.random.default_rng(alm_lmax)
+    n = o.n_alms(alm_lmax, alm_mmax)
+    w1 = (rng.normal(size=n) + 1j * rng.normal(size=n)) * np.exp(-np.arange(n) / 500.0)
+    w2 = (rng.normal(size=n) + 1j * rng.normal(size=n)) * np.exp(-np.arange(n) / 500.0)
+    for (om1, om2) in ((w1, w2), (w1, w1)):
+        G = ctx.quickpol_xi_alm(2, 0, 2, -2, om1, om2, alm_lmax, lmax, bl, bu, alm_mmax=alm_mmax)
+        W = o.quickpolW(om1, om2, alm_lmax, alm_mmax)
+        R = o.quickpol_xi(2, 0, 2, -2, W, lmax, bl, bu)
+        scale = np.abs(o.quickpol_xi(2, 0, 2, -2, np.abs(W), lmax, bl, bu))
+        Wa = o.quickpolW(np.abs(om1).astype(complex), np.abs(om2).astype(complex), alm_lmax, alm_mmax)
+        scale = np.maximum(scale, np.abs(o.quickpol_xi(2, 0, 2, -2, Wa, lmax, bl, bu)))
+        err = np.abs(G - R) / np.maximum(np.maximum(np.abs(R), 1e-3 * scale), 1e-300)
+        assert np.max(err[scale > 0]) < 1e-10

@@ -195,3 +195,16 @@ def test_alm2cl_known_answers():
     assert cl[7] == 9.0 / 15 and np.count_nonzero(cl) == 1
     # window_function_W! mean: a zero (None) term counts
     np.testing.assert_allclose(o.window_function_W([a, None], [a, a], lmax), 0.5 * cl)
+
+
+def test_quickpolW_is_alm2cl_times_2l_plus_1():
+    lmax = 30
+    rng = np.random.default_rng(2)
+    n = o.n_alms(lmax, lmax)
+    a = rng.normal(size=n) + 1j * rng.normal(size=n)
+    W = o.quickpolW(a, a, lmax)
+    for l in (0, 5, 30):
+        # m = 0 enters once as Re(a conj a) = |a_l0|^2, every m > 0 twice
+        direct = abs(a[o.alm_index(l, 0, lmax)]) ** 2 + sum(2 * abs(a[o.alm_index(l, m, lmax)]) ** 2
+                                                            for m in range(1, l + 1))
+        assert abs(W[l] - direct) < 1e-12 * direct
