@@ -619,6 +619,75 @@ def run_window(args):
     return 0
 
 
+QUICKPOL_REF_S = 3.951  # quickpolXi!, 1000 x 1000, band 100, nu = 0, s = 2: 20 Julia threads (reference notebook)
+
+
+def run_quickpol(args):
+    """quickpol_999: quickpolXi!(Xi, 0, 0, 2, 2, omega, omega) for a 1000 x 1000 Xi (l 0..999) with
+    band (100, 100) and a scan-weight coefficient set of lmax = mmax = 30000 -- the configuration
+    of the reference's QuickPol notebook.  The set is a 7.2 GB host array; only its rows with
+    l <= 2 * 999 enter Xi (the 3j support), and those are seeded random values with a decaying
+    envelope while the rest stay zero.  One step is one host call of ps_quickpol_xi_alm: packing
+    of the used rows, the copy, quickpolW and Xi on the GPU, and the copy back."""
+    import numpy as np
+    import powerspectra_gpu as pg
+    from oracle import oracle as o
+
+    lmax, band, alm_lmax = 999, 100, 30000
+    nalm = o.n_alms(alm_lmax, alm_lmax)
+    lw = 2 * lmax
+    omega = np.zeros(nalm, dtype=np.complex128)  # untouched pages stay unallocated
+    rng = np.random.default_rng(30000)
+    for m in range(lw + 1):
+        i0 = o.alm_index(m, m, alm_lmax)
+        ls = np.arange(m, lw + 1)
+        omega[i0:i0 + len(ls)] = (rng.normal(size=len(ls)) + 1j * rng.normal(size=len(ls))) * np.exp(-ls / 600.0) \
+            / (1.0 + m)
+    omega[:lw + 1] = omega[:lw + 1].real
+    ctx = pg.Context(0)
+    for _ in range(max(args.warmup, 3)):
+        X = ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band)
+    clk = ClockSampler(0)
+    ts, ks = [], []
+    launches0 = ctx.launch_count()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        X = ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band)
+        ts.append(time.perf_counter() - t0)
+        ks.append(ctx.last_kernel_ms())
+    clocks = clk.stop()
+    launches = (ctx.launch_count() - launches0) // args.steps
+    t = statistics.median(ts)
+    # CPU: the oracle (quickpolW over the used rows in numpy, Xi in C/OpenMP on all host threads)
+    packed = np.concatenate([omega[o.alm_index(m, m, alm_lmax):o.alm_index(m, m, alm_lmax) + lw + 1 - m]
+                             for m in range(lw + 1)])
+    t0 = time.perf_counter()
+    W = o.quickpolW(packed, packed, lw)
+    R = o.quickpol_xi(0, 0, 2, 2, W, lmax, band, band)
+    cpu_dt = time.perf_counter() - t0
+    scale = np.abs(o.quickpol_xi(0, 0, 2, 2, np.abs(W), lmax, band, band))
+    mask = scale > 0
+    err = float(np.max(np.abs(X - R)[mask] / np.maximum(np.abs(R), 1e-3 * scale)[mask]))
+    line = {"metric": "quickpolXi! wall time per call (1000 x 1000, band 100, nu = 0, s = 2)", "value": t,
+            "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": t * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": t / QUICKPOL_REF_S, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "quickpol_999", "lmax": lmax, "band": [band, band], "nu": [0, 0], "s": [2, 2],
+                       "alm_lmax": alm_lmax, "alm_mmax": alm_lmax,
+                       "used_rows": "l <= %d (the 3j support); the rest of the set is zero" % lw,
+                       "step": "ps_quickpol_xi_alm on host arrays: pack, copy, quickpolW + Xi kernels, copy back"},
+            "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 16 * o.n_alms(lw, lw),
+                    "d2h_bytes_per_step": 8 * (lmax + 1) ** 2},
+            "kernel_ms": statistics.median(ks), "max_rel_err_vs_oracle": err, "clocks": clocks,
+            "gpu_launches": launches,
+            "reference_published_s": QUICKPOL_REF_S,
+            "cpu_baseline": {"value": cpu_dt, "unit": "s", "cores": o.max_threads(), "kind": "port",
+                             "sample": "the whole configuration: oracle quickpolW (numpy) + Xi (C, OpenMP)"}}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -637,6 +706,8 @@ def main():
         return run_set(args)
     if args.config == "window_W_8191":
         return run_window(args)
+    if args.config == "quickpol_999":
+        return run_quickpol(args)
     return run_ours(args)
 
 

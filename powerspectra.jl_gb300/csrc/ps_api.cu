@@ -1018,25 +1018,48 @@ int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double
     if (abs(nu1) > 64 || abs(nu2) > 64 || abs(s1) > 64 || abs(s2) > 64)
         return set_err(c, PS_ERR_ARG, "spins beyond +-64 are not supported");
     PS_CUDA(c, cudaSetDevice(c->device));
-    // quickpolW on the GPU: sum_m omega1_lm conj(omega2_lm), no 1 / (2l + 1)
-    const size_t nalm = (size_t)(alm_mmax + 1) * (alm_mmax + 2) / 2 + (size_t)(alm_mmax + 1) * (alm_lmax - alm_mmax);
+    // Xi reads W[l'] only for l' <= l + l'' <= 2 lmax, so only the coefficients
+    // with l <= lw enter; those rows are packed into a smaller set (lmax lw) on
+    // the host before the copy when the given sets reach further.
+    const int lw = std::min(alm_lmax, 2 * lmax);
+    const int mw = std::min(alm_mmax, lw);
+    const size_t nalm = (size_t)(mw + 1) * (mw + 2) / 2 + (size_t)(mw + 1) * (lw - mw);
     const bool same = omega1 == omega2;
     int st;
     if ((st = ensure(c, &c->d_alm, &c->alm_cap, 2 * nalm * (same ? 1 : 2)))) return st;
-    if ((st = ensure(c, &c->d_spec, &c->spec_cap, (size_t)alm_lmax + 1))) return st;
+    if ((st = ensure(c, &c->d_spec, &c->spec_cap, (size_t)lw + 1))) return st;
     const size_t n = (size_t)lmax + 1;
     if ((st = ensure(c, &c->d_out, &c->out_cap, n * n))) return st;
-    PS_CUDA(c, cudaMemcpyAsync(c->d_alm, omega1, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    std::vector<double> packed;
+    auto upload = [&](const double* src, double* dst) -> int {
+        if (lw == alm_lmax) {
+            PS_CUDA(c, cudaMemcpyAsync(dst, src, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+            return PS_OK;
+        }
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));  // the staging vector is reused for the second set
+        packed.resize(2 * nalm);
+        size_t at = 0;
+        for (int m = 0; m <= mw; ++m) {  // row m: l = m..lw, at m (2 alm_lmax + 1 - m) / 2 + l in the source
+            const size_t from = (size_t)m * (2 * (size_t)alm_lmax + 1 - m) / 2 + m;
+            const size_t len = (size_t)(lw - m + 1);
+            memcpy(packed.data() + 2 * at, src + 2 * from, 2 * len * sizeof(double));
+            at += len;
+        }
+        PS_CUDA(c, cudaMemcpyAsync(dst, packed.data(), 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));
+        return PS_OK;
+    };
+    if ((st = upload(omega1, c->d_alm))) return st;
     const double* dA = c->d_alm;
     const double* dB = c->d_alm;
     if (!same) {
-        PS_CUDA(c, cudaMemcpyAsync(c->d_alm + 2 * nalm, omega2, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice,
-                                   c->stream));
+        if ((st = upload(omega2, c->d_alm + 2 * nalm))) return st;
         dB = c->d_alm + 2 * nalm;
     }
-    if ((st = window_run(c, &dA, &dB, 1, alm_lmax, alm_mmax, alm_lmax, c->d_spec, false))) return st;
+    // quickpolW on the GPU: sum_m omega1_lm conj(omega2_lm), no 1 / (2l + 1)
+    if ((st = window_run(c, &dA, &dB, 1, lw, mw, lw, c->d_spec, false))) return st;
     PS_CUDA(c, cudaMemsetAsync(c->d_out, 0, n * n * sizeof(double), c->stream));
-    PS_CUDA(c, ps::launch_quickpol(c->d_spec, (long long)alm_lmax + 1, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out,
+    PS_CUDA(c, ps::launch_quickpol(c->d_spec, (long long)lw + 1, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out,
                                    (long long)n, c->stream));
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->launches++;

@@ -84,13 +84,6 @@ __device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane
     return emax;
 }
 
-// squares / products of float-float values rounded to FP32 with the low words folded in
-__device__ __forceinline__ float sq_ff(ff g) { return __fmaf_rn(2.0f * g.h, g.l, __fmul_rn(g.h, g.h)); }
-__device__ __forceinline__ float mul_ff(ff a, ff b)
-{
-    return __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmul_rn(a.h, b.h)));
-}
-
 // Window configuration: 4 bits per window, product + 1 in bits 0-1 (so a used
 // window is never 0) and parity in bits 2-3.  A non-zero SPEC fixes the
 // product and parity of every window slot at compile time (the common
@@ -109,35 +102,13 @@ __device__ __forceinline__ int wpar(const CouplingParams& p, int k)
     return SPEC ? (int)((SPEC >> (4 * k + 2)) & 3u) : p.win[k].parity;
 }
 
-// Per-direction recurrence state.  `sgn` picks the direction of the factor
-// updates: forward P(j+1) = (t+1)(2d+t+1)(2l1-t)(2l2+t+2),
-// backward P(j) = (2l1-t)(2l2-t)(1+t)(2l1+2l2+1-t).
+// Per-direction recurrence state (float-float values; the 22 family is left
+// unnormalised between steps, see ff_add_raw).
 struct Sweep {
     ff f2, f2o;   // 22 family at the current point and at the previous one
-    ff a;         // a at the previous point (forward: a(j); backward: a(j+1))
     ff f0;        // 00 family at the last even point
-    float A, B, C, D;  // integer factors of the next P
     float w;      // 2j + 1 at the current point
 };
-
-template <bool N00, bool N22, bool ODD_STEP>
-__device__ __forceinline__ void sweep_step(Sweep& s, float dA, float dB, float dC, float dD, float dw)
-{
-    ff P = ff_mul_raw(two_prod(s.A, s.B), two_prod(s.C, s.D));
-    ff r = ff_rsqrt(P);
-    if (N22) {
-        // f(next) = -(c (2j+1) f(j) + a f(prev)) / a(next), c = 4
-        ff u = ff_mul_raw(s.f2, ff_make(4.0f * s.w));
-        ff v = ff_mul_raw(s.a, s.f2o);
-        ff nf = ff_neg(ff_mul(ff_add(u, v), r));
-        s.f2o = s.f2;
-        s.f2 = nf;
-    }
-    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul(ff_mul_raw(s.a, r), s.f0));  // 00 at the next even point
-    s.a = ff_mul_raw(P, r);
-    s.A += dA; s.B += dB; s.C += dC; s.D += dD;
-    s.w += dw;
-}
 
 // The window configuration one task uses, read from the parameters once: the
 // inner loops then never reload launch parameters (which, when they live in
@@ -166,11 +137,13 @@ template <int NWIN, bool N00, bool N22, uint32_t SPEC, bool EVEN>
 __device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s, const float* sw, int slot,
                                           float* c, float& n0, float& n2)
 {
-    float x22 = N22 ? sq_ff(s.f2) : 0.0f;
+    const float g2 = N22 ? __fadd_rn(s.f2.h, s.f2.l) : 0.0f;  // the value rounded to one float
+    float x22 = __fmul_rn(g2, g2);
     if (N22) n2 = __fmaf_rn(s.w, x22, n2);
     if (EVEN) {
-        float x00 = N00 ? sq_ff(s.f0) : 0.0f;
-        float x02 = (N00 && N22) ? mul_ff(s.f0, s.f2) : 0.0f;
+        const float g0 = N00 ? __fadd_rn(s.f0.h, s.f0.l) : 0.0f;
+        float x00 = __fmul_rn(g0, g0);
+        float x02 = __fmul_rn(g0, g2);
         if (N00) n0 = __fmaf_rn(s.w, x00, n0);
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
@@ -204,11 +177,14 @@ __device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s,
 // entries), and every step then costs two float-float products instead of a
 // float-float P, 1/sqrt(P) and a(j).
 constexpr int kFEnt = kChunk / 2 + 32;  // F entries per parity of u (or v)
+struct __align__(16) ffpair {
+    ff rho, r;  // loaded together (one 16-byte shared load)
+};
 struct CoefTab {
-    ff gF_rho[kChunk], gF_r[kChunk];    // forward: sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))
-    ff fF_rho[2][kFEnt], fF_r[2][kFEnt];  // forward: sqrt(F(u)/F(u+1)), 1/sqrt(F(u+1))
-    ff gB_rho[kChunk], gB_r[kChunk];    // backward: sqrt(G'(t-1)/G'(t)), 1/sqrt(G'(t))
-    ff fB_rho[2][kFEnt], fB_r[2][kFEnt];  // backward: sqrt(F'(v+1)/F'(v)), 1/sqrt(F'(v))
+    ffpair gF[kChunk];      // forward: sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))
+    ffpair fF[2][kFEnt];    // forward: sqrt(F(u)/F(u+1)), 1/sqrt(F(u+1))
+    ffpair gB[kChunk];      // backward: sqrt(G'(t-1)/G'(t)), 1/sqrt(G'(t))
+    ffpair fB[2][kFEnt];    // backward: sqrt(F'(v+1)/F'(v)), 1/sqrt(F'(v))
 };
 
 // rho = sqrt(X / Y) and r = 1 / sqrt(Y) for X >= 0, Y > 0 (float-float)
@@ -227,13 +203,11 @@ __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1,
         ff a, b;
         if (ti < T) {
             sqrt_ratio(two_prod(t, (float)(2 * l1 + 1) - t), two_prod(t + 1.0f, (float)(2 * l1) - t), a, b);
-            tb.gF_rho[lane] = a;
-            tb.gF_r[lane] = b;
+            tb.gF[lane] = ffpair{a, b};
             sqrt_ratio(two_prod((float)(2 * l1 + 1) - t, t), two_prod((float)(2 * l1) - t, 1.0f + t), a, b);
-            tb.gB_rho[lane] = a;
-            tb.gB_r[lane] = b;
+            tb.gB[lane] = ffpair{a, b};
         } else {
-            tb.gF_rho[lane] = tb.gF_r[lane] = tb.gB_rho[lane] = tb.gB_r[lane] = zero;
+            tb.gF[lane] = tb.gB[lane] = ffpair{zero, zero};
         }
     }
     const int d0 = l2_0 - l1;
@@ -246,8 +220,7 @@ __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1,
             const float u = (float)(t0 + e);
             sqrt_ratio(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
                        two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u), a, b);
-            tb.fF_rho[e & 1][e >> 1] = a;
-            tb.fF_r[e & 1][e >> 1] = b;
+            tb.fF[e & 1][e >> 1] = ffpair{a, b};
         }
         {   // backward, v = e - t0 - 31
             const int v = e - t0 - (kChunk - 1);
@@ -258,8 +231,7 @@ __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1,
             } else {
                 a = b = zero;
             }
-            tb.fB_rho[e & 1][e >> 1] = a;
-            tb.fB_r[e & 1][e >> 1] = b;
+            tb.fB[e & 1][e >> 1] = ffpair{a, b};
         }
     }
 }
@@ -269,31 +241,34 @@ template <bool N00, bool N22, bool ODD_STEP>
 __device__ __forceinline__ void tab_step(Sweep& s, ff rho, ff r, float dw)
 {
     if (N22) {
-        ff u = ff_mul_raw(ff_mul_raw(s.f2, ff_make(4.0f * s.w)), r);
+        ff u = ff_mul_raw(ff_mulf_raw(s.f2, 4.0f * s.w), r);
         ff v = ff_mul_raw(rho, s.f2o);
-        ff nf = ff_neg(ff_add(u, v));
+        ff nf = ff_neg(ff_add_raw(u, v));
         s.f2o = s.f2;
         s.f2 = nf;
     }
-    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul(rho, s.f0));
+    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul_raw(rho, s.f0));
     s.w += dw;
 }
 
 template <bool N00, bool N22, bool ODD_STEP>
 __device__ __forceinline__ void tab_fwd(Sweep& s, const CoefTab& tb, int st, int lane)
 {
-    const int e = 2 * lane + st;  // u - t0
-    ff rho = ff_mul_raw(tb.gF_rho[st], tb.fF_rho[e & 1][e >> 1]);
-    ff r = ff_mul_raw(tb.gF_r[st], tb.fF_r[e & 1][e >> 1]);
+    const int e = lane + (st >> 1);  // (u - t0) / 2; u - t0 = 2 lane + st has the parity of the step
+    const ffpair g = tb.gF[st], f = tb.fF[ODD_STEP][e];
+    ff rho = ff_mul_raw(g.rho, f.rho);
+    ff r = ff_mul_raw(g.r, f.r);
     tab_step<N00, N22, ODD_STEP>(s, rho, r, 2.0f);
 }
 
 template <bool N00, bool N22, bool ODD_STEP>
 __device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int lane)
 {
-    const int e = 2 * lane - st + (kChunk - 1);  // v - (-t0 - 31)
-    ff rho = ff_mul_raw(tb.gB_rho[st], tb.fB_rho[e & 1][e >> 1]);
-    ff r = ff_mul_raw(tb.gB_r[st], tb.fB_r[e & 1][e >> 1]);
+    // v - (-t0 - 31) = 2 lane - st + 31: odd for even steps, half of it lane + 15 - st / 2
+    const int e = lane + (kChunk / 2 - 1) - (st >> 1);
+    const ffpair g = tb.gB[st], f = tb.fB[!ODD_STEP][e];
+    ff rho = ff_mul_raw(g.rho, f.rho);
+    ff r = ff_mul_raw(g.r, f.r);
     tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
 }
 
@@ -319,11 +294,9 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     }
 
     Sweep F, B;
-    F.f2 = ff_make(1.0f); F.f2o = ff_make(0.0f); F.a = ff_make(0.0f); F.f0 = ff_make(1.0f);
-    F.A = 1.0f; F.B = (float)(2 * d + 1); F.C = (float)(2 * l1); F.D = (float)(2 * l2 + 2);
+    F.f2 = ff_make(1.0f); F.f2o = ff_make(0.0f); F.f0 = ff_make(1.0f);
     F.w = (float)(2 * jmin + 1);
-    B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.a = ff_make(0.0f); B.f0 = ff_make(1.0f);
-    B.A = (float)(2 * l1); B.B = (float)(2 * l2); B.C = 1.0f; B.D = (float)(2 * l1 + 2 * l2 + 1);
+    B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.f0 = ff_make(1.0f);
     B.w = (float)(2 * jmax + 1);
     double FW[NWIN], BW[NWIN];
 #pragma unroll

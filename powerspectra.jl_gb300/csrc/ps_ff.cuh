@@ -74,6 +74,26 @@ __device__ __forceinline__ ff ff_mul_raw(ff x, ff y)
     return ff{p, e};
 }
 
+// x * y for a float y, left unnormalised
+__device__ __forceinline__ ff ff_mulf_raw(ff x, float y)
+{
+    float p = __fmul_rn(x.h, y);
+    return ff{p, __fmaf_rn(x.l, y, __fmaf_rn(x.h, y, -p))};
+}
+
+// x + y left unnormalised: the Knuth two_sum of the high words with the low
+// words added to its error term (the renormalising fast_two_sum is skipped).
+// Products and this sum accept unnormalised inputs; after a cancelling sum the
+// low word may exceed ulp(h), so a consumer that needs the value as one float
+// must round h + l rather than take h.
+__device__ __forceinline__ ff ff_add_raw(ff x, ff y)
+{
+    float s = __fadd_rn(x.h, y.h);
+    float bb = __fsub_rn(s, x.h);
+    float e = __fadd_rn(__fsub_rn(x.h, __fsub_rn(s, bb)), __fsub_rn(y.h, bb));
+    return ff{s, __fadd_rn(e, __fadd_rn(x.l, y.l))};
+}
+
 // 1/sqrt(P): hardware FP32 estimate, then one Newton-Raphson step
 // y' = y + y (1 - P y^2) / 2 whose residual 1 - P y^2 is formed with FMAs
 // from the exact square of y, which doubles the ~22 correct bits.

