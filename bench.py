@@ -152,7 +152,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     wl = workload(args.config)
-    stride = {"tt_767": 4}.get(args.config, 48)
+    stride = {"tt_767": 2}.get(args.config, 16)
     for _ in range(args.warmup):
         cpu_baseline(wl, stride)
     vals = [cpu_baseline(wl, stride) for _ in range(args.steps)]
@@ -342,7 +342,7 @@ def run_ours(args):
     if plain is not None:
         line["plain_fp64"] = plain
     if world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(wl, {"tt_767": 1}.get(args.config, 8))
+        line["cpu_baseline"] = cpu_baseline(wl, {"tt_767": 1}.get(args.config, 3))
     print(json.dumps(line))
     ctx.close()
     if dist is not None:

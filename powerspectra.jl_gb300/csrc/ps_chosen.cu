@@ -494,10 +494,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) k_batch_chosen(const B
             __syncwarp();
         }
         const CouplingParams& g = sG[warp];
-        const int ntask = item.w & 0xff, fam = (item.w >> 8) & 0xf, tmpl = item.w >> 12;
+        const int ntask = item.w & 0xff, tmpl = item.w >> 12;  // bits 8-11 (families) only order the queue
         for (int q = 0; q < ntask; ++q) {
             const int l2_0 = item.z + 32 * q;
-            (void)fam;
             switch (tmpl) {  // the group's compile-time slot set (prepare never emits others)
             case 1: chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
             case 2: chosen_task<4, false, true, S_PPMM2>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;

@@ -62,7 +62,8 @@ struct WinPrep {
 };
 
 // Persistent batched launch: groups[item.x] holds the coupling parameters of
-// an item (group, l1, l2_0, families: 1 = 00 only, 2 = 22 only, 3 = both).
+// an item int4 (group, l1, first l2, w) with w = tasks | families << 8 |
+// kernel body << 12 (families: 1 = 00 only, 2 = 22 only, 3 = both).
 struct BatchParams {
     const CouplingParams* groups;
     const int4* items;

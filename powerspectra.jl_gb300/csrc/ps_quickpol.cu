@@ -41,31 +41,25 @@ __device__ __forceinline__ double sgB(int j, int l1, int l2, const Fam& f)
 }
 
 // Forward step j -> j + 1 with A(j) carried in `a`: returns f(j+1) and
-// replaces `a` by A(j+1).  One rsqrt gives both 1 / (j A(j+1)) and A(j+1).
+// replaces `a` by A(j+1), so each step takes one square root and one division
+// (a correctly rounded sqrt and quotient: the rounding of the plain formula).
 // j = 0 only occurs for m3 = 0, l1 = l2, where the recurrence has no f(j-1) term.
 __device__ __forceinline__ double fwd_next(int j, int l1, int l2, const Fam& f, double fc, double fp, double& a)
 {
-    const double P1 = sgP(j + 1, l1, l2, f.m3);
-    if (j == 0) {
-        const double a1 = sqrt(P1);
-        a = a1;
-        return -((double)(f.m2 - f.m1) * fc) / a1;
-    }
-    const double q = rsqrt(P1 * ((double)j * j));  // 1 / (j A(j+1))
-    const double num = fma(sgB(j, l1, l2, f), fc, (j + 1.0) * a * fp);
-    a = P1 * q * j;  // A(j+1)
-    return -num * q;
+    const double a1 = sqrt(sgP(j + 1, l1, l2, f.m3));
+    const double num = j == 0 ? (double)(f.m2 - f.m1) * fc : fma(sgB(j, l1, l2, f), fc, (j + 1.0) * a * fp);
+    a = a1;
+    return -num / (j == 0 ? a1 : (double)j * a1);
 }
 
 // Backward step j -> j - 1 with A(j+1) carried in `a` (needs j > jmin):
 // returns h(j-1) and replaces `a` by A(j).
 __device__ __forceinline__ double bwd_next(int j, int l1, int l2, const Fam& f, double hc, double hn, double& a)
 {
-    const double P0 = sgP(j, l1, l2, f.m3);
-    const double q = rsqrt(P0 * ((j + 1.0) * (j + 1.0)));  // 1 / ((j+1) A(j))
+    const double a0 = sqrt(sgP(j, l1, l2, f.m3));
     const double num = fma(sgB(j, l1, l2, f), hc, (double)j * a * hn);
-    a = P0 * q * (j + 1.0);  // A(j)
-    return -num * q;
+    a = a0;
+    return -num / ((j + 1.0) * a0);
 }
 
 __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict__ W, long long nW, int lmax, int bl,
