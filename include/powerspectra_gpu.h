@@ -154,11 +154,13 @@ int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double 
  * over the two families' common support (Xisum, src/beam.jl:17-28), W[l'] = 0
  * for l' >= nW.  W is the scan-pattern spectrum (quickpolW); Xi is a dense
  * column-major (lmax+1) x (lmax+1) matrix (ld >= lmax+1) that receives the
- * band and zeros elsewhere.  FP64, general spins; host pointers.  The
- * reference stores Xi as a BandedMatrix; here the band is written into a dense
- * matrix. */
+ * band and zeros elsewhere.  General spins (|nu|, |s| <= 64); host pointers.
+ * mode PS_MODE_PLAIN_FP64 runs the recurrences in FP64 like the reference;
+ * PS_MODE_CHOSEN runs them in float-float on the FP32 pipe (max relative error
+ * 1e-6 against FP64).  The reference stores Xi as a BandedMatrix; here the
+ * band is written into a dense matrix. */
 int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *W, int64_t nW, int lmax, int bl,
-                   int bu, double *Xi, int64_t ldx);
+                   int bu, int mode, double *Xi, int64_t ldx);
 /* quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2) (src/beam.jl:72-109) from the
  * effective scan weights themselves: W = quickpolW(omega1, omega2)
  * (src/beam.jl:40-53), W[l'] = sum_m omega1_l'm conj(omega2_l'm) over m = -l'..l'
@@ -167,7 +169,7 @@ int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *
  * coefficient sets (interleaved re, im; HEALPix m-major order, alm_lmax /
  * alm_mmax). */
 int ps_quickpol_xi_alm(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *omega1, const double *omega2,
-                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, double *Xi, int64_t ldx);
+                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, int mode, double *Xi, int64_t ldx);
 
 /* Mask spectra from harmonic coefficients (alm2cl): for l = 0..lout,
  *   W[l] = (1/nterms) sum_t cl(A[t], B[t])[l],

@@ -432,8 +432,8 @@ int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, co
  * two families (Xisum, src/beam.jl:17-28), W[l'] = 0 for l' >= nW, and
  * sgn = (-1)^(s1+s2+nu1+nu2).  Xi is dense column-major (lmax+1)^2; entries
  * outside the band are left untouched. */
-int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
-                   long ldx, int nthreads)
+static int quickpol_xi_impl(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
+                            double *Xi, long ldx, int nthreads, int absmode)
 {
     if (lmax < 0 || bl < 0 || bu < 0 || ldx < lmax + 1) return 1;
     int nt = nthreads_or_default(nthreads);
@@ -462,12 +462,28 @@ int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, i
                 int b = b1 < b2 ? b1 : b2;
                 if (b > nW - 1) b = (int)(nW - 1);
                 double acc = 0.0;
-                for (int lp = a; lp <= b; ++lp) acc += W[lp] * f1[lp - j1] * f2[lp - j2];
-                Xi[(long)lpp + (long)l * ldx] = sgn * acc;
+                if (absmode)
+                    for (int lp = a; lp <= b; ++lp) acc += fabs(W[lp] * f1[lp - j1] * f2[lp - j2]);
+                else
+                    for (int lp = a; lp <= b; ++lp) acc += W[lp] * f1[lp - j1] * f2[lp - j2];
+                Xi[(long)lpp + (long)l * ldx] = absmode ? acc : sgn * acc;
             }
         }
         free(f1);
         free(f2);
     }
     return err;
+}
+
+int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
+                   long ldx, int nthreads)
+{
+    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 0);
+}
+
+/* The same sums over |W f1 f2| (the sum of |terms| behind each element). */
+int or_quickpol_xi_abs(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
+                       double *Xi, long ldx, int nthreads)
+{
+    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 1);
 }

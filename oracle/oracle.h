@@ -40,6 +40,9 @@ int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, co
  * rows l'' = 2..lmax, columns l within the band [l''-bl, l''+bu], l >= 2. */
 int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
                    long ldx, int nthreads);
+/* The same sums over |W f1 f2|: the sum of |terms| behind each element. */
+int or_quickpol_xi_abs(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
+                       double *Xi, long ldx, int nthreads);
 
 int or_cov_nwindows(int kind);
 int or_max_threads(void);

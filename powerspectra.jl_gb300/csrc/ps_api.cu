@@ -51,6 +51,8 @@ struct ps_ctx {
     size_t alm_cap = 0;
     double* d_part = nullptr;  // alm2cl partial sums
     size_t part_cap = 0;
+    double* d_qp = nullptr;  // chosen QuickPol scratch: W as floats and its exponent
+    size_t qp_cap = 0;
     // batched workload state (ps_batch_*)
     struct Batch {
         bool ready = false;
@@ -382,6 +384,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_bf);
     cudaFree(c->d_alm);
     cudaFree(c->d_part);
+    cudaFree(c->d_qp);
     batch_release(c);
     ps_linalg_free(c->la);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -894,8 +897,27 @@ int ps_solve(ps_ctx* c, const double* M, int64_t n, int64_t ldm, const double* b
     return st;
 }
 
+// The Xi kernel of either arithmetic on a device W (nW entries) into c->d_out.
+static int quickpol_run(ps_ctx* c, const double* dW, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1,
+                        int s2, int mode)
+{
+    const size_t n = (size_t)lmax + 1;
+    if (mode == PS_MODE_CHOSEN) {
+        const size_t nf = (size_t)nW / 2 + 2;  // nW floats, then one int
+        int st = ensure(c, &c->d_qp, &c->qp_cap, nf + 1);
+        if (st) return st;
+        PS_CUDA(c, ps::launch_quickpol_ff(dW, nW, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out, (long long)n,
+                                          (float*)c->d_qp, (int*)(c->d_qp + nf), c->stream));
+        c->launches += 2;
+    } else {
+        PS_CUDA(c, ps::launch_quickpol(dW, nW, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out, (long long)n, c->stream));
+        c->launches++;
+    }
+    return PS_OK;
+}
+
 int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W, int64_t nW, int lmax, int bl, int bu,
-                   double* Xi, int64_t ldx)
+                   int mode, double* Xi, int64_t ldx)
 {
     if (!c) return PS_ERR_ARG;
     if (!W || !Xi) return set_err(c, PS_ERR_ARG, "W and Xi must not be NULL");
@@ -903,6 +925,7 @@ int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W,
         return set_err(c, PS_ERR_ARG, "need 0 <= lmax <= %d, nW >= 1, bandwidths >= 0, ldx >= lmax+1", PS_MAX_LMAX);
     if (abs(nu1) > 64 || abs(nu2) > 64 || abs(s1) > 64 || abs(s2) > 64)
         return set_err(c, PS_ERR_ARG, "spins beyond +-64 are not supported");
+    if (mode != PS_MODE_PLAIN_FP64 && mode != PS_MODE_CHOSEN) return set_err(c, PS_ERR_ARG, "unknown mode %d", mode);
     PS_CUDA(c, cudaSetDevice(c->device));
     const size_t n = (size_t)lmax + 1;
     const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
@@ -912,9 +935,8 @@ int ps_quickpol_xi(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* W,
     PS_CUDA(c, cudaMemcpyAsync(c->d_raw, W, (size_t)nuse * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     PS_CUDA(c, cudaMemsetAsync(c->d_out, 0, n * n * sizeof(double), c->stream));
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    PS_CUDA(c, ps::launch_quickpol(c->d_raw, nuse, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out, (long long)n, c->stream));
+    if ((st = quickpol_run(c, c->d_raw, nuse, lmax, bl, bu, nu1, nu2, s1, s2, mode))) return st;
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-    c->launches++;
     c->timed = true;
     PS_CUDA(c, cudaMemcpy2DAsync(Xi, (size_t)ldx * sizeof(double), c->d_out, n * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDeviceToHost, c->stream));
@@ -1007,7 +1029,7 @@ int ps_window_W(ps_ctx* c, const double* const* A, const double* const* B, int n
 }
 
 int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double* omega1, const double* omega2,
-                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, double* Xi, int64_t ldx)
+                       int alm_lmax, int alm_mmax, int lmax, int bl, int bu, int mode, double* Xi, int64_t ldx)
 {
     if (!c) return PS_ERR_ARG;
     if (!omega1 || !omega2 || !Xi) return set_err(c, PS_ERR_ARG, "omega1, omega2 and Xi must not be NULL");
@@ -1017,6 +1039,7 @@ int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double
         return set_err(c, PS_ERR_ARG, "need 0 <= lmax <= %d, bandwidths >= 0, ldx >= lmax+1", PS_MAX_LMAX);
     if (abs(nu1) > 64 || abs(nu2) > 64 || abs(s1) > 64 || abs(s2) > 64)
         return set_err(c, PS_ERR_ARG, "spins beyond +-64 are not supported");
+    if (mode != PS_MODE_PLAIN_FP64 && mode != PS_MODE_CHOSEN) return set_err(c, PS_ERR_ARG, "unknown mode %d", mode);
     PS_CUDA(c, cudaSetDevice(c->device));
     // Xi reads W[l'] only for l' <= l + l'' <= 2 lmax, so only the coefficients
     // with l <= lw enter; those rows are packed into a smaller set (lmax lw) on
@@ -1059,10 +1082,8 @@ int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double
     // quickpolW on the GPU: sum_m omega1_lm conj(omega2_lm), no 1 / (2l + 1)
     if ((st = window_run(c, &dA, &dB, 1, lw, mw, lw, c->d_spec, false))) return st;
     PS_CUDA(c, cudaMemsetAsync(c->d_out, 0, n * n * sizeof(double), c->stream));
-    PS_CUDA(c, ps::launch_quickpol(c->d_spec, (long long)lw + 1, lmax, bl, bu, nu1, nu2, s1, s2, c->d_out,
-                                   (long long)n, c->stream));
+    if ((st = quickpol_run(c, c->d_spec, (long long)lw + 1, lmax, bl, bu, nu1, nu2, s1, s2, mode))) return st;
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-    c->launches++;
     PS_CUDA(c, cudaMemcpy2DAsync(Xi, (size_t)ldx * sizeof(double), c->d_out, n * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDeviceToHost, c->stream));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -462,10 +462,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coup
 }
 
 // Persistent batched kernel: every warp takes the next item of a work queue
-// ordered by decreasing family length (longest first), across all problems
-// and window groups of the batch, until the queue is empty.  An item is up to
-// 8 warp tasks (256 consecutive l2) of one row of one window group; the
-// group's CouplingParams live in global memory.
+// that spans all problems and window groups of the batch, until the queue is
+// empty.  The queue is ordered by kernel body (the group's compile-time slot
+// list), then by decreasing family length.  An item is up to 8 warp tasks (256
+// consecutive l2) of one row of one window group; each warp copies its
+// group's CouplingParams from global into shared memory when the group
+// changes.
 template <int NWIN>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) k_batch_chosen(const BatchParams bp)
 {

@@ -19,7 +19,7 @@
 
 namespace ps {
 
-constexpr int kMaxWin = 8;       // windows per launch of the generic coupling kernel
+constexpr int kMaxWin = 8;       // windows (slots) per coupling launch
 constexpr int kWarpsPerBlock = 4;
 constexpr double kInv4Pi = 0.079577471545947667884;  // 1 / (4 pi)
 
@@ -87,6 +87,9 @@ cudaError_t launch_fma_probe(int fp64, double* sink, int blocks, int iters, cuda
 cudaError_t launch_transpose(double* dst, const double* src, int n, cudaStream_t s);
 cudaError_t launch_quickpol(const double* W, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1, int s2,
                             double* Xi, long long ldx, cudaStream_t s);
+// The chosen-arithmetic QuickPol Xi (ps_quickpol_ff.cu); wf: nW floats, e: one int of scratch.
+cudaError_t launch_quickpol_ff(const double* W, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1,
+                               int s2, double* Xi, long long ldx, float* wf, int* e, cudaStream_t s);
 
 // alm2cl reduction (ps_window.cu).  Term t pairs coefficient sets a[t], b[t]
 // (HEALPix m-major order, lmax / mmax); a null set stands for all zeros.

@@ -1,0 +1,229 @@
+// ps_quickpol_ff.cu -- the QuickPol Xi (quickpolXi!, src/beam.jl:72-109) in the
+// chosen arithmetic: the general-spin recurrences on the FP32 pipe in
+// float-float, FP64 only where the FP64 kernel (ps_quickpol.cu) needs range or
+// one-off precision.
+//
+// Same mapping and algorithm as k_quickpol_fp64 (one thread per (l'', l); both
+// families forward from their own jmin and backward from jmax, matched at one
+// common point), with:
+//   * P(j) = A(j)^2 = (j-|d|)(j+|d|)(s-j)(s+j)(j-|m3|)(j+|m3|) formed from its
+//     six exact integer factors (d = l1 - l2, s = l1 + l2 + 1): three exact
+//     two_prod pairs and two float-float products;
+//   * 1 / (j A(j+1)) = 1/sqrt(P(j+1) j^2) by ff_rsqrt, and A(j+1) carried to
+//     the next step as P(j+1) times that, times j;
+//   * B(j) = -(2j+1)(m3 d s - j(j+1)(m2 - m1)) exact in 64-bit integers, then
+//     split into two floats;
+//   * W staged once per call as floats scaled by 2^-E (E: the largest
+//     exponent of |W|), so FP32 keeps W's relative precision; entries below
+//     2^(E-149) count as zero.  The FP32 sums are flushed into FP64 every 32
+//     steps, and the result is scaled back by 2^E.
+// The family values start at 1 and stay within FP32 range for the small spins
+// QuickPol uses (|m| <= a few) at l up to 16383.
+#include "ps_internal.cuh"
+#include "ps_ff.cuh"
+
+namespace ps {
+
+namespace {
+
+constexpr int kQpFlush = 32;  // steps between FP64 flushes of the FP32 sums
+
+struct QFam {
+    int m1, m2, m3, am3;
+    int jmin;
+    long long m3ds;  // m3 * d * s
+    bool zero;
+};
+
+__device__ __forceinline__ ff qp_P(int j, int ad, int s, int am3)
+{
+    const ff a = two_prod((float)(j - ad), (float)(j + ad));
+    const ff b = two_prod((float)(s - j), (float)(s + j));
+    const ff c = two_prod((float)(j - am3), (float)(j + am3));
+    return ff_mul_raw(ff_mul_raw(a, b), c);
+}
+
+__device__ __forceinline__ ff qp_B(int j, const QFam& f)
+{
+    const long long t = f.m3ds - (long long)j * (j + 1) * (long long)(f.m2 - f.m1);
+    const long long b = -(2LL * j + 1) * t;  // exact: |b| < 2^54 for l <= 16383 and |m| <= 64
+    const float h = (float)b;                 // the split keeps 48 of its bits
+    return ff{h, (float)(b - (long long)h)};
+}
+
+// f(j+1) from f(j), f(j-1); `a` carries A(j) -> A(j+1).  j = 0 only occurs for
+// m3 = 0, l1 = l2, where the recurrence is f(1) = -(m2 - m1) f(0) / A(1).
+__device__ __forceinline__ ff qp_fwd(int j, const QFam& f, int ad, int s, ff fc, ff fp, ff& a)
+{
+    const ff P1 = qp_P(j + 1, ad, s, f.am3);
+    if (j == 0) {
+        const ff r = ff_rsqrt(P1);
+        a = ff_mul_raw(P1, r);
+        return ff_neg(ff_mulf_raw(ff_mul_raw(fc, r), (float)(f.m2 - f.m1)));
+    }
+    const ff q = ff_rsqrt(ff_mul_raw(P1, two_prod((float)j, (float)j)));  // 1 / (j A(j+1))
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(j, f), fc), ff_mul_raw(ff_mulf_raw(a, (float)(j + 1)), fp));
+    a = ff_mulf_raw(ff_mul_raw(P1, q), (float)j);
+    return ff_neg(ff_mul_raw(num, q));
+}
+
+// h(j-1) from h(j), h(j+1) (needs j > jmin); `a` carries A(j+1) -> A(j).
+__device__ __forceinline__ ff qp_bwd(int j, const QFam& f, int ad, int s, ff hc, ff hn, ff& a)
+{
+    const ff P0 = qp_P(j, ad, s, f.am3);
+    const ff q = ff_rsqrt(ff_mul_raw(P0, two_prod((float)(j + 1), (float)(j + 1))));  // 1 / ((j+1) A(j))
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(j, f), hc), ff_mul_raw(ff_mulf_raw(a, (float)j), hn));
+    a = ff_mulf_raw(ff_mul_raw(P0, q), (float)(j + 1));
+    return ff_neg(ff_mul_raw(num, q));
+}
+
+__device__ __forceinline__ float ff_round(ff x) { return __fadd_rn(x.h, x.l); }
+
+// W -> floats scaled by 2^-E, E the largest exponent of |W| (0 when W is all zero).  One block.
+__global__ void __launch_bounds__(1024) k_quickpol_stage(const double* __restrict__ W, int n, float* __restrict__ Wf,
+                                                         int* __restrict__ E_out)
+{
+    __shared__ int warp_max[32];
+    int e = -100000;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double w = W[j];
+        if (w != 0.0) e = max(e, ilogb(w));
+    }
+    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        e = threadIdx.x < (blockDim.x >> 5) ? warp_max[threadIdx.x] : -100000;
+        for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+        if (threadIdx.x == 0) warp_max[0] = e == -100000 ? 0 : e;
+    }
+    __syncthreads();
+    const int E = warp_max[0];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) Wf[j] = (float)ldexp(W[j], -E);
+    if (threadIdx.x == 0) *E_out = E;
+}
+
+__global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ Wf, const int* __restrict__ E_in,
+                                                     long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1,
+                                                     int s2, double* Xi, long long ldx)
+{
+    const int lpp = 2 + blockIdx.y;  // row l''
+    const int lo = max(2, lpp - bl), hi = min(lmax, lpp + bu);
+    const int l = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (lpp > lmax || l > hi) return;
+    const int l1 = l, l2 = lpp, jmax = l1 + l2;
+    const int ad = abs(l1 - l2), s = l1 + l2 + 1;
+    QFam F[2];
+    F[0].m1 = -s1; F[0].m2 = -nu1; F[0].m3 = s1 + nu1;
+    F[1].m1 = -s2; F[1].m2 = -nu2; F[1].m3 = s2 + nu2;
+    bool any_zero = false;
+    int jm = 0;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        F[k].am3 = abs(F[k].m3);
+        F[k].m3ds = (long long)F[k].m3 * (l1 - l2) * s;
+        F[k].jmin = max(ad, F[k].am3);
+        F[k].zero = abs(F[k].m1) > l1 || abs(F[k].m2) > l2 || F[k].jmin > jmax;
+        any_zero |= F[k].zero;
+        jm = max(jm, (F[k].jmin + jmax) / 2);
+    }
+    double xi = 0.0;
+    if (!any_zero) {
+        if (jm >= jmax) jm = jmax - 1;
+        const bool fwd0 = F[0].jmin <= jm, fwd1 = F[1].jmin <= jm;
+        const ff zero = ff_make(0.0f), one = ff_make(1.0f);
+        // ---- forward: each family from its own jmin up to jm (values at jm + 1 kept) ----
+        ff fp0 = zero, fc0 = zero, fp1 = zero, fc1 = zero, af0 = zero, af1 = zero;
+        double NF0 = 0.0, NF1 = 0.0, SF = 0.0;
+        float nf0 = 0.0f, nf1 = 0.0f, sf = 0.0f;
+        int cnt = 0;
+        const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
+        for (int j = jlo; j <= jm; ++j) {
+            if (fwd0 && j == F[0].jmin) fc0 = one;
+            if (fwd1 && j == F[1].jmin) fc1 = one;
+            const float g0 = ff_round(fc0), g1 = ff_round(fc1), w = (float)(2 * j + 1);
+            nf0 = __fmaf_rn(w, __fmul_rn(g0, g0), nf0);
+            nf1 = __fmaf_rn(w, __fmul_rn(g1, g1), nf1);
+            if (j < nW) sf = __fmaf_rn(__fmul_rn(__ldg(Wf + j), g0), g1, sf);
+            if (fwd0 && j >= F[0].jmin) {
+                const ff n = qp_fwd(j, F[0], ad, s, fc0, fp0, af0);
+                fp0 = fc0;
+                fc0 = n;
+            }
+            if (fwd1 && j >= F[1].jmin) {
+                const ff n = qp_fwd(j, F[1], ad, s, fc1, fp1, af1);
+                fp1 = fc1;
+                fc1 = n;
+            }
+            if (++cnt == kQpFlush) {
+                NF0 += nf0; NF1 += nf1; SF += sf;
+                nf0 = nf1 = sf = 0.0f;
+                cnt = 0;
+            }
+        }
+        NF0 += nf0; NF1 += nf1; SF += sf;
+        // ---- backward: from jmax down to jm + 1 (and to jmin for backward-only families) ----
+        ff hn0 = zero, hc0 = one, hn1 = zero, hc1 = one, ab0 = zero, ab1 = zero;
+        ff hm0_0 = zero, hm1_0 = zero, hm0_1 = zero, hm1_1 = zero;  // h(jm), h(jm+1) per family
+        double NB0 = 0.0, NB1 = 0.0, SB = 0.0;
+        float nb0 = 0.0f, nb1 = 0.0f, sb = 0.0f;
+        cnt = 0;
+        const int jstop = min(fwd0 ? jm + 1 : F[0].jmin, fwd1 ? jm + 1 : F[1].jmin);
+        for (int j = jmax; j >= jstop; --j) {
+            const bool in0 = j >= (fwd0 ? jm + 1 : F[0].jmin), in1 = j >= (fwd1 ? jm + 1 : F[1].jmin);
+            const float v0 = in0 ? ff_round(hc0) : 0.0f, v1 = in1 ? ff_round(hc1) : 0.0f, w = (float)(2 * j + 1);
+            nb0 = __fmaf_rn(w, __fmul_rn(v0, v0), nb0);
+            nb1 = __fmaf_rn(w, __fmul_rn(v1, v1), nb1);
+            if (j < nW) sb = __fmaf_rn(__fmul_rn(__ldg(Wf + j), v0), v1, sb);
+            if (in0 && j > F[0].jmin) {
+                if (j == jm + 1) hm1_0 = hc0;
+                const ff n = qp_bwd(j, F[0], ad, s, hc0, hn0, ab0);
+                hn0 = hc0;
+                hc0 = n;
+                if (j == jm + 1) hm0_0 = hc0;
+            }
+            if (in1 && j > F[1].jmin) {
+                if (j == jm + 1) hm1_1 = hc1;
+                const ff n = qp_bwd(j, F[1], ad, s, hc1, hn1, ab1);
+                hn1 = hc1;
+                hc1 = n;
+                if (j == jm + 1) hm0_1 = hc1;
+            }
+            if (++cnt == kQpFlush) {
+                NB0 += nb0; NB1 += nb1; SB += sb;
+                nb0 = nb1 = sb = 0.0f;
+                cnt = 0;
+            }
+        }
+        NB0 += nb0; NB1 += nb1; SB += sb;
+        // ---- match, normalise, sign (FP64) ----
+        const double p0 = ff_to_double(fp0), c0 = ff_to_double(fc0), p1 = ff_to_double(fp1), c1 = ff_to_double(fc1);
+        const double a0 = ff_to_double(hm0_0), b0 = ff_to_double(hm1_0), a1 = ff_to_double(hm0_1),
+                     b1 = ff_to_double(hm1_1);
+        const double lam0 = fwd0 ? (p0 * a0 + c0 * b0) / (a0 * a0 + b0 * b0) : 1.0;
+        const double lam1 = fwd1 ? (p1 * a1 + c1 * b1) / (a1 * a1 + b1 * b1) : 1.0;
+        const double N0 = fma(lam0 * lam0, NB0, NF0), N1 = fma(lam1 * lam1, NB1, NF1);
+        const double cs0 = ((l1 - l2 - F[0].m3) & 1) ? -1.0 : 1.0, cs1 = ((l1 - l2 - F[1].m3) & 1) ? -1.0 : 1.0;
+        const double sg0 = (lam0 < 0.0) ? -cs0 : cs0, sg1 = (lam1 < 0.0) ? -cs1 : cs1;
+        xi = ldexp(fma(lam0 * lam1, SB, SF) * sg0 * sg1 * rsqrt(N0 * N1), *E_in);
+    }
+    const double sgn = ((s1 + s2 + nu1 + nu2) & 1) ? -1.0 : 1.0;
+    Xi[(long long)lpp + (long long)l * ldx] = sgn * xi;
+}
+
+}  // namespace
+
+cudaError_t launch_quickpol_ff(const double* W, long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1,
+                               int s2, double* Xi, long long ldx, float* wf, int* e, cudaStream_t st)
+{
+    if (lmax < 2) return cudaSuccess;
+    k_quickpol_stage<<<1, 1024, 0, st>>>(W, (int)nW, wf, e);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    const int width = bl + bu + 1;
+    dim3 grid((width + 127) / 128, lmax - 1);
+    k_quickpol_ff<<<grid, 128, 0, st>>>(wf, e, nW, lmax, bl, bu, nu1, nu2, s1, s2, Xi, ldx);
+    return cudaGetLastError();
+}
+
+}  // namespace ps

@@ -144,10 +144,10 @@ function PowerSpectra.quickpolΞ!(𝚵::SpectralArray{Float64,2}, ν₁, ν₂, 
     X = Matrix{Float64}(undef, lmax + 1, lmax + 1)
     c = ctx()
     st = ccall((:ps_quickpol_xi_alm, libps), Cint,
-               (Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Cint, Cint,
+               (Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Cint, Cint, Cint,
                 Ptr{Float64}, Int64),
                c, ν₁, ν₂, s₁, s₂, Ptr{Float64}(pointer(ω₁.alm)), Ptr{Float64}(pointer(ω₂.alm)),
-               min(ω₁.lmax, ω₂.lmax), min(ω₁.mmax, ω₂.mmax), lmax, bl, bu, X, lmax + 1)
+               min(ω₁.lmax, ω₂.lmax), min(ω₁.mmax, ω₂.mmax), lmax, bl, bu, MODE[], X, lmax + 1)
     check(st, c)
     for ℓ″ in 2:lmax, ℓ in PowerSpectra.specrowrange(𝚵, ℓ″)
         𝚵[ℓ″, ℓ] = X[ℓ″ + 1, ℓ + 1]

@@ -105,9 +105,9 @@ def load(path=None):
         lib.ps_decouple_covmat.restype = ci
         lib.ps_solve.argtypes = [vp, _DP, i64, i64, _DP, ci, i64, _DP, i64]
         lib.ps_solve.restype = ci
-        lib.ps_quickpol_xi.argtypes = [vp, ci, ci, ci, ci, _DP, i64, ci, ci, ci, _DP, i64]
+        lib.ps_quickpol_xi.argtypes = [vp, ci, ci, ci, ci, _DP, i64, ci, ci, ci, ci, _DP, i64]
         lib.ps_quickpol_xi.restype = ci
-        lib.ps_quickpol_xi_alm.argtypes = [vp, ci, ci, ci, ci, _DP, _DP, ci, ci, ci, ci, ci, _DP, i64]
+        lib.ps_quickpol_xi_alm.argtypes = [vp, ci, ci, ci, ci, _DP, _DP, ci, ci, ci, ci, ci, ci, _DP, i64]
         lib.ps_quickpol_xi_alm.restype = ci
         lib.ps_decouple_covmat_device.argtypes = [vp, _DP, _DP, _DP, i64, i64, _DP, i64]
         lib.ps_decouple_covmat_device.restype = ci
@@ -234,16 +234,16 @@ class Context:
         self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
                                                 mode_code(mode), dptr_array(ml), int(ldm)))
 
-    def quickpol_xi(self, nu1, nu2, s1, s2, W, lmax, bl, bu):
+    def quickpol_xi(self, nu1, nu2, s1, s2, W, lmax, bl, bu, mode="plain"):
         """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band."""
         W = np.ascontiguousarray(W, dtype=np.float64)
         n = lmax + 1
         X = np.empty((n, n), dtype=np.float64, order="F")
         self.check(self.lib.ps_quickpol_xi(self.handle, int(nu1), int(nu2), int(s1), int(s2), dptr(W), len(W), lmax,
-                                           int(bl), int(bu), dptr(X), n))
+                                           int(bl), int(bu), mode_code(mode), dptr(X), n))
         return X
 
-    def quickpol_xi_alm(self, nu1, nu2, s1, s2, omega1, omega2, alm_lmax, lmax, bl, bu, alm_mmax=None):
+    def quickpol_xi_alm(self, nu1, nu2, s1, s2, omega1, omega2, alm_lmax, lmax, bl, bu, alm_mmax=None, mode="plain"):
         """quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2) (src/beam.jl:72-109): W = quickpolW(omega1,
         omega2) and Xi on the GPU, from complex128 scan-weight coefficient sets (HEALPix order)."""
         alm_mmax = alm_lmax if alm_mmax is None else alm_mmax
@@ -256,7 +256,7 @@ class Context:
         X = np.empty((n, n), dtype=np.float64, order="F")
         self.check(self.lib.ps_quickpol_xi_alm(self.handle, int(nu1), int(nu2), int(s1), int(s2),
                                                dptr(o1.view(np.float64)), dptr(o2.view(np.float64)), alm_lmax,
-                                               alm_mmax, lmax, int(bl), int(bu), dptr(X), n))
+                                               alm_mmax, lmax, int(bl), int(bu), mode_code(mode), dptr(X), n))
         return X
 
     def window_W(self, A, B, lmax, mmax=None, lout=None):

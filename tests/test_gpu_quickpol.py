@@ -60,3 +60,42 @@ def test_quickpol_from_scan_weights(ctx, alm_lmax, alm_mmax, lmax, bl, bu):
         scale = np.maximum(scale, np.abs(o.quickpol_xi(2, 0, 2, -2, Wa, lmax, bl, bu)))
         err = np.abs(G - R) / np.maximum(np.maximum(np.abs(R), 1e-3 * scale), 1e-300)
         assert np.max(err[scale > 0]) < 1e-10
+
+
+@pytest.mark.parametrize("nu1,nu2,s1,s2", [(0, 0, 0, 0), (0, 0, 2, 2), (1, -1, 2, 0), (2, 2, -2, 2), (-3, 1, 2, -2),
+                                           (4, -4, 0, 2)])
+@pytest.mark.parametrize("lmax,bl,bu,nWk", [(120, 10, 10, "2L"), (300, 30, 5, "L"), (60, 100, 100, "short")])
+def test_quickpol_chosen_vs_oracle(ctx, nu1, nu2, s1, s2, lmax, bl, bu, nWk):
+    """The float-float (chosen) QuickPol kernel: max error 1e-6 against the FP64 oracle, relative to
+    the sum of |terms| behind each element (the sum of W f1 f2 cancels: the two families differ, so
+    their product changes sign; an FP32 partial sum resolves it only to that sum's precision)."""
+    nW = {"2L": 2 * lmax + 1, "L": lmax + 1, "short": lmax // 2}[nWk]
+    rng = np.random.default_rng(lmax + 5 * nu2 + 11 * s2)
+    W = rng.random(nW) * np.exp(-np.arange(nW) / 40.0) * 1e-30  # far from 1: the staging scale must work
+    G = ctx.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, mode="chosen")
+    R = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu)
+    A = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, absolute=True)
+    band = np.zeros_like(G, dtype=bool)
+    for r in range(2, lmax + 1):
+        band[r, max(2, r - bl):min(lmax, r + bu) + 1] = True
+    assert not np.any(G[~band])
+    err = np.abs(G - R) / np.maximum(A, 1e-300)
+    assert np.max(err[band]) < 1e-6
+
+
+def test_quickpol_chosen_large_l(ctx):
+    """l up to 2000 with the notebook's spins (nu = 0, s = 2): chosen against the FP64 kernel."""
+    lmax, band = 2000, 20
+    l = np.arange(2 * lmax + 1)
+    W = (1.0 + np.cos(l / 37.0)) * np.exp(-l / 900.0)
+    P = ctx.quickpol_xi(0, 0, 2, 2, W, lmax, band, band, mode="plain")
+    C = ctx.quickpol_xi(0, 0, 2, 2, W, lmax, band, band, mode="chosen")
+    A = o.quickpol_xi(0, 0, 2, 2, W, lmax, band, band, absolute=True)
+    mask = A > 0
+    assert np.max(np.abs(C - P)[mask] / A[mask]) < 1e-6
+
+
+def test_quickpol_mode_error(ctx):
+    import powerspectra_gpu as pg
+    with pytest.raises(pg.PowerSpectraArgumentError):
+        ctx.quickpol_xi(0, 0, 2, 2, np.ones(10), 8, 2, 2, mode=7)
