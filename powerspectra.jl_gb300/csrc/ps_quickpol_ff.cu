@@ -11,8 +11,9 @@
 //     two_prod pairs and two float-float products;
 //   * 1 / (j A(j+1)) = 1/sqrt(P(j+1) j^2) by ff_rsqrt, and A(j+1) carried to
 //     the next step as P(j+1) times that, times j;
-//   * B(j) = -(2j+1)(m3 d s - j(j+1)(m2 - m1)) exact in 64-bit integers, then
-//     split into two floats;
+//   * B(j) = -(2j+1)(m3 d s - j(j+1)(m2 - m1)) in float-float from exact
+//     pieces, and the factors both families share (all of P(j) but
+//     (j - |m3|)(j + |m3|), and j(j+1)) formed once per point;
 //   * W staged once per call as floats scaled by 2^-E (E: the largest
 //     exponent of |W|), so FP32 keeps W's relative precision; entries below
 //     2^(E-149) count as zero.  The FP32 sums are flushed into FP64 every 32
@@ -31,48 +32,64 @@ constexpr int kQpFlush = 32;  // steps between FP64 flushes of the FP32 sums
 struct QFam {
     int m1, m2, m3, am3;
     int jmin;
-    long long m3ds;  // m3 * d * s
+    ff m3ds;     // m3 * d * s (d = l1 - l2, s = l1 + l2 + 1), exact in 64-bit integers, split into two floats
+    float dm;    // m2 - m1
     bool zero;
 };
 
-__device__ __forceinline__ ff qp_P(int j, int ad, int s, int am3)
+// The parts of one step's coefficients that both families share: at point j,
+// the factor (j^2 - d^2)(s^2 - j^2) of P(j), and j (j + 1).
+struct QShared {
+    ff ds;   // (j - |d|)(j + |d|)(s - j)(s + j)
+    ff jj1;  // j (j + 1)
+};
+
+__device__ __forceinline__ QShared qp_shared(int j, int ad, int s)
 {
-    const ff a = two_prod((float)(j - ad), (float)(j + ad));
-    const ff b = two_prod((float)(s - j), (float)(s + j));
-    const ff c = two_prod((float)(j - am3), (float)(j + am3));
-    return ff_mul_raw(ff_mul_raw(a, b), c);
+    QShared q;
+    q.ds = ff_mul_raw(two_prod((float)(j - ad), (float)(j + ad)), two_prod((float)(s - j), (float)(s + j)));
+    q.jj1 = two_prod((float)j, (float)(j + 1));
+    return q;
 }
 
-__device__ __forceinline__ ff qp_B(int j, const QFam& f)
+// P(j) = ds(j) (j - |m3|)(j + |m3|)
+__device__ __forceinline__ ff qp_P(const QShared& q, int j, int am3)
 {
-    const long long t = f.m3ds - (long long)j * (j + 1) * (long long)(f.m2 - f.m1);
-    const long long b = -(2LL * j + 1) * t;  // exact: |b| < 2^54 for l <= 16383 and |m| <= 64
-    const float h = (float)b;                 // the split keeps 48 of its bits
-    return ff{h, (float)(b - (long long)h)};
+    return ff_mul_raw(q.ds, two_prod((float)(j - am3), (float)(j + am3)));
 }
 
-// f(j+1) from f(j), f(j-1); `a` carries A(j) -> A(j+1).  j = 0 only occurs for
+// B(j) = -(2j+1) (m3 d s - j (j+1) (m2 - m1))
+__device__ __forceinline__ ff qp_B(const QShared& q, int j, const QFam& f)
+{
+    const ff t = ff_add_raw(f.m3ds, ff_neg(ff_mulf_raw(q.jj1, f.dm)));
+    return ff_neg(ff_mulf_raw(t, (float)(2 * j + 1)));
+}
+
+// f(j+1) from f(j), f(j-1) with the point-(j+1) shared parts qn and the
+// point-j shared parts qc; `a` carries A(j) -> A(j+1).  j = 0 only occurs for
 // m3 = 0, l1 = l2, where the recurrence is f(1) = -(m2 - m1) f(0) / A(1).
-__device__ __forceinline__ ff qp_fwd(int j, const QFam& f, int ad, int s, ff fc, ff fp, ff& a)
+__device__ __forceinline__ ff qp_fwd(int j, const QFam& f, const QShared& qc, const QShared& qn, const ff& jsq, ff fc,
+                                     ff fp, ff& a)
 {
-    const ff P1 = qp_P(j + 1, ad, s, f.am3);
+    const ff P1 = qp_P(qn, j + 1, f.am3);
     if (j == 0) {
         const ff r = ff_rsqrt(P1);
         a = ff_mul_raw(P1, r);
-        return ff_neg(ff_mulf_raw(ff_mul_raw(fc, r), (float)(f.m2 - f.m1)));
+        return ff_neg(ff_mulf_raw(ff_mul_raw(fc, r), f.dm));
     }
-    const ff q = ff_rsqrt(ff_mul_raw(P1, two_prod((float)j, (float)j)));  // 1 / (j A(j+1))
-    const ff num = ff_add_raw(ff_mul_raw(qp_B(j, f), fc), ff_mul_raw(ff_mulf_raw(a, (float)(j + 1)), fp));
+    const ff q = ff_rsqrt(ff_mul_raw(P1, jsq));  // 1 / (j A(j+1))
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), fc), ff_mul_raw(ff_mulf_raw(a, (float)(j + 1)), fp));
     a = ff_mulf_raw(ff_mul_raw(P1, q), (float)j);
     return ff_neg(ff_mul_raw(num, q));
 }
 
-// h(j-1) from h(j), h(j+1) (needs j > jmin); `a` carries A(j+1) -> A(j).
-__device__ __forceinline__ ff qp_bwd(int j, const QFam& f, int ad, int s, ff hc, ff hn, ff& a)
+// h(j-1) from h(j), h(j+1) (needs j > jmin) with the point-j shared parts qc;
+// `a` carries A(j+1) -> A(j).  j1sq = (j+1)^2.
+__device__ __forceinline__ ff qp_bwd(int j, const QFam& f, const QShared& qc, const ff& j1sq, ff hc, ff hn, ff& a)
 {
-    const ff P0 = qp_P(j, ad, s, f.am3);
-    const ff q = ff_rsqrt(ff_mul_raw(P0, two_prod((float)(j + 1), (float)(j + 1))));  // 1 / ((j+1) A(j))
-    const ff num = ff_add_raw(ff_mul_raw(qp_B(j, f), hc), ff_mul_raw(ff_mulf_raw(a, (float)j), hn));
+    const ff P0 = qp_P(qc, j, f.am3);
+    const ff q = ff_rsqrt(ff_mul_raw(P0, j1sq));  // 1 / ((j+1) A(j))
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), hc), ff_mul_raw(ff_mulf_raw(a, (float)j), hn));
     a = ff_mulf_raw(ff_mul_raw(P0, q), (float)(j + 1));
     return ff_neg(ff_mul_raw(num, q));
 }
@@ -121,7 +138,10 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         F[k].am3 = abs(F[k].m3);
-        F[k].m3ds = (long long)F[k].m3 * (l1 - l2) * s;
+        const long long m3ds = (long long)F[k].m3 * (l1 - l2) * s;  // |m3 d s| < 2^38
+        const float h = (float)m3ds;
+        F[k].m3ds = ff{h, (float)(m3ds - (long long)h)};
+        F[k].dm = (float)(F[k].m2 - F[k].m1);
         F[k].jmin = max(ad, F[k].am3);
         F[k].zero = abs(F[k].m1) > l1 || abs(F[k].m2) > l2 || F[k].jmin > jmax;
         any_zero |= F[k].zero;
@@ -138,6 +158,7 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
         float nf0 = 0.0f, nf1 = 0.0f, sf = 0.0f;
         int cnt = 0;
         const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
+        QShared qc = qp_shared(jlo, ad, s);  // carried: the next point's parts become the current ones
         for (int j = jlo; j <= jm; ++j) {
             if (fwd0 && j == F[0].jmin) fc0 = one;
             if (fwd1 && j == F[1].jmin) fc1 = one;
@@ -145,16 +166,19 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
             nf0 = __fmaf_rn(w, __fmul_rn(g0, g0), nf0);
             nf1 = __fmaf_rn(w, __fmul_rn(g1, g1), nf1);
             if (j < nW) sf = __fmaf_rn(__fmul_rn(__ldg(Wf + j), g0), g1, sf);
+            const QShared qn = qp_shared(j + 1, ad, s);
+            const ff jsq = two_prod((float)j, (float)j);
             if (fwd0 && j >= F[0].jmin) {
-                const ff n = qp_fwd(j, F[0], ad, s, fc0, fp0, af0);
+                const ff n = qp_fwd(j, F[0], qc, qn, jsq, fc0, fp0, af0);
                 fp0 = fc0;
                 fc0 = n;
             }
             if (fwd1 && j >= F[1].jmin) {
-                const ff n = qp_fwd(j, F[1], ad, s, fc1, fp1, af1);
+                const ff n = qp_fwd(j, F[1], qc, qn, jsq, fc1, fp1, af1);
                 fp1 = fc1;
                 fc1 = n;
             }
+            qc = qn;
             if (++cnt == kQpFlush) {
                 NF0 += nf0; NF1 += nf1; SF += sf;
                 nf0 = nf1 = sf = 0.0f;
@@ -175,16 +199,18 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
             nb0 = __fmaf_rn(w, __fmul_rn(v0, v0), nb0);
             nb1 = __fmaf_rn(w, __fmul_rn(v1, v1), nb1);
             if (j < nW) sb = __fmaf_rn(__fmul_rn(__ldg(Wf + j), v0), v1, sb);
+            const QShared qc = qp_shared(j, ad, s);
+            const ff j1sq = two_prod((float)(j + 1), (float)(j + 1));
             if (in0 && j > F[0].jmin) {
                 if (j == jm + 1) hm1_0 = hc0;
-                const ff n = qp_bwd(j, F[0], ad, s, hc0, hn0, ab0);
+                const ff n = qp_bwd(j, F[0], qc, j1sq, hc0, hn0, ab0);
                 hn0 = hc0;
                 hc0 = n;
                 if (j == jm + 1) hm0_0 = hc0;
             }
             if (in1 && j > F[1].jmin) {
                 if (j == jm + 1) hm1_1 = hc1;
-                const ff n = qp_bwd(j, F[1], ad, s, hc1, hn1, ab1);
+                const ff n = qp_bwd(j, F[1], qc, j1sq, hc1, hn1, ab1);
                 hn1 = hc1;
                 hc1 = n;
                 if (j == jm + 1) hm0_1 = hc1;
