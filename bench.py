@@ -522,7 +522,7 @@ def run_window(args):
     import powerspectra_gpu as pg
     from oracle import oracle as o
 
-    L, nsets = 8191, 8
+    L, nsets = args.lmax or 8191, 8
     torch.cuda.set_device(0)
     ctx = pg.Context(0)
     stream = torch.cuda.Stream()
@@ -601,19 +601,20 @@ def run_window(args):
     line = {"metric": "alm2cl coefficient bytes/s (window_function_W! mask spectra)", "value": bytes_step / t / 1e9,
             "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "window_W_8191", "lmax": L, "mmax": L, "sets": nsets,
+            "data": "synthetic", "config": {"workload": "window_W_%d" % L, "lmax": L, "mmax": L, "sets": nsets,
                                             "spectra_per_step": len(pairs), "bytes_per_step": bytes_step,
                                             "l2": "inputs (537 MB per set) larger than L2"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "traffic": WINDOW_TRAFFIC, "kernel": "k_alm2cl_partial + k_alm2cl_reduce, one cross spectrum",
+                         "traffic": WINDOW_TRAFFIC * nalm / o.n_alms(8191, 8191),  # scaled by the coefficients
+                         "kernel": "k_alm2cl_partial + k_alm2cl_reduce, one cross spectrum",
                          "ms_per_call": t1 * 1e3, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
             "e2e": {"value": e2e_bytes / e2e_dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": e2e_bytes,
                     "d2h_bytes_per_step": 8 * (L + 1) * len(e2e_pairs),
                     "what": "ps_window_W on pinned host sets: 1 auto and 2 cross spectra"},
             "max_rel_err_vs_oracle": err, "clocks": clocks, "gpu_launches": launches,
             "cpu_baseline": {"value": 2 * nalm * 16 / cpu_dt / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
-                             "sample": "one cross spectrum at lmax 8191 with the oracle's numpy alm2cl, %.1f s"
-                                       % cpu_dt}}
+                             "sample": "one cross spectrum at lmax %d with the oracle's numpy alm2cl, %.1f s"
+                                       % (L, cpu_dt)}}
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -709,6 +710,8 @@ def main():
                     help="chosen: FP32-pipe recurrence with compensation (the product path); plain: FP64")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 kernel")
+    ap.add_argument("--lmax", type=int, default=0,
+                    help="window_W_8191 only: another lmax (a smaller case for profiling); the JSON names it")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "ps_internal.cuh"
@@ -53,6 +54,8 @@ struct ps_ctx {
     size_t part_cap = 0;
     double* d_qp = nullptr;  // chosen QuickPol scratch: W as floats and its exponent
     size_t qp_cap = 0;
+    double* h_pack = nullptr;  // pinned host staging for packed coefficient sets
+    size_t pack_cap = 0;
     // batched workload state (ps_batch_*)
     struct Batch {
         bool ready = false;
@@ -106,6 +109,23 @@ static int ensure(ps_ctx* c, double** p, size_t* cap, size_t need)
                        cudaGetErrorString(e));
     }
     *cap = need;
+    return PS_OK;
+}
+
+static int ensure_pinned(ps_ctx* c, size_t need)
+{
+    if (need <= c->pack_cap) return PS_OK;
+    cudaFreeHost(c->h_pack);
+    c->h_pack = nullptr;
+    c->pack_cap = 0;
+    cudaError_t e = cudaMallocHost((void**)&c->h_pack, need * sizeof(double));
+    if (e != cudaSuccess) {
+        c->h_pack = nullptr;
+        cudaGetLastError();
+        return set_err(c, PS_ERR_OOM, "cudaMallocHost of %zu bytes failed: %s", need * sizeof(double),
+                       cudaGetErrorString(e));
+    }
+    c->pack_cap = need;
     return PS_OK;
 }
 
@@ -385,6 +405,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_alm);
     cudaFree(c->d_part);
     cudaFree(c->d_qp);
+    cudaFreeHost(c->h_pack);
     batch_release(c);
     ps_linalg_free(c->la);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1053,22 +1074,28 @@ int ps_quickpol_xi_alm(ps_ctx* c, int nu1, int nu2, int s1, int s2, const double
     if ((st = ensure(c, &c->d_spec, &c->spec_cap, (size_t)lw + 1))) return st;
     const size_t n = (size_t)lmax + 1;
     if ((st = ensure(c, &c->d_out, &c->out_cap, n * n))) return st;
-    std::vector<double> packed;
     auto upload = [&](const double* src, double* dst) -> int {
         if (lw == alm_lmax) {
             PS_CUDA(c, cudaMemcpyAsync(dst, src, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
             return PS_OK;
         }
-        PS_CUDA(c, cudaStreamSynchronize(c->stream));  // the staging vector is reused for the second set
-        packed.resize(2 * nalm);
-        size_t at = 0;
-        for (int m = 0; m <= mw; ++m) {  // row m: l = m..lw, at m (2 alm_lmax + 1 - m) / 2 + l in the source
-            const size_t from = (size_t)m * (2 * (size_t)alm_lmax + 1 - m) / 2 + m;
-            const size_t len = (size_t)(lw - m + 1);
-            memcpy(packed.data() + 2 * at, src + 2 * from, 2 * len * sizeof(double));
-            at += len;
-        }
-        PS_CUDA(c, cudaMemcpyAsync(dst, packed.data(), 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));  // the pinned staging is reused for the second set
+        int st2 = ensure_pinned(c, 2 * nalm);
+        if (st2) return st2;
+        // rows m: l = m..lw, at m (2 alm_lmax + 1 - m) / 2 + l in the source and
+        // m (2 lw + 1 - m) / 2 + l in the packed set; packed by a few host threads
+        const int nth = (int)std::min<size_t>(8, 1 + nalm / (1 << 18));
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nth; ++t)
+            pool.emplace_back([&, t] {
+                for (int m = t; m <= mw; m += nth) {
+                    const size_t from = (size_t)m * (2 * (size_t)alm_lmax + 1 - m) / 2 + m;
+                    const size_t to = (size_t)m * (2 * (size_t)lw + 1 - m) / 2 + m;
+                    memcpy(c->h_pack + 2 * to, src + 2 * from, 2 * (size_t)(lw - m + 1) * sizeof(double));
+                }
+            });
+        for (auto& th : pool) th.join();
+        PS_CUDA(c, cudaMemcpyAsync(dst, c->h_pack, 2 * nalm * sizeof(double), cudaMemcpyHostToDevice, c->stream));
         PS_CUDA(c, cudaStreamSynchronize(c->stream));
         return PS_OK;
     };

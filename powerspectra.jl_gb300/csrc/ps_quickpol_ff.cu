@@ -31,6 +31,7 @@ constexpr int kQpFlush = 32;  // steps between FP64 flushes of the FP32 sums
 
 struct QFam {
     int m1, m2, m3, am3;
+    float am3f;  // |m3| as a float
     int jmin;
     ff m3ds;     // m3 * d * s (d = l1 - l2, s = l1 + l2 + 1), exact in 64-bit integers, split into two floats
     float dm;    // m2 - m1
@@ -44,53 +45,56 @@ struct QShared {
     ff jj1;  // j (j + 1)
 };
 
-__device__ __forceinline__ QShared qp_shared(int j, int ad, int s)
+// j, |d| and s arrive as floats (exact integers below 2^24): the loops carry j
+// as a float, so no integer-to-float conversion (which shares GB300's narrow
+// FP64 pipe) runs per step.
+__device__ __forceinline__ QShared qp_shared(float j, float ad, float s)
 {
     QShared q;
-    q.ds = ff_mul_raw(two_prod((float)(j - ad), (float)(j + ad)), two_prod((float)(s - j), (float)(s + j)));
-    q.jj1 = two_prod((float)j, (float)(j + 1));
+    q.ds = ff_mul_raw(two_prod(j - ad, j + ad), two_prod(s - j, s + j));
+    q.jj1 = two_prod(j, j + 1.0f);
     return q;
 }
 
 // P(j) = ds(j) (j - |m3|)(j + |m3|)
-__device__ __forceinline__ ff qp_P(const QShared& q, int j, int am3)
+__device__ __forceinline__ ff qp_P(const QShared& q, float j, float am3)
 {
-    return ff_mul_raw(q.ds, two_prod((float)(j - am3), (float)(j + am3)));
+    return ff_mul_raw(q.ds, two_prod(j - am3, j + am3));
 }
 
 // B(j) = -(2j+1) (m3 d s - j (j+1) (m2 - m1))
-__device__ __forceinline__ ff qp_B(const QShared& q, int j, const QFam& f)
+__device__ __forceinline__ ff qp_B(const QShared& q, float j, const QFam& f)
 {
     const ff t = ff_add_raw(f.m3ds, ff_neg(ff_mulf_raw(q.jj1, f.dm)));
-    return ff_neg(ff_mulf_raw(t, (float)(2 * j + 1)));
+    return ff_neg(ff_mulf_raw(t, __fmaf_rn(2.0f, j, 1.0f)));
 }
 
 // f(j+1) from f(j), f(j-1) with the point-(j+1) shared parts qn and the
 // point-j shared parts qc; `a` carries A(j) -> A(j+1).  j = 0 only occurs for
 // m3 = 0, l1 = l2, where the recurrence is f(1) = -(m2 - m1) f(0) / A(1).
-__device__ __forceinline__ ff qp_fwd(int j, const QFam& f, const QShared& qc, const QShared& qn, const ff& jsq, ff fc,
+__device__ __forceinline__ ff qp_fwd(float j, const QFam& f, const QShared& qc, const QShared& qn, const ff& jsq, ff fc,
                                      ff fp, ff& a)
 {
-    const ff P1 = qp_P(qn, j + 1, f.am3);
-    if (j == 0) {
+    const ff P1 = qp_P(qn, j + 1.0f, f.am3f);
+    if (j == 0.0f) {
         const ff r = ff_rsqrt(P1);
         a = ff_mul_raw(P1, r);
         return ff_neg(ff_mulf_raw(ff_mul_raw(fc, r), f.dm));
     }
     const ff q = ff_rsqrt(ff_mul_raw(P1, jsq));  // 1 / (j A(j+1))
-    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), fc), ff_mul_raw(ff_mulf_raw(a, (float)(j + 1)), fp));
-    a = ff_mulf_raw(ff_mul_raw(P1, q), (float)j);
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), fc), ff_mul_raw(ff_mulf_raw(a, j + 1.0f), fp));
+    a = ff_mulf_raw(ff_mul_raw(P1, q), j);
     return ff_neg(ff_mul_raw(num, q));
 }
 
 // h(j-1) from h(j), h(j+1) (needs j > jmin) with the point-j shared parts qc;
 // `a` carries A(j+1) -> A(j).  j1sq = (j+1)^2.
-__device__ __forceinline__ ff qp_bwd(int j, const QFam& f, const QShared& qc, const ff& j1sq, ff hc, ff hn, ff& a)
+__device__ __forceinline__ ff qp_bwd(float j, const QFam& f, const QShared& qc, const ff& j1sq, ff hc, ff hn, ff& a)
 {
-    const ff P0 = qp_P(qc, j, f.am3);
+    const ff P0 = qp_P(qc, j, f.am3f);
     const ff q = ff_rsqrt(ff_mul_raw(P0, j1sq));  // 1 / ((j+1) A(j))
-    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), hc), ff_mul_raw(ff_mulf_raw(a, (float)j), hn));
-    a = ff_mulf_raw(ff_mul_raw(P0, q), (float)(j + 1));
+    const ff num = ff_add_raw(ff_mul_raw(qp_B(qc, j, f), hc), ff_mul_raw(ff_mulf_raw(a, j), hn));
+    a = ff_mulf_raw(ff_mul_raw(P0, q), j + 1.0f);
     return ff_neg(ff_mul_raw(num, q));
 }
 
@@ -130,6 +134,7 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
     if (lpp > lmax || l > hi) return;
     const int l1 = l, l2 = lpp, jmax = l1 + l2;
     const int ad = abs(l1 - l2), s = l1 + l2 + 1;
+    const float adf = (float)ad, spf = (float)s;  // |d| and s as floats
     QFam F[2];
     F[0].m1 = -s1; F[0].m2 = -nu1; F[0].m3 = s1 + nu1;
     F[1].m1 = -s2; F[1].m2 = -nu2; F[1].m3 = s2 + nu2;
@@ -138,6 +143,7 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         F[k].am3 = abs(F[k].m3);
+        F[k].am3f = (float)F[k].am3;
         const long long m3ds = (long long)F[k].m3 * (l1 - l2) * s;  // |m3 d s| < 2^38
         const float h = (float)m3ds;
         F[k].m3ds = ff{h, (float)(m3ds - (long long)h)};
@@ -158,23 +164,24 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
         float nf0 = 0.0f, nf1 = 0.0f, sf = 0.0f;
         int cnt = 0;
         const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
-        QShared qc = qp_shared(jlo, ad, s);  // carried: the next point's parts become the current ones
-        for (int j = jlo; j <= jm; ++j) {
+        QShared qc = qp_shared((float)jlo, adf, spf);  // carried: the next point's parts become the current ones
+        float jf = (float)jlo;                         // j as a float, stepped with j
+        for (int j = jlo; j <= jm; ++j, jf += 1.0f) {
             if (fwd0 && j == F[0].jmin) fc0 = one;
             if (fwd1 && j == F[1].jmin) fc1 = one;
-            const float g0 = ff_round(fc0), g1 = ff_round(fc1), w = (float)(2 * j + 1);
+            const float g0 = ff_round(fc0), g1 = ff_round(fc1), w = __fmaf_rn(2.0f, jf, 1.0f);
             nf0 = __fmaf_rn(w, __fmul_rn(g0, g0), nf0);
             nf1 = __fmaf_rn(w, __fmul_rn(g1, g1), nf1);
             if (j < nW) sf = __fmaf_rn(__fmul_rn(__ldg(Wf + j), g0), g1, sf);
-            const QShared qn = qp_shared(j + 1, ad, s);
-            const ff jsq = two_prod((float)j, (float)j);
+            const QShared qn = qp_shared(jf + 1.0f, adf, spf);
+            const ff jsq = two_prod(jf, jf);
             if (fwd0 && j >= F[0].jmin) {
-                const ff n = qp_fwd(j, F[0], qc, qn, jsq, fc0, fp0, af0);
+                const ff n = qp_fwd(jf, F[0], qc, qn, jsq, fc0, fp0, af0);
                 fp0 = fc0;
                 fc0 = n;
             }
             if (fwd1 && j >= F[1].jmin) {
-                const ff n = qp_fwd(j, F[1], qc, qn, jsq, fc1, fp1, af1);
+                const ff n = qp_fwd(jf, F[1], qc, qn, jsq, fc1, fp1, af1);
                 fp1 = fc1;
                 fc1 = n;
             }
@@ -193,24 +200,25 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
         float nb0 = 0.0f, nb1 = 0.0f, sb = 0.0f;
         cnt = 0;
         const int jstop = min(fwd0 ? jm + 1 : F[0].jmin, fwd1 ? jm + 1 : F[1].jmin);
-        for (int j = jmax; j >= jstop; --j) {
+        float jbf = (float)jmax;
+        for (int j = jmax; j >= jstop; --j, jbf -= 1.0f) {
             const bool in0 = j >= (fwd0 ? jm + 1 : F[0].jmin), in1 = j >= (fwd1 ? jm + 1 : F[1].jmin);
-            const float v0 = in0 ? ff_round(hc0) : 0.0f, v1 = in1 ? ff_round(hc1) : 0.0f, w = (float)(2 * j + 1);
+            const float v0 = in0 ? ff_round(hc0) : 0.0f, v1 = in1 ? ff_round(hc1) : 0.0f, w = __fmaf_rn(2.0f, jbf, 1.0f);
             nb0 = __fmaf_rn(w, __fmul_rn(v0, v0), nb0);
             nb1 = __fmaf_rn(w, __fmul_rn(v1, v1), nb1);
             if (j < nW) sb = __fmaf_rn(__fmul_rn(__ldg(Wf + j), v0), v1, sb);
-            const QShared qc = qp_shared(j, ad, s);
-            const ff j1sq = two_prod((float)(j + 1), (float)(j + 1));
+            const QShared qc = qp_shared(jbf, adf, spf);
+            const ff j1sq = two_prod(jbf + 1.0f, jbf + 1.0f);
             if (in0 && j > F[0].jmin) {
                 if (j == jm + 1) hm1_0 = hc0;
-                const ff n = qp_bwd(j, F[0], qc, j1sq, hc0, hn0, ab0);
+                const ff n = qp_bwd(jbf, F[0], qc, j1sq, hc0, hn0, ab0);
                 hn0 = hc0;
                 hc0 = n;
                 if (j == jm + 1) hm0_0 = hc0;
             }
             if (in1 && j > F[1].jmin) {
                 if (j == jm + 1) hm1_1 = hc1;
-                const ff n = qp_bwd(j, F[1], qc, j1sq, hc1, hn1, ab1);
+                const ff n = qp_bwd(jbf, F[1], qc, j1sq, hc1, hn1, ab1);
                 hn1 = hc1;
                 hc1 = n;
                 if (j == jm + 1) hm0_1 = hc1;
