@@ -444,6 +444,19 @@ double ps_last_kernel_ms(const ps_ctx* c)
 
 uint64_t ps_launch_count(const ps_ctx* c) { return c ? (uint64_t)c->launches : 0; }
 
+// The device address of a page-locked host buffer that is mapped into the
+// device's address space (cudaHostAlloc / cudaHostRegister memory under unified
+// addressing), or nullptr for ordinary pageable memory.
+static double* mapped_host(double* h)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? (double*)a.devicePointer : nullptr;
+}
+
 static int mcm_multi_impl(ps_ctx* c, unsigned cases, const double* const W[4], int64_t nW, int lmin, int lmax, int mode,
                           double* const M[4], int64_t ldm, bool host)
 {
@@ -471,7 +484,16 @@ static int mcm_multi_impl(ps_ctx* c, unsigned cases, const double* const W[4], i
     p.nwin = K;
     if ((st = stage_windows(c, p, wsel, K, nW, lmax, host, mode))) return st;
     const long long n = lmax - lmin + 1;
-    if (host) {
+    // Host outputs in mapped page-locked memory are written by the kernel
+    // itself, so the transfer to the host overlaps the computation; pageable
+    // outputs go through a device staging matrix and one copy each.
+    bool direct = host;
+    double* mapped[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int k = 0; k < K && direct; ++k) direct = (mapped[k] = mapped_host(M[sel[k]])) != nullptr;
+    if (direct) {
+        for (int k = 0; k < K; ++k) p.out[k] = mapped[k];
+        p.ldo = ldm;
+    } else if (host) {
         if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
         for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
         p.ldo = n;
@@ -480,7 +502,9 @@ static int mcm_multi_impl(ps_ctx* c, unsigned cases, const double* const W[4], i
         p.ldo = ldm;
     }
     if ((st = run_coupling(c, p, mode))) return st;
-    if (host) {
+    if (direct) {
+        PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    } else if (host) {
         for (int k = 0; k < K; ++k)
             PS_CUDA(c, cudaMemcpy2DAsync(M[sel[k]], (size_t)ldm * sizeof(double), p.out[k], (size_t)n * sizeof(double),
                                          (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));

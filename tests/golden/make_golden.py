@@ -13,6 +13,9 @@
   oracle_small.npz    oracle matrices (mode coupling, all spin cases, two window
                       lengths; all seven covariance kinds) at small lmax, to pin
                       the oracle against accidental change.
+  theory_noise.npz    the reference test suite's signal and noise spectra
+                      (test/data/theory.csv: cltt, clte, clee, clbb; noise.csv:
+                      nltt, nlee; l = 0..767), read from the reference checkout.
 
 Run from the repository root:  python tests/golden/make_golden.py [--ref PATH]
 """
@@ -34,6 +37,20 @@ def make_namaster(ref):
     out = {k: np.loadtxt(os.path.join(d, "mcm_%s_diag.txt" % k)) for k in ("TT", "EE", "TE")}
     np.savez(os.path.join(HERE, "namaster_diag.npz"), **out)
     print("namaster_diag.npz", {k: v.shape for k, v in out.items()})
+
+
+def make_theory_noise(ref):
+    d = os.path.join(ref, "test", "data")
+    out = {}
+    for fname in ("theory.csv", "noise.csv"):
+        with open(os.path.join(d, fname)) as f:
+            cols = f.readline().strip().split(",")
+            data = np.loadtxt(f, delimiter=",")
+        for i, c in enumerate(cols[1:], start=1):
+            out[c] = data[:, i]
+        assert np.array_equal(data[:, 0], np.arange(len(data)))
+    np.savez(os.path.join(HERE, "theory_noise.npz"), **out)
+    print("theory_noise.npz", {k: v.shape for k, v in out.items()})
 
 
 def make_decouple(ref):
@@ -122,6 +139,8 @@ if __name__ == "__main__":
         make_namaster(a.ref)
     if a.only in ("all", "decouple"):
         make_decouple(a.ref)
+    if a.only in ("all", "theory"):
+        make_theory_noise(a.ref)
     if a.only in ("all", "oracle"):
         make_oracle_small()
     if a.only in ("all", "exact"):

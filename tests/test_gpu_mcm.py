@@ -164,3 +164,21 @@ def test_launch_count_and_timing(ctx):
     ctx.mcm(0, W, 0, 20)
     assert ctx.launch_count() > n0
     assert ctx.last_kernel_ms() >= 0.0
+
+
+@pytest.mark.parametrize("mode", ["plain", "chosen"])
+def test_pinned_host_outputs_written_in_place(ctx, mode):
+    """Outputs in page-locked host memory are written by the kernel directly (no staging copy);
+    the result equals the pageable-output path bit for bit."""
+    import torch
+    from powerspectra_gpu import synthetic as syn
+    L = 300
+    c = syn.all_spins(L)
+    Ws = {0: c["WT"], 1: c["WTP"], 2: c["WP"], 3: c["WP"]}
+    n = L + 1
+    pinned = {s: torch.full((n, n), np.nan, dtype=torch.float64).pin_memory().numpy().T for s in Ws}
+    pageable = ctx.mcm_multi(Ws, 0, L, mode=mode)
+    got = ctx.mcm_multi(Ws, 0, L, mode=mode, outs=pinned)
+    for s in Ws:
+        assert got[s] is pinned[s]
+        assert np.array_equal(pinned[s], pageable[s])
