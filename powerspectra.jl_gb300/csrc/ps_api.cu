@@ -612,7 +612,11 @@ static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* c
         for (int i = 0; i < NR; ++i) p.R[i] = R[i];
     }
     const long long n = lmax - lmin + 1;
-    if (host) {
+    double* mapped = host ? mapped_host(C) : nullptr;  // page-locked C: written by the kernel itself
+    if (mapped) {
+        p.out[0] = mapped;
+        p.ldo = ldc;
+    } else if (host) {
         if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)n * n))) return st;
         p.out[0] = c->d_out;
         p.ldo = n;
@@ -622,8 +626,9 @@ static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* c
     }
     if ((st = run_coupling(c, p, mode))) return st;
     if (host) {
-        PS_CUDA(c, cudaMemcpy2DAsync(C, (size_t)ldc * sizeof(double), p.out[0], (size_t)n * sizeof(double),
-                                     (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        if (!mapped)
+            PS_CUDA(c, cudaMemcpy2DAsync(C, (size_t)ldc * sizeof(double), p.out[0], (size_t)n * sizeof(double),
+                                         (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
         PS_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     return PS_OK;

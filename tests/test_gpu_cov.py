@@ -93,3 +93,18 @@ def test_cov_argument_errors(ctx):
         ctx.coupledcov("TTEE", [one[:5]] * 4, [], [one] * 2, 0, 10)  # spectra shorter than lmax+1
     with pytest.raises(pg.PowerSpectraArgumentError):
         ctx.coupledcov("TTEE", [one] * 4, [], [one] * 3, 0, 10)  # wrong window count
+
+
+def test_pinned_host_output_written_in_place(ctx):
+    """A page-locked covariance output is written by the kernel directly; same bits as the
+    pageable path."""
+    import torch
+    import powerspectra_gpu as pg
+    from powerspectra_gpu import synthetic as syn
+    L = 200
+    ws, spectra, noise = syn.covariance_inputs(L)
+    kind, S, R, Ws = pg.covariance.gather("TE", "TE", ws, spectra, noise)
+    ref = ctx.coupledcov(kind, S, R, Ws, 0, L, mode="chosen")
+    pinned = torch.full((L + 1, L + 1), np.nan, dtype=torch.float64).pin_memory().numpy().T
+    got = ctx.coupledcov(kind, S, R, Ws, 0, L, mode="chosen", out=pinned)
+    assert got is pinned and np.array_equal(pinned, ref)
