@@ -96,3 +96,19 @@ def test_chosen_lmax_8191_sampled_rows(ctx):
         for r in rows:
             assert max_err_scaled(C[s][r, r:], R[r, r:], np.abs(R[r, r:])) < TOL, (s, r)
             assert max_err_scaled(C[s][r:, r], R[r:, r], np.abs(R[r:, r])) < TOL, (s, r)
+
+
+def test_chosen_at_the_largest_lmax(ctx):
+    """lmax 16383 (the largest the library accepts), nW 32767, TT and ++ from one window pass:
+    sampled rows against the oracle.  At this size the integer factors of the step coefficients
+    reach 2^16 and their products 2^64, the edge of what the float-float tables are built for."""
+    from powerspectra_gpu import synthetic as syn
+    L = 16383
+    W = syn.mask_spectrum(2 * L + 1, 0.6, 1500.0, seed=16383)
+    rows = [2, 9000, 16383]
+    C = ctx.mcm_multi({0: W, 2: W}, 0, L, mode="chosen")
+    for s in (0, 2):
+        R = o.inner_mcm(s, W, 0, L, rows=rows)
+        for r in rows:
+            assert max_err_scaled(C[s][r, r:], R[r, r:], np.abs(R[r, r:])) < TOL, (s, r)
+            assert max_err_scaled(C[s][r:, r], R[r:, r], np.abs(R[r:, r])) < TOL, (s, r)
