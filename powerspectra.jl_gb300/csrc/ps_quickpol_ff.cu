@@ -5,7 +5,7 @@
 //
 // Same mapping and algorithm as k_quickpol_fp64 (one thread per (l'', l); both
 // families forward from their own jmin and backward from jmax, matched at one
-// common point), with:
+// common point; here the two sweeps run interleaved in one loop), with:
 //   * P(j) = A(j)^2 = (j-|d|)(j+|d|)(s-j)(s+j)(j-|m3|)(j+|m3|) formed from its
 //     six exact integer factors (d = l1 - l2, s = l1 + l2 + 1): three exact
 //     two_prod pairs and two float-float products;
@@ -158,78 +158,76 @@ __global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ W
         if (jm >= jmax) jm = jmax - 1;
         const bool fwd0 = F[0].jmin <= jm, fwd1 = F[1].jmin <= jm;
         const ff zero = ff_make(0.0f), one = ff_make(1.0f);
-        // ---- forward: each family from its own jmin up to jm (values at jm + 1 kept) ----
+        // The forward sweep (each family from its own jmin up to jm; values at
+        // jm + 1 kept) and the backward sweep (from jmax down to jm + 1, and to
+        // jmin for backward-only families) run interleaved in one loop: four
+        // independent dependency chains per thread.
         ff fp0 = zero, fc0 = zero, fp1 = zero, fc1 = zero, af0 = zero, af1 = zero;
-        double NF0 = 0.0, NF1 = 0.0, SF = 0.0;
-        float nf0 = 0.0f, nf1 = 0.0f, sf = 0.0f;
-        int cnt = 0;
-        const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
-        QShared qc = qp_shared((float)jlo, adf, spf);  // carried: the next point's parts become the current ones
-        float jf = (float)jlo;                         // j as a float, stepped with j
-        for (int j = jlo; j <= jm; ++j, jf += 1.0f) {
-            if (fwd0 && j == F[0].jmin) fc0 = one;
-            if (fwd1 && j == F[1].jmin) fc1 = one;
-            const float g0 = ff_round(fc0), g1 = ff_round(fc1), w = __fmaf_rn(2.0f, jf, 1.0f);
-            nf0 = __fmaf_rn(w, __fmul_rn(g0, g0), nf0);
-            nf1 = __fmaf_rn(w, __fmul_rn(g1, g1), nf1);
-            if (j < nW) sf = __fmaf_rn(__fmul_rn(__ldg(Wf + j), g0), g1, sf);
-            const QShared qn = qp_shared(jf + 1.0f, adf, spf);
-            const ff jsq = two_prod(jf, jf);
-            if (fwd0 && j >= F[0].jmin) {
-                const ff n = qp_fwd(jf, F[0], qc, qn, jsq, fc0, fp0, af0);
-                fp0 = fc0;
-                fc0 = n;
-            }
-            if (fwd1 && j >= F[1].jmin) {
-                const ff n = qp_fwd(jf, F[1], qc, qn, jsq, fc1, fp1, af1);
-                fp1 = fc1;
-                fc1 = n;
-            }
-            qc = qn;
-            if (++cnt == kQpFlush) {
-                NF0 += nf0; NF1 += nf1; SF += sf;
-                nf0 = nf1 = sf = 0.0f;
-                cnt = 0;
-            }
-        }
-        NF0 += nf0; NF1 += nf1; SF += sf;
-        // ---- backward: from jmax down to jm + 1 (and to jmin for backward-only families) ----
         ff hn0 = zero, hc0 = one, hn1 = zero, hc1 = one, ab0 = zero, ab1 = zero;
         ff hm0_0 = zero, hm1_0 = zero, hm0_1 = zero, hm1_1 = zero;  // h(jm), h(jm+1) per family
-        double NB0 = 0.0, NB1 = 0.0, SB = 0.0;
-        float nb0 = 0.0f, nb1 = 0.0f, sb = 0.0f;
-        cnt = 0;
+        double NF0 = 0.0, NF1 = 0.0, SF = 0.0, NB0 = 0.0, NB1 = 0.0, SB = 0.0;
+        float nf0 = 0.0f, nf1 = 0.0f, sf = 0.0f, nb0 = 0.0f, nb1 = 0.0f, sb = 0.0f;
+        const int jlo = min(fwd0 ? F[0].jmin : jm + 1, fwd1 ? F[1].jmin : jm + 1);
         const int jstop = min(fwd0 ? jm + 1 : F[0].jmin, fwd1 ? jm + 1 : F[1].jmin);
-        float jbf = (float)jmax;
-        for (int j = jmax; j >= jstop; --j, jbf -= 1.0f) {
-            const bool in0 = j >= (fwd0 ? jm + 1 : F[0].jmin), in1 = j >= (fwd1 ? jm + 1 : F[1].jmin);
-            const float v0 = in0 ? ff_round(hc0) : 0.0f, v1 = in1 ? ff_round(hc1) : 0.0f, w = __fmaf_rn(2.0f, jbf, 1.0f);
-            nb0 = __fmaf_rn(w, __fmul_rn(v0, v0), nb0);
-            nb1 = __fmaf_rn(w, __fmul_rn(v1, v1), nb1);
-            if (j < nW) sb = __fmaf_rn(__fmul_rn(__ldg(Wf + j), v0), v1, sb);
-            const QShared qc = qp_shared(jbf, adf, spf);
-            const ff j1sq = two_prod(jbf + 1.0f, jbf + 1.0f);
-            if (in0 && j > F[0].jmin) {
-                if (j == jm + 1) hm1_0 = hc0;
-                const ff n = qp_bwd(jbf, F[0], qc, j1sq, hc0, hn0, ab0);
-                hn0 = hc0;
-                hc0 = n;
-                if (j == jm + 1) hm0_0 = hc0;
+        const int nfwd = jm - jlo + 1, nbwd = jmax - jstop + 1, nit = max(nfwd, nbwd);
+        QShared qc = qp_shared((float)jlo, adf, spf);  // forward: the next point's parts become the current ones
+        float jf = (float)jlo, jbf = (float)jmax;      // the two sweeps' points as floats
+        int cnt = 0;
+        for (int it = 0; it < nit; ++it, jf += 1.0f, jbf -= 1.0f) {
+            if (it < nfwd) {
+                const int j = jlo + it;
+                if (fwd0 && j == F[0].jmin) fc0 = one;
+                if (fwd1 && j == F[1].jmin) fc1 = one;
+                const float g0 = ff_round(fc0), g1 = ff_round(fc1), w = __fmaf_rn(2.0f, jf, 1.0f);
+                nf0 = __fmaf_rn(w, __fmul_rn(g0, g0), nf0);
+                nf1 = __fmaf_rn(w, __fmul_rn(g1, g1), nf1);
+                if (j < nW) sf = __fmaf_rn(__fmul_rn(__ldg(Wf + j), g0), g1, sf);
+                const QShared qn = qp_shared(jf + 1.0f, adf, spf);
+                const ff jsq = two_prod(jf, jf);
+                if (fwd0 && j >= F[0].jmin) {
+                    const ff n = qp_fwd(jf, F[0], qc, qn, jsq, fc0, fp0, af0);
+                    fp0 = fc0;
+                    fc0 = n;
+                }
+                if (fwd1 && j >= F[1].jmin) {
+                    const ff n = qp_fwd(jf, F[1], qc, qn, jsq, fc1, fp1, af1);
+                    fp1 = fc1;
+                    fc1 = n;
+                }
+                qc = qn;
             }
-            if (in1 && j > F[1].jmin) {
-                if (j == jm + 1) hm1_1 = hc1;
-                const ff n = qp_bwd(jbf, F[1], qc, j1sq, hc1, hn1, ab1);
-                hn1 = hc1;
-                hc1 = n;
-                if (j == jm + 1) hm0_1 = hc1;
+            if (it < nbwd) {
+                const int j = jmax - it;
+                const bool in0 = j >= (fwd0 ? jm + 1 : F[0].jmin), in1 = j >= (fwd1 ? jm + 1 : F[1].jmin);
+                const float v0 = in0 ? ff_round(hc0) : 0.0f, v1 = in1 ? ff_round(hc1) : 0.0f;
+                const float w = __fmaf_rn(2.0f, jbf, 1.0f);
+                nb0 = __fmaf_rn(w, __fmul_rn(v0, v0), nb0);
+                nb1 = __fmaf_rn(w, __fmul_rn(v1, v1), nb1);
+                if (j < nW) sb = __fmaf_rn(__fmul_rn(__ldg(Wf + j), v0), v1, sb);
+                const QShared qb = qp_shared(jbf, adf, spf);
+                const ff j1sq = two_prod(jbf + 1.0f, jbf + 1.0f);
+                if (in0 && j > F[0].jmin) {
+                    if (j == jm + 1) hm1_0 = hc0;
+                    const ff n = qp_bwd(jbf, F[0], qb, j1sq, hc0, hn0, ab0);
+                    hn0 = hc0;
+                    hc0 = n;
+                    if (j == jm + 1) hm0_0 = hc0;
+                }
+                if (in1 && j > F[1].jmin) {
+                    if (j == jm + 1) hm1_1 = hc1;
+                    const ff n = qp_bwd(jbf, F[1], qb, j1sq, hc1, hn1, ab1);
+                    hn1 = hc1;
+                    hc1 = n;
+                    if (j == jm + 1) hm0_1 = hc1;
+                }
             }
             if (++cnt == kQpFlush) {
-                NB0 += nb0; NB1 += nb1; SB += sb;
-                nb0 = nb1 = sb = 0.0f;
+                NF0 += nf0; NF1 += nf1; SF += sf; NB0 += nb0; NB1 += nb1; SB += sb;
+                nf0 = nf1 = sf = nb0 = nb1 = sb = 0.0f;
                 cnt = 0;
             }
         }
-        NB0 += nb0; NB1 += nb1; SB += sb;
+        NF0 += nf0; NF1 += nf1; SF += sf; NB0 += nb0; NB1 += nb1; SB += sb;
         // ---- match, normalise, sign (FP64) ----
         const double p0 = ff_to_double(fp0), c0 = ff_to_double(fc0), p1 = ff_to_double(fp1), c1 = ff_to_double(fc1);
         const double a0 = ff_to_double(hm0_0), b0 = ff_to_double(hm1_0), a1 = ff_to_double(hm0_1),
