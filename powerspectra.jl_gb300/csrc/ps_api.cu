@@ -1057,14 +1057,26 @@ int ps_window_W(ps_ctx* c, const double* const* A, const double* const* B, int n
     for (int t = 0; t < nterms; ++t)
         for (const double* q : {A[t], B[t]})
             if (q && std::find(uniq.begin(), uniq.end(), q) == uniq.end()) uniq.push_back(q);
-    if ((st = ensure(c, &c->d_alm, &c->alm_cap, 2 * nalm * (uniq.size() ? uniq.size() : 1)))) return st;
+    // A page-locked, mapped set is read by the kernel where it lies (over the
+    // host link, once); any other set is copied to the device first.
+    std::vector<const double*> where(uniq.size());
+    size_t ncopy = 0;
+    for (size_t u = 0; u < uniq.size(); ++u) {
+        const double* m = mapped_host(const_cast<double*>(uniq[u]));
+        where[u] = (m && ((uintptr_t)m & 15) == 0) ? m : nullptr;
+        if (!where[u]) ++ncopy;
+    }
+    if ((st = ensure(c, &c->d_alm, &c->alm_cap, 2 * nalm * (ncopy ? ncopy : 1)))) return st;
     if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)lout + 1))) return st;
-    for (size_t u = 0; u < uniq.size(); ++u)
-        PS_CUDA(c, cudaMemcpyAsync(c->d_alm + 2 * nalm * u, uniq[u], 2 * nalm * sizeof(double), cudaMemcpyHostToDevice,
-                                   c->stream));
+    for (size_t u = 0, k = 0; u < uniq.size(); ++u) {
+        if (where[u]) continue;
+        where[u] = c->d_alm + 2 * nalm * k++;
+        PS_CUDA(c, cudaMemcpyAsync(const_cast<double*>(where[u]), uniq[u], 2 * nalm * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+    }
     auto dev = [&](const double* q) -> const double* {
         if (!q) return nullptr;
-        return c->d_alm + 2 * nalm * (size_t)(std::find(uniq.begin(), uniq.end(), q) - uniq.begin());
+        return where[(size_t)(std::find(uniq.begin(), uniq.end(), q) - uniq.begin())];
     };
     const double* dA[ps::kAlmMaxTerms];
     const double* dB[ps::kAlmMaxTerms];

@@ -132,3 +132,17 @@ def test_alm_workspace_feeds_coupledcov(ctx):
         kind, S, R, Ws = pg.covariance.gather(*ch, ref_ws, spectra, noise)
         ref = o.loop_cov(kind, S, R, Ws, 0, L)
         assert max_err_scaled(C.parent, ref, cov_scale(kind, S, R, Ws, 0, L)) < 1e-11, ch
+
+
+def test_pinned_host_sets_read_in_place(ctx):
+    """Page-locked coefficient sets are read by the kernel where they lie; same bits as copied sets."""
+    import torch
+    lmax = 700
+    a, b = _alm(lmax, lmax, 21), _alm(lmax, lmax, 22)
+    ref = ctx.window_W([a, a], [b, None], lmax)
+    pa = torch.from_numpy(a.view(np.float64).copy()).pin_memory().numpy().view(np.complex128)
+    pb = torch.from_numpy(b.view(np.float64).copy()).pin_memory().numpy().view(np.complex128)
+    got = ctx.window_W([pa, pa], [pb, None], lmax)
+    assert np.array_equal(got, ref)
+    mixed = ctx.window_W([pa, a], [b, pb], lmax)  # one pinned and one pageable set per term
+    np.testing.assert_allclose(mixed, 0.5 * (ctx.window_W([a], [b], lmax) + ctx.window_W([a], [b], lmax)), rtol=1e-15)
