@@ -205,7 +205,7 @@ typedef struct ps_problem {
 /* Batched uneven workload in one persistent launch (chosen arithmetic).
  * The reference has no counterpart: it runs the problems one `mcm` call at a
  * time.  prepare() splits every problem into window groups of up to
- * `group_slots` (2 or 4) (window, case) slots -- whole windows per group, so
+ * `group_slots` (2, 4 or 8) (window, case) slots -- whole windows per group, so
  * the ++ and -- of one spectrum share their family -- builds one work queue
  * over all problems ordered by kernel body and decreasing family length, and
  * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
@@ -217,7 +217,7 @@ typedef struct ps_problem {
 int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);
 int ps_batch_run(ps_ctx *ctx);
 int ps_batch_graph_launch(ps_ctx *ctx);
-/* Times every (group_slots in {2, 4}) x (blocks per SM) configuration on
+/* Times every (group_slots in {2, 4, 8}) x (blocks per SM) configuration on
  * the given problems, keeps the fastest as the context's default and returns it. */
 int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best_group_slots,
                       int *best_blocks_per_sm, double *best_ms);

@@ -685,7 +685,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
             }
         }
         base.wlen = wlen;
-        const int gs = mode == PS_MODE_CHOSEN ? 4 : ps::kMaxWin;
+        const int gs = ps::kMaxWin;  // one generation of the families serves up to 8 slots
         for (const auto& grp : group_slots(cases, K, gs)) {
             ps::CouplingParams p = base;
             p.nwin = (int)grp.size();
@@ -709,7 +709,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     for (int i = 0; i < nprob; ++i)
         if ((st = check_problem(c, probs[i], i))) return st;
     if (gs == 0) gs = c->tuned_group_slots ? c->tuned_group_slots : 4;
-    if (gs != 2 && gs != 4) return set_err(c, PS_ERR_ARG, "group_slots must be 2 or 4 (got %d)", gs);
+    if (gs != 2 && gs != 4 && gs != 8) return set_err(c, PS_ERR_ARG, "group_slots must be 2, 4 or 8 (got %d)", gs);
     PS_CUDA(c, cudaSetDevice(c->device));
     batch_release(c);
     ps_ctx::Batch& b = c->batch;
@@ -769,7 +769,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
                 if (g.win[q].product != ps::PROD_00_00) f22 = true;
             }
             const int fam = (f00 ? 1 : 0) | (f22 ? 2 : 0);
-            const int tmpl = ps::chosen_batch_template(g);
+            const int tmpl = ps::chosen_batch_template(g, gs);
             if (tmpl == 0) {
                 batch_release(c);
                 return set_err(c, PS_ERR_UNSUPPORTED, "problem %d: no batched kernel body for a window group", i);
@@ -805,7 +805,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     int nsm = 0;
     PS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
-    int occ = ps::batch_blocks_per_sm();
+    int occ = ps::batch_blocks_per_sm(gs);
     if (bps == 0) bps = c->tuned_blocks_per_sm ? c->tuned_blocks_per_sm : occ;
     if (bps < 1 || bps > occ) bps = occ;
     b.nitems = (int)sorted.size();
@@ -828,7 +828,7 @@ static int batch_enqueue(ps_ctx* c, cudaStream_t s)
     bp.nitems = b.nitems;
     bp.counter = b.d_counter;
     PS_CUDA(c, cudaEventRecord(c->ev0, s));
-    PS_CUDA(c, ps::launch_batch_chosen(bp, b.blocks, s));
+    PS_CUDA(c, ps::launch_batch_chosen(bp, b.blocks, b.group_slots, s));
     PS_CUDA(c, cudaEventRecord(c->ev1, s));
     return PS_OK;
 }
@@ -879,11 +879,11 @@ int ps_batch_graph_launch(ps_ctx* c)
 int ps_batch_autotune(ps_ctx* c, const ps_problem* probs, int nprob, int* best_gs, int* best_bps, double* best_ms)
 {
     if (!c) return PS_ERR_ARG;
-    const int cand_gs[2] = {2, 4};
+    const int cand_gs[3] = {2, 4, 8};
     double best = 1e300;
     int bg = 4, bb = 0, st;
-    for (int gi = 0; gi < 2; ++gi) {
-        int occ = ps::batch_blocks_per_sm();
+    for (int gi = 0; gi < 3; ++gi) {
+        int occ = ps::batch_blocks_per_sm(cand_gs[gi]);
         for (int bps = 1; bps <= occ; ++bps) {
             if ((st = ps_batch_prepare(c, probs, nprob, cand_gs[gi], bps))) return st;
             if ((st = ps_batch_run(c))) return st;  // warm-up

@@ -1,595 +1,12 @@
-// ps_chosen.cu -- the chosen coupling kernel: FP32-pipe recurrences with
-// two-word compensation, block-floating-point windows, FP64 anchors.
-//
-// Same work and mapping as the plain kernel (one warp = 32 consecutive l2 of one
-// l1 row; families (l1 l2 l3; 0 0 0) and (l1 l2 l3; -2 2 0) in registers,
-// contracted on the fly; see ps_plain_fp64.cu for the recurrence), with the
-// arithmetic moved off the FP64 pipe:
-//
-//  * recurrence state and coefficients are float-float values (ps_ff.cuh), so
-//    each step carries ~2^-46 relative error instead of FP32's 2^-24.  The
-//    step factors a(j)/a(j+1) and 1/a(j+1) split into a lane-uniform part and
-//    a part shared along u = 2i + t (see "coefficient tables" below); each
-//    chunk the warp tabulates both as float-float square-root ratios formed
-//    from exact integer products (FP32 1/sqrt estimate plus one compensated
-//    Newton step), and every step multiplies two table entries;
-//  * the forward (from jmin) and backward (from jmax) sweeps run interleaved
-//    in one loop: two independent dependency chains per lane;
-//  * windows are stored as (mantissa, exponent) pairs.  Every 32 steps each
-//    warp stages the slice of every window it is about to read into shared
-//    memory, scaled by 2^-E with E the largest exponent of the slice, so FP32
-//    keeps full relative precision whatever the windows' dynamic range
-//    (mask spectra span > 1e-45 at l ~ 8000).  The 32-step FP32 partial sums
-//    are added into FP64 totals with the factor 2^E;
-//  * FP64 is kept where stability and range need it: the last forward point,
-//    the least-squares match of the two sweeps, the normalisation, the sign and
-//    the totals.
-#include "ps_internal.cuh"
-#include "ps_epilogue.cuh"
-#include "ps_ff.cuh"
-
-#include <stdint.h>
+// ps_chosen.cu -- launches of the chosen coupling kernel (ps_chosen_task.cuh)
+// for window groups of up to 5 slots, and the window preparation kernels.
+// Groups of 6-8 slots are instantiated in ps_chosen8.cu, the batched kernel in
+// ps_batch_chosen.cu, so the three compile in parallel.
+#include "ps_chosen_task.cuh"
 
 namespace ps {
 
-constexpr int kChunk = 32;               // steps between window restaging / FP64 flushes
-constexpr int kSlots = kChunk + 32;      // staged window entries per warp, direction and window
-constexpr int kStagePerLane = kSlots / 32;
-
-__device__ __forceinline__ double pow2d(int e)
-{
-    e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
-    return __longlong_as_double((long long)(e + 1023) << 52);
-}
-
-__device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 below the normal range
-{
-    return d < -126 ? 0.0f : __int_as_float((d + 127) << 23);
-}
-
-// Window slices move in two stages.  fetch_slice issues asynchronous copies
-// (cp.async, 8 bytes per lane and slot) of the raw (mantissa, exponent) slots
-// [base, base + kSlots) into shared memory; they land while the previous chunk
-// computes.  scale_slice then rescales the raw slice by 2^-E, with E the
-// slice's largest exponent, into the FP32 slots the steps read, and returns E.
-__device__ __forceinline__ void fetch_slice(int2* raw, const int2* __restrict__ bf, int base, int wlen, int lane)
-{
-#pragma unroll
-    for (int q = 0; q < kStagePerLane; ++q) {
-        const int j = base + lane + 32 * q;
-        int2* d = raw + lane + 32 * q;
-        if (j >= 0 && j < wlen) {
-            const unsigned sa = (unsigned)__cvta_generic_to_shared(d);
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(bf + j) : "memory");
-        } else {
-            *d = make_int2(0, kZeroExp);
-        }
-    }
-}
-__device__ __forceinline__ void fetch_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void fetch_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-__device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane)
-{
-    int2 v[kStagePerLane];
-    int emax = kZeroExp;
-#pragma unroll
-    for (int q = 0; q < kStagePerLane; ++q) {
-        v[q] = raw[lane + 32 * q];
-        emax = max(emax, v[q].y);
-    }
-    emax = __reduce_max_sync(0xffffffffu, emax);
-#pragma unroll
-    for (int q = 0; q < kStagePerLane; ++q) dst[lane + 32 * q] = __int_as_float(v[q].x) * pow2f_or_zero(v[q].y - emax);
-    return emax;
-}
-
-// Window configuration: 4 bits per window, product + 1 in bits 0-1 (so a used
-// window is never 0) and parity in bits 2-3.  A non-zero SPEC fixes the
-// product and parity of every window slot at compile time (the common
-// mode-coupling and covariance sets); the number of used slots stays a launch
-// parameter (p.nwin <= NWIN), so one instantiation serves every prefix of its
-// slot list.  SPEC == 0 reads the configuration from the launch parameters.
-__host__ __device__ constexpr uint32_t wspec(int prod, int par) { return (uint32_t)((prod + 1) | (par << 2)); }
-template <uint32_t SPEC>
-__device__ __forceinline__ int wprod(const CouplingParams& p, int k)
-{
-    return SPEC ? (int)((SPEC >> (4 * k)) & 3u) - 1 : p.win[k].product;
-}
-template <uint32_t SPEC>
-__device__ __forceinline__ int wpar(const CouplingParams& p, int k)
-{
-    return SPEC ? (int)((SPEC >> (4 * k + 2)) & 3u) : p.win[k].parity;
-}
-
-// Per-direction recurrence state (float-float values; the 22 family is left
-// unnormalised between steps, see ff_add_raw).
-struct Sweep {
-    ff f2, f2o;   // 22 family at the current point and at the previous one
-    ff f0;        // 00 family at the last even point
-    float w;      // 2j + 1 at the current point
-};
-
-// The window configuration one task uses, read from the parameters once: the
-// inner loops then never reload launch parameters (which, when they live in
-// shared memory, the compiler could not keep in registers across the loop's
-// shared-memory stores).
-template <int NWIN>
-struct WinCfg {
-    int nwin;
-    int prod[NWIN], par[NWIN];
-};
-
-template <int NWIN, uint32_t SPEC>
-__device__ __forceinline__ WinCfg<NWIN> win_cfg(const CouplingParams& p)
-{
-    WinCfg<NWIN> c;
-    c.nwin = p.nwin;
-#pragma unroll
-    for (int k = 0; k < NWIN; ++k) {
-        c.prod[k] = wprod<SPEC>(p, k);
-        c.par[k] = wpar<SPEC>(p, k);
-    }
-    return c;
-}
-
-template <int NWIN, bool N00, bool N22, uint32_t SPEC, bool EVEN>
-__device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s, const float* sw, int slot,
-                                          float* c, float& n0, float& n2)
-{
-    const float g2 = N22 ? __fadd_rn(s.f2.h, s.f2.l) : 0.0f;  // the value rounded to one float
-    float x22 = __fmul_rn(g2, g2);
-    if (N22) n2 = __fmaf_rn(s.w, x22, n2);
-    if (EVEN) {
-        const float g0 = N00 ? __fadd_rn(s.f0.h, s.f0.l) : 0.0f;
-        float x00 = __fmul_rn(g0, g0);
-        float x02 = __fmul_rn(g0, g2);
-        if (N00) n0 = __fmaf_rn(s.w, x00, n0);
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin && p.par[k] != PAR_ODD) {
-                const int pr = p.prod[k];
-                float x = pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02);
-                c[k] = __fmaf_rn(x, sw[k * kSlots + slot], c[k]);
-            }
-        }
-    } else if (N22) {
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin && p.prod[k] == PROD_22_22 && p.par[k] != PAR_EVEN)
-                c[k] = __fmaf_rn(x22, sw[k * kSlots + slot], c[k]);
-        }
-    }
-}
-
-// One warp task: 32 consecutive l2 from l2_0 of row l1.  sF / sB are the
-// warp's shared-memory staging areas ([NWIN][kSlots] floats each).
-// ---- coefficient tables ----------------------------------------------------
-// For lane i of a warp task (l1, l2_0 + i) the recurrence coefficient at
-// forward step t factorises as P = G(t) F(u), u = 2i + t, with
-//   G(t) = t (2 l1 + 1 - t)             (the same for every lane)
-//   F(u) = (2 d0 + u)(2 l2_0 + 1 + u)   (d0 = l2_0 - l1, shared along u)
-// and at backward step t as P' = G'(t) F'(v), v = 2i - t, with
-//   G'(t) = (2 l1 - t)(1 + t),  F'(v) = (2 l2_0 + v)(2 l1 + 2 l2_0 + 1 + v).
-// So the step factors rho = a(j)/a(j+1) and 1/a(j+1) are products of a
-// lane-uniform G factor and a shared F factor.  Once per chunk the warp
-// tabulates these square-root ratios in shared memory (each lane a few
-// entries), and every step then costs two float-float products instead of a
-// float-float P, 1/sqrt(P) and a(j).
-constexpr int kFEnt = kChunk / 2 + 32;  // F entries per parity of u (or v)
-struct __align__(16) ffpair {
-    ff rho, r;  // loaded together (one 16-byte shared load)
-};
-struct CoefTab {
-    ffpair gF[kChunk];      // forward: sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))
-    ffpair fF[2][kFEnt];    // forward: sqrt(F(u)/F(u+1)), 1/sqrt(F(u+1))
-    ffpair gB[kChunk];      // backward: sqrt(G'(t-1)/G'(t)), 1/sqrt(G'(t))
-    ffpair fB[2][kFEnt];    // backward: sqrt(F'(v+1)/F'(v)), 1/sqrt(F'(v))
-};
-
-// rho = sqrt(X / Y) and r = 1 / sqrt(Y) for X >= 0, Y > 0 (float-float)
-__device__ __forceinline__ void sqrt_ratio(ff X, ff Y, ff& rho, ff& r)
-{
-    r = ff_rsqrt(Y);
-    rho = X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
-}
-
-__device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1, int l2_0, int lane)
-{
-    const ff zero = ff_make(0.0f);
-    {
-        const int ti = t0 + lane;
-        const float t = (float)ti;
-        ff a, b;
-        if (ti < T) {
-            sqrt_ratio(two_prod(t, (float)(2 * l1 + 1) - t), two_prod(t + 1.0f, (float)(2 * l1) - t), a, b);
-            tb.gF[lane] = ffpair{a, b};
-            sqrt_ratio(two_prod((float)(2 * l1 + 1) - t, t), two_prod((float)(2 * l1) - t, 1.0f + t), a, b);
-            tb.gB[lane] = ffpair{a, b};
-        } else {
-            tb.gF[lane] = tb.gB[lane] = ffpair{zero, zero};
-        }
-    }
-    const int d0 = l2_0 - l1;
-#pragma unroll
-    for (int q = 0; q < (2 * kFEnt + 31) / 32; ++q) {
-        const int e = lane + 32 * q;
-        if (e >= 2 * kFEnt) break;
-        ff a = zero, b = zero;
-        {   // forward, u = t0 + e
-            const float u = (float)(t0 + e);
-            sqrt_ratio(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
-                       two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u), a, b);
-            tb.fF[e & 1][e >> 1] = ffpair{a, b};
-        }
-        {   // backward, v = e - t0 - 31
-            const int v = e - t0 - (kChunk - 1);
-            if (2 * l2_0 + v > 0) {
-                const float fv = (float)v;
-                sqrt_ratio(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
-                           two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv), a, b);
-            } else {
-                a = b = zero;
-            }
-            tb.fB[e & 1][e >> 1] = ffpair{a, b};
-        }
-    }
-}
-
-// One table-driven step: f(next) = -(c (2j+1) f(cur) r + rho f(prev)), c = 4.
-template <bool N00, bool N22, bool ODD_STEP>
-__device__ __forceinline__ void tab_step(Sweep& s, ff rho, ff r, float dw)
-{
-    if (N22) {
-        ff u = ff_mul_raw(ff_mulf_raw(s.f2, 4.0f * s.w), r);
-        ff v = ff_mul_raw(rho, s.f2o);
-        ff nf = ff_neg(ff_add_raw(u, v));
-        s.f2o = s.f2;
-        s.f2 = nf;
-    }
-    if (N00 && ODD_STEP) s.f0 = ff_neg(ff_mul_raw(rho, s.f0));
-    s.w += dw;
-}
-
-template <bool N00, bool N22, bool ODD_STEP>
-__device__ __forceinline__ void tab_fwd(Sweep& s, const CoefTab& tb, int st, int lane)
-{
-    const int e = lane + (st >> 1);  // (u - t0) / 2; u - t0 = 2 lane + st has the parity of the step
-    const ffpair g = tb.gF[st], f = tb.fF[ODD_STEP][e];
-    ff rho = ff_mul_raw(g.rho, f.rho);
-    ff r = ff_mul_raw(g.r, f.r);
-    tab_step<N00, N22, ODD_STEP>(s, rho, r, 2.0f);
-}
-
-template <bool N00, bool N22, bool ODD_STEP>
-__device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int lane)
-{
-    // v - (-t0 - 31) = 2 lane - st + 31: odd for even steps, half of it lane + 15 - st / 2
-    const int e = lane + (kChunk / 2 - 1) - (st >> 1);
-    const ffpair g = tb.gB[st], f = tb.fB[!ODD_STEP][e];
-    ff rho = ff_mul_raw(g.rho, f.rho);
-    ff r = ff_mul_raw(g.r, f.r);
-    tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
-}
-
-template <int NWIN, bool N00, bool N22, uint32_t SPEC>
-__device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
-                                            float* sB, int2* raw, CoefTab& tb, const int lane)
-{
-    const int l2raw = l2_0 + lane;
-    const bool active = l2raw <= p.lmax;
-    const int l2 = active ? l2raw : p.lmax;
-    const int d = l2 - l1;
-    const int jmin = d, jmax = l1 + l2;
-    const int T = l1;
-    const bool fam22 = N22 && (l1 >= 2);
-    const int jmin0 = l2_0 - l1, jmax0 = l2_0 + l1;  // lane 0's ends: lane i reads slot i + step
-    const WinCfg<NWIN> wc = win_cfg<NWIN, SPEC>(p);
-
-    double Xi[kMaxWin];
-    if (T == 0) {
-        xi_single_term(p, l2, Xi);
-        if (active) write_pair(p, l1, l2, Xi);
-        return;
-    }
-
-    Sweep F, B;
-    F.f2 = ff_make(1.0f); F.f2o = ff_make(0.0f); F.f0 = ff_make(1.0f);
-    F.w = (float)(2 * jmin + 1);
-    B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.f0 = ff_make(1.0f);
-    B.w = (float)(2 * jmax + 1);
-    double FW[NWIN], BW[NWIN];
-#pragma unroll
-    for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
-    double FN0 = 0.0, FN2 = 0.0, BN0 = 0.0, BN2 = 0.0;
-
-    int2* rF = raw;                  // raw forward slices, [NWIN][kSlots]
-    int2* rB = raw + NWIN * kSlots;  // raw backward slices
-#pragma unroll
-    for (int k = 0; k < NWIN; ++k) {
-        if (k < p.nwin) {
-            fetch_slice(rF + k * kSlots, p.win[k].bf, jmin0, p.wlen, lane);
-            fetch_slice(rB + k * kSlots, p.win[k].bf, jmax0 - kChunk + 1, p.wlen, lane);
-        }
-    }
-    fetch_commit();
-    for (int t0 = 0; t0 < T; t0 += kChunk) {
-        int eF[NWIN], eB[NWIN];
-        fetch_wait_all();
-        __syncwarp();
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin) {
-                eF[k] = scale_slice(sF + k * kSlots, rF + k * kSlots, lane);
-                eB[k] = scale_slice(sB + k * kSlots, rB + k * kSlots, lane);
-            } else {
-                eF[k] = eB[k] = kZeroExp;
-            }
-        }
-        build_tables(tb, t0, T, l1, l2_0, lane);
-        __syncwarp();
-        if (t0 + kChunk < T) {  // the next chunk's slices land while this one computes
-#pragma unroll
-            for (int k = 0; k < NWIN; ++k) {
-                if (k < p.nwin) {
-                    fetch_slice(rF + k * kSlots, p.win[k].bf, jmin0 + t0 + kChunk, p.wlen, lane);
-                    fetch_slice(rB + k * kSlots, p.win[k].bf, jmax0 - t0 - 2 * kChunk + 1, p.wlen, lane);
-                }
-            }
-        }
-        fetch_commit();
-        float cF[NWIN], cB[NWIN];
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) cF[k] = cB[k] = 0.0f;
-        float n0F = 0.0f, n2F = 0.0f, n0B = 0.0f, n2B = 0.0f;
-        const int steps = min(kChunk, T - t0);  // t0 is even, so step s has the parity of s
-        int s = 0;
-        for (; s + 1 < steps; s += 2) {
-            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, false>(F, tb, s, lane);
-            tab_bwd<N00, N22, false>(B, tb, s, lane);
-            sweep_acc<NWIN, N00, N22, SPEC, false>(wc, F, sF, lane + s + 1, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, false>(wc, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, true>(F, tb, s + 1, lane);
-            tab_bwd<N00, N22, true>(B, tb, s + 1, lane);
-        }
-        if (s < steps) {  // one even step left (T odd, last chunk)
-            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
-            sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, false>(F, tb, s, lane);
-            tab_bwd<N00, N22, false>(B, tb, s, lane);
-        }
-        // ---- FP64 flush of the chunk sums ----
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) {
-            FW[k] = fma((double)cF[k], pow2d(eF[k]), FW[k]);
-            BW[k] = fma((double)cB[k], pow2d(eB[k]), BW[k]);
-        }
-        FN0 += (double)n0F;
-        FN2 += (double)n2F;
-        BN0 += (double)n0B;
-        BN2 += (double)n2B;
-        __syncwarp();
-    }
-
-    // last forward point t = T (j = jm), in FP64; its parity is that of T
-    const int jm = jmin + T;
-    const bool evenT = (T & 1) == 0;
-    {
-        double g2d = ff_to_double(F.f2), g0d = (N00 && evenT) ? ff_to_double(F.f0) : 0.0;
-        double x22 = g2d * g2d, x00 = g0d * g0d, x02 = g0d * g2d, w = 2.0 * jm + 1.0;
-        if (N22) FN2 = fma(w, x22, FN2);
-        if (N00) FN0 = fma(w, x00, FN0);
-#pragma unroll
-        for (int k = 0; k < NWIN; ++k) {
-            if (k < p.nwin) {
-                const int pr = wprod<SPEC>(p, k), pa = wpar<SPEC>(p, k);
-                double ww = __ldg(p.win[k].wW + jm);
-                if (evenT && pa != PAR_ODD)
-                    FW[k] = fma(pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02), ww, FW[k]);
-                else if (!evenT && pr == PROD_22_22 && pa != PAR_EVEN)
-                    FW[k] = fma(x22, ww, FW[k]);
-            }
-        }
-    }
-    // one more forward step for g(jm + 1) (and the 00 value at jm + 1 when T is odd)
-    const double gm0 = ff_to_double(F.f2);
-    double gm1 = 0.0, g0s;
-    {
-        // P(jm) = T(2d+T)(2l1+1-T)(2l2+1+T), P(jm+1) = (T+1)(2d+T+1)(2l1-T)(2l2+2+T)
-        const float fT = (float)T;
-        ff P0 = ff_mul_raw(two_prod(fT, (float)(2 * d) + fT), two_prod((float)(2 * l1 + 1) - fT, (float)(2 * l2 + 1) + fT));
-        ff P1 = ff_mul_raw(two_prod(fT + 1.0f, (float)(2 * d + 1) + fT), two_prod((float)(2 * l1) - fT, (float)(2 * l2 + 2) + fT));
-        ff rho, r;
-        sqrt_ratio(P0, P1, rho, r);
-        if (N22) gm1 = ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mul_raw(F.f2, ff_make(4.0f * F.w)), r), ff_mul_raw(rho, F.f2o))));
-        g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(rho, F.f0))) : ff_to_double(F.f0);
-    }
-
-    const double hm0 = ff_to_double(B.f2), hm1 = ff_to_double(B.f2o), h0s = ff_to_double(B.f0);
-
-    // match, normalise, sign (FP64)
-    const double lam0 = N00 ? g0s / h0s : 0.0;
-    const double lam2 = fam22 ? (gm0 * hm0 + gm1 * hm1) / (hm0 * hm0 + hm1 * hm1) : 0.0;
-    const double N0 = fma(lam0 * lam0, BN0, FN0);
-    const double N2 = fma(lam2 * lam2, BN2, FN2);
-    const double inv0 = N00 ? kInv4Pi / N0 : 0.0;
-    const double inv2 = fam22 ? kInv4Pi / N2 : 0.0;
-    double inv02 = 0.0;
-    if (N00 && fam22) inv02 = (((lam0 < 0.0) != (lam2 < 0.0)) ? -kInv4Pi : kInv4Pi) * rsqrt(N0 * N2);
-#pragma unroll
-    for (int k = 0; k < kMaxWin; ++k) {
-        Xi[k] = 0.0;
-        if (k < NWIN && k < p.nwin) {
-            const int pr = wprod<SPEC>(p, k);
-            if (pr == PROD_00_00)
-                Xi[k] = fma(lam0 * lam0, BW[k], FW[k]) * inv0;
-            else if (!fam22)
-                Xi[k] = 0.0;
-            else if (pr == PROD_22_22)
-                Xi[k] = fma(lam2 * lam2, BW[k], FW[k]) * inv2;
-            else
-                Xi[k] = fma(lam0 * lam2, BW[k], FW[k]) * inv02;
-        }
-    }
-    if (active) write_pair(p, l1, l2, Xi);
-}
-
-// n copies of one slot spec w (4 bits) in consecutive slots
-__host__ __device__ constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
-constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
-constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
-// the window sets of the mode-coupling and covariance entry points
-constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
-constexpr uint32_t S_PPMM = WPP | (WMM << 4);
-constexpr uint32_t S_PPMM2 = S_PPMM | (S_PPMM << 8);  // (++, --) of two windows
-static_assert(((S_PPMM2 >> 8) & 0xffu) == S_PPMM && ((S_PPMM2 >> 4) & 0xfu) == WMM, "slot layout of S_PPMM2");
-constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
-
-template <int NWIN, bool N00, bool N22, uint32_t SPEC>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
-{
-    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
-    __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
-    __shared__ CoefTab sT[kWarpsPerBlock];
-    const int warp = threadIdx.x >> 5;
-    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    if (gw >= p.ntasks) return;  // warp-uniform
-    const int2 task = p.tasks[gw];
-    chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], &sR[warp][0][0][0],
-                                      sT[warp], threadIdx.x & 31);
-}
-
-// Persistent batched kernel: every warp takes the next item of a work queue
-// that spans all problems and window groups of the batch, until the queue is
-// empty.  The queue is ordered by kernel body (the group's compile-time slot
-// list), then by decreasing family length.  An item is up to 8 warp tasks (256
-// consecutive l2) of one row of one window group; each warp copies its
-// group's CouplingParams from global into shared memory when the group
-// changes.
-template <int NWIN>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5) k_batch_chosen(const BatchParams bp)
-{
-    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
-    // each warp's copy of its current group's parameters: read in the inner
-    // loops, so they live in shared memory rather than behind global loads
-    __shared__ CouplingParams sG[kWarpsPerBlock];
-    __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
-    __shared__ CoefTab sT[kWarpsPerBlock];
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    float* sF = &sW[warp][0][0][0];
-    float* sB = &sW[warp][1][0][0];
-    int cur = -1;
-    for (;;) {
-        int it = 0;
-        if (lane == 0) it = (int)atomicAdd(bp.counter, 1u);
-        it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= bp.nitems) break;  // every warp leaves once the queue is drained; nothing waits
-        const int4 item = bp.items[it];  // (group, l1, first l2, tasks | families << 8 | template << 12)
-        if (item.x != cur) {
-            const int* src = reinterpret_cast<const int*>(bp.groups + item.x);
-            int* dst = reinterpret_cast<int*>(&sG[warp]);
-            for (int q = lane; q < (int)(sizeof(CouplingParams) / sizeof(int)); q += 32) dst[q] = src[q];
-            cur = item.x;
-            __syncwarp();
-        }
-        const CouplingParams& g = sG[warp];
-        const int ntask = item.w & 0xff, tmpl = item.w >> 12;  // bits 8-11 (families) only order the queue
-        for (int q = 0; q < ntask; ++q) {
-            const int l2_0 = item.z + 32 * q;
-            switch (tmpl) {  // the group's compile-time slot set (prepare never emits others)
-            case 1: chosen_task<4, true, false, rep(W00, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 2: chosen_task<4, false, true, S_PPMM2>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 3: chosen_task<4, true, true, S_MCM4>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 4: chosen_task<4, false, true, rep(WPP, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 5: chosen_task<4, false, true, rep(WMM, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            case 6: chosen_task<4, true, true, rep(W02, 4)>(g, item.y, l2_0, sF, sB, &sR[warp][0][0][0], sT[warp], lane); break;
-            default: break;  // prepare rejects groups without a body
-            }
-            __syncwarp();
-        }
-    }
-}
-
-cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, cudaStream_t s)
-{
-    if (bp.nitems <= 0) return cudaSuccess;
-    k_batch_chosen<4><<<blocks, kWarpsPerBlock * 32, 0, s>>>(bp);
-    return cudaGetLastError();
-}
-
-int batch_blocks_per_sm()
-{
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_chosen<4>, kWarpsPerBlock * 32, 0) != cudaSuccess) {
-        cudaGetLastError();
-        return 1;
-    }
-    return n > 0 ? n : 1;
-}
-
-// families a compile-time window set needs
-constexpr bool spec_needs(uint32_t spec, int nwin, bool fam00)
-{
-    bool need = false;
-    for (int k = 0; k < nwin; ++k) {
-        int pr = (int)((spec >> (4 * k)) & 3u) - 1;
-        need = need || (fam00 ? pr != PROD_22_22 : pr != PROD_00_00);
-    }
-    return need;
-}
-
-template <int NWIN, uint32_t SPEC>
-static cudaError_t launch_cfg(const CouplingParams& p, bool n00, bool n22, cudaStream_t s)
-{
-    const int threads = kWarpsPerBlock * 32;
-    const unsigned blocks = (unsigned)((p.ntasks + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    if constexpr (SPEC != 0) {
-        constexpr bool a = spec_needs(SPEC, NWIN, true), b = spec_needs(SPEC, NWIN, false);
-        (void)n00;
-        (void)n22;
-        k_coupling_chosen<NWIN, a, b, SPEC><<<blocks, threads, 0, s>>>(p);
-    } else {
-        if (n00 && n22)
-            k_coupling_chosen<NWIN, true, true, 0><<<blocks, threads, 0, s>>>(p);
-        else if (n22)
-            k_coupling_chosen<NWIN, false, true, 0><<<blocks, threads, 0, s>>>(p);
-        else
-            k_coupling_chosen<NWIN, true, false, 0><<<blocks, threads, 0, s>>>(p);
-    }
-    return cudaGetLastError();
-}
-
-
-// True when the first `nwin` slots of `spec` equal those of the template T.
-static bool spec_fits(uint32_t spec, int nwin, uint32_t T, int TN)
-{
-    if (nwin > TN) return false;
-    for (int k = 0; k < nwin; ++k)
-        if (((spec >> (4 * k)) & 0xfu) != ((T >> (4 * k)) & 0xfu)) return false;
-    return true;
-}
-
-static uint32_t spec_of(const CouplingParams& p)
-{
-    uint32_t spec = 0;
-    for (int k = 0; k < p.nwin && k < 8; ++k) spec |= wspec(p.win[k].product, p.win[k].parity) << (4 * k);
-    return spec;
-}
-
-int chosen_batch_template(const CouplingParams& p)
-{
-    const uint32_t spec = spec_of(p);
-    if (spec_fits(spec, p.nwin, rep(W00, 4), 4)) return 1;
-    if (spec_fits(spec, p.nwin, S_PPMM2, 4)) return 2;
-    if (spec_fits(spec, p.nwin, S_MCM4, 4)) return 3;
-    if (spec_fits(spec, p.nwin, rep(WPP, 4), 4)) return 4;
-    if (spec_fits(spec, p.nwin, rep(WMM, 4), 4)) return 5;
-    if (spec_fits(spec, p.nwin, rep(W02, 4), 4)) return 6;
-    return 0;
-}
+cudaError_t launch_chosen8(const CouplingParams& p, uint32_t spec, bool n00, bool n22, cudaStream_t s);
 
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s)
 {
@@ -614,12 +31,10 @@ cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s)
     if (spec_fits(spec, nw, rep(WPP, 4), 4)) return launch_cfg<4, rep(WPP, 4)>(p, n00, n22, s);
     if (spec_fits(spec, nw, rep(WMM, 4), 4)) return launch_cfg<4, rep(WMM, 4)>(p, n00, n22, s);
     if (spec_fits(spec, nw, S_TETE, 5)) return launch_cfg<5, S_TETE>(p, n00, n22, s);
-    if (spec_fits(spec, nw, rep(W00, 8), 8)) return launch_cfg<8, rep(W00, 8)>(p, n00, n22, s);
-    if (spec_fits(spec, nw, rep(WPP, 8), 8)) return launch_cfg<8, rep(WPP, 8)>(p, n00, n22, s);
     if (nw <= 1) return launch_cfg<1, 0>(p, n00, n22, s);
     if (nw <= 2) return launch_cfg<2, 0>(p, n00, n22, s);
     if (nw <= 4) return launch_cfg<4, 0>(p, n00, n22, s);
-    return launch_cfg<8, 0>(p, n00, n22, s);
+    return launch_chosen8(p, spec, n00, n22, s);
 }
 
 // (2 l3 + 1) W[l3] in FP64 -> (float mantissa in [0.5, 1), exponent); zeros -> (0, kZeroExp)

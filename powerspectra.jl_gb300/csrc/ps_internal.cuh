@@ -72,9 +72,10 @@ struct BatchParams {
 };
 
 // Launchers (ps_plain_fp64.cu, ps_chosen.cu).
-cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, cudaStream_t s);
-int batch_blocks_per_sm();
-int chosen_batch_template(const CouplingParams& p);  // compile-time slot set of a batch group (0: none fits)
+// The batched kernel with NWIN = 4 or 8 slots per group (nwin > 4 selects 8).
+cudaError_t launch_batch_chosen(const BatchParams& bp, int blocks, int nwin, cudaStream_t s);
+int batch_blocks_per_sm(int nwin);
+int chosen_batch_template(const CouplingParams& p, int nwin);  // compile-time slot set of a batch group (0: none fits)
 cudaError_t launch_prep_windows(const WinPrep* list, int n, int max_wlen, cudaStream_t s);
 cudaError_t launch_plain_fp64(const CouplingParams& p, cudaStream_t s);
 cudaError_t launch_chosen(const CouplingParams& p, cudaStream_t s);

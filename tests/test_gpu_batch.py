@@ -102,8 +102,8 @@ def test_batch_autotune_and_group_sizes(ctx):
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     try:
         best = ctx.batch_autotune(probs)
-        assert best["group_slots"] in (2, 4) and best["blocks_per_sm"] >= 1 and best["ms"] > 0
-        for gs in (2, 4):
+        assert best["group_slots"] in (2, 4, 8) and best["blocks_per_sm"] >= 1 and best["ms"] > 0
+        for gs in (2, 4, 8):
             ctx.batch_prepare(probs, group_slots=gs)
             ctx.batch_run()
             torch.cuda.synchronize()
@@ -121,4 +121,4 @@ def test_batch_argument_errors(ctx):
         ctx.batch_prepare([{"lmin": 0, "lmax": 10, "cases": 1, "nW": 10, "ldm": 11, "W": [0], "M": [1, 0, 0, 0]}])
     with pytest.raises(pg.PowerSpectraArgumentError):
         ctx.batch_prepare([{"lmin": 0, "lmax": 10, "cases": 1, "nW": 21, "ldm": 11, "W": [1], "M": [1, 0, 0, 0]}],
-                          group_slots=8)
+                          group_slots=3)
