@@ -128,6 +128,10 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
+/* The same with host spectra and host matrices: returns when every M is
+ * filled (page-locked matrices are written by the kernel in place). */
+int ps_mcm_set(ps_ctx *ctx, unsigned cases, const double *const *W, int K, int64_t nW, int lmin, int lmax, int mode,
+               double *const *M, int64_t ldm);
 
 /* decouple_covmat (src/covariance.jl:8-14): out = B1^-1 * Y * B2^-T for n x n
  * column-major host matrices Y, B1, B2 (leading dimension ld), by two FP64 LU

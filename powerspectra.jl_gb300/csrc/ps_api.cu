@@ -701,6 +701,49 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
     return PS_OK;
 }
 
+int ps_mcm_set(ps_ctx* c, unsigned cases, const double* const* W, int K, int64_t nW, int lmin, int lmax, int mode,
+               double* const* M, int64_t ldm)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldm);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    if (cases == 0 || (cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "cases mask 0x%x must select bits 0..3", cases);
+    if (K < 1 || !W || !M) return set_err(c, PS_ERR_ARG, "K >= 1 and W, M arrays required");
+    for (int k = 0; k < K; ++k) {
+        if (!W[k]) return set_err(c, PS_ERR_ARG, "W[%d] is NULL", k);
+        for (int s = 0; s < 4; ++s)
+            if ((cases & (1u << s)) && !M[4 * k + s]) return set_err(c, PS_ERR_ARG, "M[%d] is NULL", 4 * k + s);
+    }
+    PS_CUDA(c, cudaSetDevice(c->device));
+    // spectra in: only the entries the families can reach (l3 <= 2 lmax)
+    const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+    if ((st = ensure(c, &c->d_raw, &c->raw_cap, (size_t)K * nuse))) return st;
+    std::vector<const double*> dW(K);
+    for (int k = 0; k < K; ++k) {
+        PS_CUDA(c, cudaMemcpyAsync(c->d_raw + (size_t)k * nuse, W[k], (size_t)nuse * sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+        dW[k] = c->d_raw + (size_t)k * nuse;
+    }
+    // matrices out: page-locked ones are written in place, the others staged (same leading dimension)
+    const size_t n = (size_t)(lmax - lmin + 1);
+    std::vector<double*> dM(4 * (size_t)K, nullptr);
+    std::vector<int> staged;
+    for (int i = 0; i < 4 * K; ++i) {
+        if (!(cases & (1u << (i & 3)))) continue;
+        if (!(dM[i] = mapped_host(M[i]))) staged.push_back(i);
+    }
+    if (!staged.empty()) {
+        if ((st = ensure(c, &c->d_out, &c->out_cap, staged.size() * n * (size_t)ldm))) return st;
+        for (size_t q = 0; q < staged.size(); ++q) dM[staged[q]] = c->d_out + q * n * (size_t)ldm;
+    }
+    if ((st = ps_mcm_set_device(c, cases, dW.data(), K, nuse, lmin, lmax, mode, dM.data(), ldm))) return st;
+    for (int i : staged)
+        PS_CUDA(c, cudaMemcpy2DAsync(M[i], (size_t)ldm * sizeof(double), dM[i], (size_t)ldm * sizeof(double),
+                                     n * sizeof(double), n, cudaMemcpyDeviceToHost, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
 int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int bps)
 {
     if (!c) return PS_ERR_ARG;

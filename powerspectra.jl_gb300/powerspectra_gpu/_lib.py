@@ -29,7 +29,7 @@ EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_sync
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
            "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device",
-           "ps_quickpol_xi_alm")
+           "ps_quickpol_xi_alm", "ps_mcm_set")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -92,6 +92,8 @@ def load(path=None):
         lib.ps_coupledcov_device.restype = ci
         lib.ps_mcm_set_device.argtypes = [vp, ctypes.c_uint, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
         lib.ps_mcm_set_device.restype = ci
+        lib.ps_mcm_set.argtypes = [vp, ctypes.c_uint, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
+        lib.ps_mcm_set.restype = ci
         lib.ps_batch_prepare.argtypes = [vp, ctypes.POINTER(PSProblem), ci, ci, ci]
         lib.ps_batch_prepare.restype = ci
         lib.ps_batch_run.argtypes = [vp]
@@ -326,6 +328,25 @@ class Context:
         self.check(self.lib.ps_coupledcov_device(self.handle, k, dptr_array([int(x) for x in dS]),
                                                  dptr_array([int(x) for x in dR]), dptr_array([int(x) for x in dW]),
                                                  int(nW), lmin, lmax, mode_code(mode), dptr(int(dC)), int(ldc)))
+
+    def mcm_set(self, cases, Ws, lmin, lmax, mode="chosen", outs=None):
+        """mcm for a set of host spectra on one grid: returns {(k, s): matrix} for window k and each spin
+        case s selected in `cases` (F-ordered float64; `outs` may supply them, e.g. page-locked)."""
+        Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]
+        n = lmax - lmin + 1
+        nW = min(len(w) for w in Ws)
+        res, ml = {}, []
+        for k in range(len(Ws)):
+            for s in range(4):
+                if cases & (1 << s):
+                    m = outs[k, s] if outs is not None else np.empty((n, n), dtype=np.float64, order="F")
+                    res[k, s] = m
+                    ml.append(m)
+                else:
+                    ml.append(None)
+        self.check(self.lib.ps_mcm_set(self.handle, int(cases), dptr_array(Ws), len(Ws), nW, lmin, lmax,
+                                       mode_code(mode), dptr_array(ml), n))
+        return res
 
     def mcm_set_device(self, cases, dW, nW, lmin, lmax, dM, ldm, mode="chosen"):
         """Many spectra on one grid: dW list of K device addresses, dM list of 4K

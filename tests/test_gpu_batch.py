@@ -122,3 +122,24 @@ def test_batch_argument_errors(ctx):
     with pytest.raises(pg.PowerSpectraArgumentError):
         ctx.batch_prepare([{"lmin": 0, "lmax": 10, "cases": 1, "nW": 21, "ldm": 11, "W": [1], "M": [1, 0, 0, 0]}],
                           group_slots=3)
+
+
+@pytest.mark.parametrize("cases", [0xF, 0xC, 0x1])
+def test_mcm_set_host(ctx, cases):
+    """ps_mcm_set: host spectra in, host matrices out (some page-locked, written in place)."""
+    L, K, lmin = 70, 3, 2
+    Ws = [_W(2 * L + 1, seed=40 + k) for k in range(K)]
+    n = L - lmin + 1
+    outs = {}
+    for k in range(K):
+        for s in range(4):
+            if cases & (1 << s):
+                if (k + s) % 2:
+                    outs[k, s] = torch.empty((n, n), dtype=torch.float64).pin_memory().numpy().T
+                else:
+                    outs[k, s] = np.empty((n, n), dtype=np.float64, order="F")
+    got = ctx.mcm_set(cases, Ws, lmin, L, mode="chosen", outs=outs)
+    for (k, s), m in got.items():
+        assert m is outs[k, s]
+        ref = o.inner_mcm(s, Ws[k], lmin, L)
+        assert max_err_scaled(m, ref, cond_scale(s, Ws[k], lmin, L)) < 1e-6, (k, s)
