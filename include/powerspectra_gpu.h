@@ -213,16 +213,18 @@ typedef struct ps_problem {
  * the ++ and -- of one spectrum share their family -- builds one work queue
  * over all problems ordered by kernel body and decreasing family length, and
  * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
- * ps_batch_autotune() found, else defaults.
- * run() enqueues the window preparation, the queue reset and ONE persistent
- * kernel.  graph_launch() captures run() into a CUDA graph on first use and
- * replays it afterwards.  The problems' pointers must stay valid while the
+ * ps_batch_autotune() found, else defaults.  blocks_per_sm = -1 selects the
+ * launch form instead: one chosen-kernel launch per window group.
+ * run() enqueues the window preparation, then the queue reset and ONE
+ * persistent kernel (or the per-group launches).  graph_launch() captures run()
+ * into a CUDA graph on first use and replays it afterwards.  The problems' pointers must stay valid while the
  * batch is in use. */
 int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);
 int ps_batch_run(ps_ctx *ctx);
 int ps_batch_graph_launch(ps_ctx *ctx);
-/* Times every (group_slots in {2, 4, 8}) x (blocks per SM) configuration on
- * the given problems, keeps the fastest as the context's default and returns it. */
+/* Times every (group_slots in {2, 4, 8}) x (blocks per SM, or -1 for the
+ * launch form) configuration on the given problems, keeps the fastest as the
+ * context's default and returns it. */
 int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best_group_slots,
                       int *best_blocks_per_sm, double *best_ms);
 

@@ -67,6 +67,11 @@ struct ps_ctx {
         double* d_win = nullptr;
         int2* d_bf = nullptr;
         cudaGraphExec_t exec = nullptr;
+        // one-launch-per-group form: the groups' parameters on the host, with
+        // task lists per (lmin, lmax) in d_tasks
+        bool launches = false;
+        std::vector<ps::CouplingParams> host_groups;
+        int2* d_tasks = nullptr;
     } batch;
     int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
     ps_linalg* la = nullptr;
@@ -290,6 +295,7 @@ static void batch_release(ps_ctx* c)
     cudaFree(b.d_counter);
     cudaFree(b.d_win);
     cudaFree(b.d_bf);
+    cudaFree(b.d_tasks);
     b = ps_ctx::Batch();
 }
 
@@ -840,22 +846,45 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     });
     std::vector<int4> sorted(items.size());
     for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+    // the warp task lists of every distinct (lmin, lmax), for the launch form
+    std::vector<int2> tasks;
+    std::vector<std::pair<long long, std::pair<size_t, int>>> task_of;  // (lmin, lmax) key -> (offset, count)
+    for (int i = 0; i < nprob; ++i) {
+        const long long key = ((long long)probs[i].lmin << 32) | (unsigned)probs[i].lmax;
+        bool have = false;
+        for (const auto& t : task_of) have = have || t.first == key;
+        if (have) continue;
+        const size_t off = tasks.size();
+        for (int l1 = probs[i].lmax; l1 >= probs[i].lmin; --l1)  // heaviest rows first
+            for (int l2 = l1; l2 <= probs[i].lmax; l2 += 32) tasks.push_back(make_int2(l1, l2));
+        task_of.push_back({key, {off, (int)(tasks.size() - off)}});
+    }
     if ((st = dev_upload(c, &b.d_groups, groups)) || (st = dev_upload(c, &b.d_items, sorted)) ||
-        (st = dev_upload(c, &b.d_preps, preps))) {
+        (st = dev_upload(c, &b.d_preps, preps)) || (st = dev_upload(c, &b.d_tasks, tasks))) {
         batch_release(c);
         return st;
+    }
+    b.host_groups = groups;
+    for (auto& g : b.host_groups) {
+        const long long key = ((long long)g.lmin << 32) | (unsigned)g.lmax;
+        for (const auto& t : task_of)
+            if (t.first == key) {
+                g.tasks = b.d_tasks + t.second.first;
+                g.ntasks = t.second.second;
+            }
     }
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     int nsm = 0;
     PS_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     int occ = ps::batch_blocks_per_sm(gs);
     if (bps == 0) bps = c->tuned_blocks_per_sm ? c->tuned_blocks_per_sm : occ;
-    if (bps < 1 || bps > occ) bps = occ;
+    b.launches = bps < 0;
+    if (!b.launches && (bps < 1 || bps > occ)) bps = occ;
     b.nitems = (int)sorted.size();
     b.npreps = (int)preps.size();
     b.max_wlen = max_wlen;
     b.group_slots = gs;
-    b.blocks = nsm * bps;
+    b.blocks = b.launches ? 0 : nsm * bps;
     b.ready = true;
     return PS_OK;
 }
@@ -864,6 +893,12 @@ static int batch_enqueue(ps_ctx* c, cudaStream_t s)
 {
     ps_ctx::Batch& b = c->batch;
     PS_CUDA(c, ps::launch_prep_windows(b.d_preps, b.npreps, b.max_wlen, s));
+    if (b.launches) {  // one chosen-kernel launch per window group, all on the stream
+        PS_CUDA(c, cudaEventRecord(c->ev0, s));
+        for (const auto& g : b.host_groups) PS_CUDA(c, ps::launch_chosen(g, s));
+        PS_CUDA(c, cudaEventRecord(c->ev1, s));
+        return PS_OK;
+    }
     PS_CUDA(c, cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s));
     ps::BatchParams bp;
     bp.groups = b.d_groups;
@@ -883,7 +918,7 @@ int ps_batch_run(ps_ctx* c)
     PS_CUDA(c, cudaSetDevice(c->device));
     int st = batch_enqueue(c, c->stream);
     if (st) return st;
-    c->launches += 2;
+    c->launches += c->batch.launches ? 1 + c->batch.host_groups.size() : 2;
     c->timed = true;
     return PS_OK;
 }
@@ -914,7 +949,7 @@ int ps_batch_graph_launch(ps_ctx* c)
         }
     }
     PS_CUDA(c, cudaGraphLaunch(b.exec, c->stream));
-    c->launches += 2;
+    c->launches += b.launches ? 1 + b.host_groups.size() : 2;
     c->timed = true;
     return PS_OK;
 }
@@ -927,7 +962,8 @@ int ps_batch_autotune(ps_ctx* c, const ps_problem* probs, int nprob, int* best_g
     int bg = 4, bb = 0, st;
     for (int gi = 0; gi < 3; ++gi) {
         int occ = ps::batch_blocks_per_sm(cand_gs[gi]);
-        for (int bps = 1; bps <= occ; ++bps) {
+        for (int bps = -1; bps <= occ; ++bps) {  // -1: one launch per group
+            if (bps == 0) continue;
             if ((st = ps_batch_prepare(c, probs, nprob, cand_gs[gi], bps))) return st;
             if ((st = ps_batch_run(c))) return st;  // warm-up
             if ((st = ps_batch_run(c))) return st;

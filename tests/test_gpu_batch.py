@@ -102,12 +102,17 @@ def test_batch_autotune_and_group_sizes(ctx):
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     try:
         best = ctx.batch_autotune(probs)
-        assert best["group_slots"] in (2, 4, 8) and best["blocks_per_sm"] >= 1 and best["ms"] > 0
+        assert best["group_slots"] in (2, 4, 8) and best["blocks_per_sm"] != 0 and best["ms"] > 0
         for gs in (2, 4, 8):
-            ctx.batch_prepare(probs, group_slots=gs)
-            ctx.batch_run()
-            torch.cuda.synchronize()
-            _check(refs)
+            for bps in (0, -1):  # persistent kernel, and one launch per group
+                for _, _, _, _, dM in refs:
+                    for m in dM:
+                        if m is not None:
+                            m.fill_(float("nan"))
+                ctx.batch_prepare(probs, group_slots=gs, blocks_per_sm=bps)
+                ctx.batch_run()
+                torch.cuda.synchronize()
+                _check(refs)
     finally:
         ctx.set_stream(0)
 
@@ -143,3 +148,21 @@ def test_mcm_set_host(ctx, cases):
         assert m is outs[k, s]
         ref = o.inner_mcm(s, Ws[k], lmin, L)
         assert max_err_scaled(m, ref, cond_scale(s, Ws[k], lmin, L)) < 1e-6, (k, s)
+
+
+def test_batch_launch_form_in_a_graph(ctx):
+    """blocks_per_sm = -1: one launch per window group, captured into a CUDA graph and replayed."""
+    probs, refs = _batch_problems(seed=5)
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        ctx.batch_prepare(probs, group_slots=8, blocks_per_sm=-1)
+        for _ in range(2):
+            for _, _, _, _, dM in refs:
+                for m in dM:
+                    if m is not None:
+                        m.fill_(float("nan"))
+            ctx.batch_graph_launch()
+            torch.cuda.synchronize()
+            _check(refs)
+    finally:
+        ctx.set_stream(0)
