@@ -182,3 +182,14 @@ def test_pinned_host_outputs_written_in_place(ctx, mode):
     for s in Ws:
         assert got[s] is pinned[s]
         assert np.array_equal(pinned[s], pageable[s])
+
+
+def test_fma_probe_and_instrumentation(ctx):
+    """The FMA-chain probe behind the bench roofline: both rates positive, FP32 far above FP64 on
+    this part; kernel timing and launch counting advance with a call."""
+    f64, f32 = ctx.fma_peak(fp64=True), ctx.fma_peak(fp64=False)
+    assert f64 > 0 and f32 > 8 * f64
+    n0 = ctx.launch_count()
+    W = np.ones(41)
+    ctx.mcm(0, W, 0, 20, mode="chosen")
+    assert ctx.launch_count() > n0 and ctx.last_kernel_ms() > 0
