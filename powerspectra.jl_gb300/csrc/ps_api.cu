@@ -1091,9 +1091,9 @@ static int window_run(ps_ctx* c, const double* const* dA, const double* const* d
     int st = ensure(c, &c->d_part, &c->part_cap, (size_t)nterms * p.nmchunks * ((size_t)lout + 1));
     if (st) return st;
     p.partial = c->d_part;
+    // the context's kernel time is the partial-sum kernel's (the reduction is small)
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    PS_CUDA(c, ps::launch_alm2cl(p, 1.0 / nterms, per_l, dW, c->stream));
-    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    PS_CUDA(c, ps::launch_alm2cl(p, 1.0 / nterms, per_l, dW, c->stream, c->ev1));
     c->launches += 2;
     c->timed = true;
     return PS_OK;

@@ -105,7 +105,9 @@ struct AlmParams {
     double* partial;  // nterms * nmchunks * (lout + 1)
 };
 int alm2cl_chunks(int mmax);
-cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s);
+// after_partial, when given, is recorded between the partial-sum kernel and the reduction.
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s,
+                          cudaEvent_t after_partial = nullptr);
 
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);

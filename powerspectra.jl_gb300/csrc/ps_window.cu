@@ -96,12 +96,14 @@ __global__ void k_alm2cl_reduce(const double* __restrict__ partial, int nterms, 
 
 int alm2cl_chunks(int mmax) { return (mmax + kAlmChunk) / kAlmChunk; }
 
-cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s)
+cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s,
+                          cudaEvent_t after_partial)
 {
     dim3 grid((p.lout + kAlmThreads) / kAlmThreads, p.nmchunks, p.nterms);
     k_alm2cl_partial<<<grid, kAlmThreads, 0, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (after_partial && (e = cudaEventRecord(after_partial, s)) != cudaSuccess) return e;
     k_alm2cl_reduce<<<(p.lout + 128) / 128, 128, 0, s>>>(p.partial, p.nterms, p.nmchunks, p.lout, scale, per_l ? 1 : 0, W);
     return cudaGetLastError();
 }
