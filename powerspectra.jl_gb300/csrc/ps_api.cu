@@ -567,13 +567,23 @@ int ps_xi(ps_ctx* c, int product, int parity, const double* const* W, int K, int
     }
     if ((st = stage_windows(c, p, W, K, nW, lmax, true, mode))) return st;
     const long long n = lmax - lmin + 1;
-    if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
-    for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
-    p.ldo = n;
+    // page-locked outputs are written in place (then with leading dimension ldx), others staged
+    bool direct = true;
+    double* mapped[ps::kMaxWin] = {};
+    for (int k = 0; k < K && direct; ++k) direct = (mapped[k] = mapped_host(Xi[k])) != nullptr;
+    if (direct) {
+        for (int k = 0; k < K; ++k) p.out[k] = mapped[k];
+        p.ldo = ldx;
+    } else {
+        if ((st = ensure(c, &c->d_out, &c->out_cap, (size_t)K * n * n))) return st;
+        for (int k = 0; k < K; ++k) p.out[k] = c->d_out + (size_t)k * n * n;
+        p.ldo = n;
+    }
     if ((st = run_coupling(c, p, mode))) return st;
-    for (int k = 0; k < K; ++k)
-        PS_CUDA(c, cudaMemcpy2DAsync(Xi[k], (size_t)ldx * sizeof(double), p.out[k], (size_t)n * sizeof(double),
-                                     (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    if (!direct)
+        for (int k = 0; k < K; ++k)
+            PS_CUDA(c, cudaMemcpy2DAsync(Xi[k], (size_t)ldx * sizeof(double), p.out[k], (size_t)n * sizeof(double),
+                                         (size_t)n * sizeof(double), (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PS_OK;
 }

@@ -386,10 +386,11 @@ class Context:
                                               ctypes.byref(ms)))
         return {"group_slots": g.value, "blocks_per_sm": b.value, "ms": ms.value}
 
-    def xi(self, product, parity, Ws, lmin, lmax, mode="plain"):
+    def xi(self, product, parity, Ws, lmin, lmax, mode="plain", outs=None):
         Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]
         n = lmax - lmin + 1
-        outs = [np.empty((n, n), dtype=np.float64, order="F") for _ in Ws]
+        if outs is None:
+            outs = [np.empty((n, n), dtype=np.float64, order="F") for _ in Ws]
         nW = min(len(w) for w in Ws)
         self.check(self.lib.ps_xi(self.handle, int(product), int(parity), dptr_array(Ws), len(Ws), nW, lmin, lmax,
                                   mode_code(mode), dptr_array(outs), n))

@@ -108,3 +108,16 @@ def test_pinned_host_output_written_in_place(ctx):
     pinned = torch.full((L + 1, L + 1), np.nan, dtype=torch.float64).pin_memory().numpy().T
     got = ctx.coupledcov(kind, S, R, Ws, 0, L, mode="chosen", out=pinned)
     assert got is pinned and np.array_equal(pinned, ref)
+
+
+def test_xi_pinned_outputs(ctx):
+    """ps_xi writes page-locked outputs in place; same bits as the staged path."""
+    import torch
+    from powerspectra_gpu import synthetic as syn
+    L = 120
+    Ws = [syn.mask_spectrum(2 * L + 1, 0.5, 50.0, seed=k) for k in range(3)]
+    ref = ctx.xi(1, 1, Ws, 0, L, mode="chosen")
+    pinned = [torch.full((L + 1, L + 1), np.nan, dtype=torch.float64).pin_memory().numpy().T for _ in Ws]
+    got = ctx.xi(1, 1, Ws, 0, L, mode="chosen", outs=pinned)
+    for g, p, r in zip(got, pinned, ref):
+        assert g is p and np.array_equal(p, r)
