@@ -353,7 +353,7 @@ def run_ours(args):
 SET_CONFIGS = ("batched_64", "large_8191", "cov_2508")
 
 
-def _set_problems(name):
+def _set_problems(name, lmax=0):
     """Host-side definition of the multi-matrix configurations.
 
     batched_64: 64 problems, lmax drawn from {511, ..., 6143}, K in 1..16 seeded mask
@@ -369,7 +369,7 @@ def _set_problems(name):
                         "nW": pr["lmax"] + 1, "W": pr["W"]})
         return out
     if name == "large_8191":
-        big = syn.large_set()
+        big = syn.large_set(lmax=lmax or 8191)
         groups = {0x1: [], 0x4: [], 0x8: []}
         for k, W in enumerate(big["W"]):
             groups[(0x1, 0x4, 0x8)[k % 3]].append(W)
@@ -408,7 +408,8 @@ def run_set(args):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / 1e3 / steps
 
-    line = {"config": {"workload": args.config}, "unit": UNIT}
+    line = {"config": {"workload": args.config if not args.lmax else "%s (lmax %d)" % (args.config, args.lmax)},
+            "unit": UNIT}
     if args.config == "cov_2508":
         L = 2508
         ws, spectra, noise = syn.covariance_inputs(L)
@@ -434,7 +435,7 @@ def run_set(args):
         plain = lambda: run("plain", outs_p)
         mats = list(zip(outs_c, outs_p))
     else:
-        probs = _set_problems(args.config)
+        probs = _set_problems(args.config, args.lmax)
         prob_dev, mats = [], []
         for pr in probs:
             n = pr["lmax"] - pr["lmin"] + 1
@@ -715,7 +716,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 kernel")
     ap.add_argument("--lmax", type=int, default=0,
-                    help="window_W_8191 only: another lmax (a smaller case for profiling); the JSON names it")
+                    help="window_W_8191 and large_8191: another lmax (a smaller case for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
