@@ -17,6 +17,9 @@
  *     0..nW-1, exactly like Xi_TT/Xi_EE/Xi_EB/Xi_TE (src/modecoupling.jl:3-66).
  *   - Host-pointer entry points copy inputs in, compute, copy results out and
  *     return when the output is filled (synchronous, like the Julia loops).
+ *     Outputs in page-locked host memory that is mapped into the device's
+ *     address space (cudaHostAlloc, cudaHostRegister) are written by the
+ *     kernel in place, with the same results.
  *     `_device` entry points take device pointers and enqueue on the context's
  *     stream without synchronising.
  *   - Every call returns PS_OK (0) or an error code; the message is kept per
@@ -160,8 +163,8 @@ int ps_solve(ps_ctx *ctx, const double *M, int64_t n, int64_t ldm, const double 
  * column-major (lmax+1) x (lmax+1) matrix (ld >= lmax+1) that receives the
  * band and zeros elsewhere.  General spins (|nu|, |s| <= 64); host pointers.
  * mode PS_MODE_PLAIN_FP64 runs the recurrences in FP64 like the reference;
- * PS_MODE_CHOSEN runs them in float-float on the FP32 pipe (max relative error
- * 1e-6 against FP64).  The reference stores Xi as a BandedMatrix; here the
+ * PS_MODE_CHOSEN runs them in float-float on the FP32 pipe (max error 1e-6 of
+ * the sum of |W f1 f2| behind each element, against FP64).  The reference stores Xi as a BandedMatrix; here the
  * band is written into a dense matrix. */
 int ps_quickpol_xi(ps_ctx *ctx, int nu1, int nu2, int s1, int s2, const double *W, int64_t nW, int lmax, int bl,
                    int bu, int mode, double *Xi, int64_t ldx);
@@ -217,8 +220,8 @@ typedef struct ps_problem {
  * launch form instead: one chosen-kernel launch per window group.
  * run() enqueues the window preparation, then the queue reset and ONE
  * persistent kernel (or the per-group launches).  graph_launch() captures run()
- * into a CUDA graph on first use and replays it afterwards.  The problems' pointers must stay valid while the
- * batch is in use. */
+ * into a CUDA graph on first use and replays it afterwards.  The problems'
+ * pointers must stay valid while the batch is in use. */
 int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);
 int ps_batch_run(ps_ctx *ctx);
 int ps_batch_graph_launch(ps_ctx *ctx);
