@@ -179,63 +179,77 @@ __device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s,
 // lane-uniform G factor and a shared F factor.  Once per chunk the warp
 // tabulates these square-root ratios in shared memory (each lane a few
 // entries), and every step then costs two float-float products instead of a
-// float-float P, 1/sqrt(P) and a(j).
+// float-float P, 1/sqrt(P) and a(j).  G'(t-1)/G'(t) = G(t)/G(t+1), built from
+// the same two products (each commutative), so one G table serves both sweeps.
 constexpr int kFEnt = kChunk / 2 + 32;  // F entries per parity of u (or v)
 struct __align__(16) ffpair {
     ff rho, r;  // loaded together (one 16-byte shared load)
 };
 struct CoefTab {
-    ffpair gF[kChunk];      // forward: sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))
+    ffpair g[kChunk];       // sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1)); both sweeps
     ffpair fF[2][kFEnt];    // forward: sqrt(F(u)/F(u+1)), 1/sqrt(F(u+1))
-    ffpair gB[kChunk];      // backward: sqrt(G'(t-1)/G'(t)), 1/sqrt(G'(t))
     ffpair fB[2][kFEnt];    // backward: sqrt(F'(v+1)/F'(v)), 1/sqrt(F'(v))
 };
 
-// rho = sqrt(X / Y) and r = 1 / sqrt(Y) for X >= 0, Y > 0 (float-float)
+// rho = sqrt(X / Y) for X >= 0, Y > 0 (float-float); 0 for X = 0
+__device__ __forceinline__ ff sqrt_ratio_rho(ff X, ff Y)
+{
+    return X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
+}
+// rho as above and r = 1 / sqrt(Y)
 __device__ __forceinline__ void sqrt_ratio(ff X, ff Y, ff& rho, ff& r)
 {
     r = ff_rsqrt(Y);
-    rho = X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
+    rho = sqrt_ratio_rho(X, Y);
 }
 
+// Without the (2 -2 0) family only the odd steps of the (0 0 0) recurrence use
+// the tables, and only rho: odd u forward and even v backward, so each lane
+// builds one F entry per 32 instead of two and no 1/sqrt(Y).
+template <bool N22>
 __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1, int l2_0, int lane)
 {
     const ff zero = ff_make(0.0f);
     {
         const int ti = t0 + lane;
         const float t = (float)ti;
-        ff a, b;
+        ff a = zero, b = zero;
         if (ti < T) {
-            sqrt_ratio(two_prod(t, (float)(2 * l1 + 1) - t), two_prod(t + 1.0f, (float)(2 * l1) - t), a, b);
-            tb.gF[lane] = ffpair{a, b};
-            sqrt_ratio(two_prod((float)(2 * l1 + 1) - t, t), two_prod((float)(2 * l1) - t, 1.0f + t), a, b);
-            tb.gB[lane] = ffpair{a, b};
-        } else {
-            tb.gF[lane] = tb.gB[lane] = ffpair{zero, zero};
+            const ff X = two_prod(t, (float)(2 * l1 + 1) - t), Y = two_prod(t + 1.0f, (float)(2 * l1) - t);
+            if (N22) sqrt_ratio(X, Y, a, b);
+            else a = sqrt_ratio_rho(X, Y);
         }
+        tb.g[lane] = ffpair{a, b};
     }
     const int d0 = l2_0 - l1;
 #pragma unroll
     for (int q = 0; q < (2 * kFEnt + 31) / 32; ++q) {
         const int e = lane + 32 * q;
         if (e >= 2 * kFEnt) break;
-        ff a = zero, b = zero;
-        {   // forward, u = t0 + e
-            const float u = (float)(t0 + e);
+        const float u = (float)(t0 + e);             // forward, u = t0 + e
+        const int v = e - t0 - (kChunk - 1);          // backward, v = e - t0 - 31
+        const bool vok = 2 * l2_0 + v > 0;
+        const float fv = (float)v;
+        if (N22) {
+            ff a, b;
             sqrt_ratio(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
                        two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u), a, b);
             tb.fF[e & 1][e >> 1] = ffpair{a, b};
-        }
-        {   // backward, v = e - t0 - 31
-            const int v = e - t0 - (kChunk - 1);
-            if (2 * l2_0 + v > 0) {
-                const float fv = (float)v;
+            if (vok) {
                 sqrt_ratio(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
                            two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv), a, b);
             } else {
                 a = b = zero;
             }
             tb.fB[e & 1][e >> 1] = ffpair{a, b};
+        } else if (e & 1) {  // odd forward step: fF[1]
+            tb.fF[1][e >> 1].rho = sqrt_ratio_rho(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
+                                                  two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u));
+        } else {             // odd backward step: fB[0]
+            tb.fB[0][e >> 1].rho =
+                vok ? sqrt_ratio_rho(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
+                                     two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv))
+                    : zero;
         }
     }
 }
@@ -259,7 +273,7 @@ template <bool N00, bool N22, bool ODD_STEP>
 __device__ __forceinline__ void tab_fwd(Sweep& s, const CoefTab& tb, int st, int lane)
 {
     const int e = lane + (st >> 1);  // (u - t0) / 2; u - t0 = 2 lane + st has the parity of the step
-    const ffpair g = tb.gF[st], f = tb.fF[ODD_STEP][e];
+    const ffpair g = tb.g[st], f = tb.fF[ODD_STEP][e];
     ff rho = ff_mul_raw(g.rho, f.rho);
     ff r = ff_mul_raw(g.r, f.r);
     tab_step<N00, N22, ODD_STEP>(s, rho, r, 2.0f);
@@ -270,7 +284,7 @@ __device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int
 {
     // v - (-t0 - 31) = 2 lane - st + 31: odd for even steps, half of it lane + 15 - st / 2
     const int e = lane + (kChunk / 2 - 1) - (st >> 1);
-    const ffpair g = tb.gB[st], f = tb.fB[!ODD_STEP][e];
+    const ffpair g = tb.g[st], f = tb.fB[!ODD_STEP][e];
     ff rho = ff_mul_raw(g.rho, f.rho);
     ff r = ff_mul_raw(g.r, f.r);
     tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
@@ -330,7 +344,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
                 eF[k] = eB[k] = kZeroExp;
             }
         }
-        build_tables(tb, t0, T, l1, l2_0, lane);
+        build_tables<N22>(tb, t0, T, l1, l2_0, lane);
         __syncwarp();
         if (t0 + kChunk < T) {  // the next chunk's slices land while this one computes
 #pragma unroll
