@@ -203,9 +203,75 @@ __device__ __forceinline__ void sqrt_ratio(ff X, ff Y, ff& rho, ff& r)
     rho = sqrt_ratio_rho(X, Y);
 }
 
+// F entry e of the chunk at t0: forward u = t0 + e, backward v = e - t0 - 31.
+__device__ __forceinline__ void f_fwd(CoefTab& tb, int e, int t0, int l1, int l2_0)
+{
+    const int d0 = l2_0 - l1;
+    const float u = (float)(t0 + e);
+    const ff X = two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u);
+    const ff Y = two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u);
+    ff a, b;
+    sqrt_ratio(X, Y, a, b);
+    tb.fF[e & 1][e >> 1] = ffpair{a, b};
+}
+__device__ __forceinline__ void f_bwd(CoefTab& tb, int e, int t0, int l1, int l2_0)
+{
+    const int v = e - t0 - (kChunk - 1);
+    const float fv = (float)v;
+    ff a = ff_make(0.0f), b = ff_make(0.0f);
+    if (2 * l2_0 + v > 0)
+        sqrt_ratio(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
+                   two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv), a, b);
+    tb.fB[e & 1][e >> 1] = ffpair{a, b};
+}
 // Without the (2 -2 0) family only the odd steps of the (0 0 0) recurrence use
-// the tables, and only rho: odd u forward and even v backward, so each lane
-// builds one F entry per 32 instead of two and no 1/sqrt(Y).
+// the tables, and only rho: odd e forward (fF[1]) and even e backward (fB[0]).
+// Lanes of odd e form a forward entry and lanes of even e a backward one, from
+// operands selected per lane, with one shared sqrt_ratio_rho.
+__device__ __forceinline__ void f_rho_odd_steps(CoefTab& tb, int e, int t0, int l1, int l2_0)
+{
+    const bool fwd = e & 1;
+    const int d0 = l2_0 - l1;
+    const float u = (float)(t0 + e);
+    const int v = e - t0 - (kChunk - 1);
+    const float fv = (float)v;
+    const float x1 = fwd ? (float)(2 * d0) + u : (float)(2 * l2_0 + 1) + fv;
+    const float x2 = fwd ? (float)(2 * l2_0 + 1) + u : (float)(2 * l1 + 2 * l2_0 + 2) + fv;
+    const float y1 = fwd ? (float)(2 * d0 + 1) + u : (float)(2 * l2_0) + fv;
+    const float y2 = fwd ? (float)(2 * l2_0 + 2) + u : (float)(2 * l1 + 2 * l2_0 + 1) + fv;
+    ff rho = sqrt_ratio_rho(two_prod(x1, x2), two_prod(y1, y2));
+    if (!fwd && 2 * l2_0 + v <= 0) rho = ff_make(0.0f);
+    (fwd ? tb.fF[1][e >> 1] : tb.fB[0][e >> 1]).rho = rho;
+}
+
+// The F entries of a task's first chunk (t0 = 0), formed in full.
+template <bool N22>
+__device__ __forceinline__ void init_f_tables(CoefTab& tb, int l1, int l2_0, int lane)
+{
+#pragma unroll
+    for (int q = 0; q < 2 * kFEnt / 32; ++q) {
+        const int e = lane + 32 * q;
+        if (N22) {
+            f_fwd(tb, e, 0, l1, l2_0);
+            f_bwd(tb, e, 0, l1, l2_0);
+        } else {
+            f_rho_odd_steps(tb, e, 0, l1, l2_0);
+        }
+    }
+}
+
+// One in-place move of a table row by 16 entries: every lane reads before any writes.
+__device__ __forceinline__ void move_row(ffpair* row, int from, int to)
+{
+    const ffpair x = row[from];
+    __syncwarp();
+    row[to] = x;
+}
+
+// The tables of the chunk at t0.  The G entries are formed anew each chunk.
+// The F entries of the first chunk come from init_f_tables; after that 64 of
+// the 96 entries per sweep are the previous chunk's moved by 32 in e (16 per
+// parity: forward down, backward up), and only 32 are new.
 template <bool N22>
 __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1, int l2_0, int lane)
 {
@@ -221,36 +287,19 @@ __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1,
         }
         tb.g[lane] = ffpair{a, b};
     }
-    const int d0 = l2_0 - l1;
-#pragma unroll
-    for (int q = 0; q < (2 * kFEnt + 31) / 32; ++q) {
-        const int e = lane + 32 * q;
-        if (e >= 2 * kFEnt) break;
-        const float u = (float)(t0 + e);             // forward, u = t0 + e
-        const int v = e - t0 - (kChunk - 1);          // backward, v = e - t0 - 31
-        const bool vok = 2 * l2_0 + v > 0;
-        const float fv = (float)v;
-        if (N22) {
-            ff a, b;
-            sqrt_ratio(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
-                       two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u), a, b);
-            tb.fF[e & 1][e >> 1] = ffpair{a, b};
-            if (vok) {
-                sqrt_ratio(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
-                           two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv), a, b);
-            } else {
-                a = b = zero;
-            }
-            tb.fB[e & 1][e >> 1] = ffpair{a, b};
-        } else if (e & 1) {  // odd forward step: fF[1]
-            tb.fF[1][e >> 1].rho = sqrt_ratio_rho(two_prod((float)(2 * d0) + u, (float)(2 * l2_0 + 1) + u),
-                                                  two_prod((float)(2 * d0 + 1) + u, (float)(2 * l2_0 + 2) + u));
-        } else {             // odd backward step: fB[0]
-            tb.fB[0][e >> 1].rho =
-                vok ? sqrt_ratio_rho(two_prod((float)(2 * l2_0 + 1) + fv, (float)(2 * l1 + 2 * l2_0 + 2) + fv),
-                                     two_prod((float)(2 * l2_0) + fv, (float)(2 * l1 + 2 * l2_0 + 1) + fv))
-                    : zero;
-        }
+    if (t0 == 0) return;
+    static_assert(2 * kFEnt == 96 && kChunk == 32, "the move below assumes 96 F entries and 32-step chunks");
+    if (N22) {
+        move_row(tb.fF[0], lane + 16, lane);
+        move_row(tb.fF[1], lane + 16, lane);
+        move_row(tb.fB[0], lane, lane + 16);
+        move_row(tb.fB[1], lane, lane + 16);
+        f_fwd(tb, 64 + lane, t0, l1, l2_0);
+        f_bwd(tb, lane, t0, l1, l2_0);
+    } else {
+        move_row(tb.fF[1], lane + 16, lane);
+        move_row(tb.fB[0], lane, lane + 16);
+        f_rho_odd_steps(tb, (lane & 1) ? 64 + lane : lane, t0, l1, l2_0);
     }
 }
 
@@ -331,6 +380,7 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
         }
     }
     fetch_commit();
+    init_f_tables<N22>(tb, l1, l2_0, lane);
     for (int t0 = 0; t0 < T; t0 += kChunk) {
         int eF[NWIN], eB[NWIN];
         fetch_wait_all();
