@@ -32,10 +32,14 @@ struct ps_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     char err[512] = {0};
-    // warp task list for the current (lmin, lmax)
+    // warp task lists for the current (lmin, lmax): rows for the plain kernel,
+    // tiles for the chosen kernel
     int2* d_tasks = nullptr;
     size_t tasks_cap = 0;
     int ntasks = 0, task_lmin = -1, task_lmax = -1;
+    int2* d_tiles = nullptr;
+    size_t tiles_cap = 0;
+    int ntiles = 0, tile_lmin = -1, tile_lmax = -1;
     // padded windows, raw inputs, spectra, outputs (element counts)
     double* d_win = nullptr;
     size_t win_cap = 0;
@@ -134,29 +138,81 @@ static int ensure_pinned(ps_ctx* c, size_t need)
     return PS_OK;
 }
 
+// The plain kernel's warp tasks: rows by decreasing l1 (longest families
+// first), 32 consecutive l2 per task from l2 = l1.
+static void row_task_list(int lmin, int lmax, std::vector<int2>& t)
+{
+    t.clear();
+    t.reserve((size_t)(lmax - lmin + 1) * ((lmax - lmin) / 32 + 1));
+    for (int l1 = lmax; l1 >= lmin; --l1)
+        for (int l2 = l1; l2 <= lmax; l2 += 32) t.push_back(make_int2(l1, l2));
+}
+
+// The chosen kernel's warp tasks, in tiles of kTileRows (one block).  Rows and
+// columns are counted from o = lmax + 1 - 32 nb (nb = ceil(n / 32)), so that
+// the last 32-column block ends at lmax: tile (g, b) holds rows o + 4g ..
+// o + 4g + 3 (l1 = -1 below lmin) over the 32 columns from l2_0 = o + 32 b,
+// for b from the block that holds row o + 4g to the last.  Every row then has
+// the same warp tasks as 32-column steps from l1 would give, and the only idle
+// lanes are those left of the diagonal.  Row groups from the top (longest
+// families first).  The kernel writes each tile's row halves as runs of four
+// doubles.
+static void tile_task_list(int lmin, int lmax, std::vector<int2>& t)
+{
+    static_assert(ps::kTileRows == 4 && 32 % ps::kTileRows == 0, "tiles of four rows inside one 32-column block");
+    const int n = lmax - lmin + 1, NB = (n + 31) / 32, o = lmax + 1 - 32 * NB, glo = (lmin - o) / 4;
+    t.clear();
+    t.reserve((size_t)32 * NB * NB);
+    for (int g = 8 * NB - 1; g >= glo; --g)
+        for (int b = g / 8; b < NB; ++b)
+            for (int q = 0; q < 4; ++q) {
+                const int l1 = o + 4 * g + q;
+                t.push_back(make_int2(l1 >= lmin ? l1 : -1, o + 32 * b));
+            }
+}
+
+static int upload_tasks(ps_ctx* c, const std::vector<int2>& t, int2** d, size_t* cap)
+{
+    if (t.size() > *cap) {
+        if (*d) cudaFree(*d);
+        *d = nullptr;
+        *cap = 0;
+        cudaError_t e = cudaMalloc((void**)d, t.size() * sizeof(int2));
+        if (e != cudaSuccess) {
+            *d = nullptr;
+            cudaGetLastError();
+            return set_err(c, PS_ERR_OOM, "cudaMalloc of the task list failed: %s", cudaGetErrorString(e));
+        }
+        *cap = t.size();
+    }
+    PS_CUDA(c, cudaMemcpyAsync(*d, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PS_OK;
+}
+
 static int ensure_tasks(ps_ctx* c, int lmin, int lmax)
 {
     if (c->task_lmin == lmin && c->task_lmax == lmax && c->d_tasks) return PS_OK;
     std::vector<int2> t;
-    t.reserve((size_t)(lmax - lmin + 1) * ((lmax - lmin) / 32 + 1));
-    for (int l1 = lmax; l1 >= lmin; --l1)  // heaviest rows (longest families) first
-        for (int l2 = l1; l2 <= lmax; l2 += 32) t.push_back(make_int2(l1, l2));
-    if (t.size() > c->tasks_cap) {
-        if (c->d_tasks) cudaFree(c->d_tasks);
-        c->d_tasks = nullptr;
-        c->tasks_cap = 0;
-        cudaError_t e = cudaMalloc((void**)&c->d_tasks, t.size() * sizeof(int2));
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            return set_err(c, PS_ERR_OOM, "cudaMalloc of the task list failed: %s", cudaGetErrorString(e));
-        }
-        c->tasks_cap = t.size();
-    }
-    PS_CUDA(c, cudaMemcpyAsync(c->d_tasks, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
-    PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    row_task_list(lmin, lmax, t);
+    c->task_lmin = c->task_lmax = -1;
+    if (int st = upload_tasks(c, t, &c->d_tasks, &c->tasks_cap)) return st;
     c->ntasks = (int)t.size();
     c->task_lmin = lmin;
     c->task_lmax = lmax;
+    return PS_OK;
+}
+
+static int ensure_tiles(ps_ctx* c, int lmin, int lmax)
+{
+    if (c->tile_lmin == lmin && c->tile_lmax == lmax && c->d_tiles) return PS_OK;
+    std::vector<int2> t;
+    tile_task_list(lmin, lmax, t);
+    c->tile_lmin = c->tile_lmax = -1;
+    if (int st = upload_tasks(c, t, &c->d_tiles, &c->tiles_cap)) return st;
+    c->ntiles = (int)t.size();
+    c->tile_lmin = lmin;
+    c->tile_lmax = lmax;
     return PS_OK;
 }
 
@@ -217,10 +273,11 @@ void cov_window_spec(int kind, int k, int* product, int* parity)
 // Launch the coupling kernel with event timing on the context stream.
 static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode)
 {
-    int st = ensure_tasks(c, p.lmin, p.lmax);
+    const bool chosen = mode == PS_MODE_CHOSEN;
+    int st = chosen ? ensure_tiles(c, p.lmin, p.lmax) : ensure_tasks(c, p.lmin, p.lmax);
     if (st) return st;
-    p.tasks = c->d_tasks;
-    p.ntasks = c->ntasks;
+    p.tasks = chosen ? c->d_tiles : c->d_tasks;
+    p.ntasks = chosen ? c->ntiles : c->ntasks;
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
     if (mode == PS_MODE_CHOSEN)
         PS_CUDA(c, ps::launch_chosen(p, c->stream));
@@ -402,6 +459,7 @@ void ps_destroy(ps_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     cudaFree(c->d_tasks);
+    cudaFree(c->d_tiles);
     cudaFree(c->d_win);
     cudaFree(c->d_raw);
     cudaFree(c->d_spec);
@@ -856,8 +914,8 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     });
     std::vector<int4> sorted(items.size());
     for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
-    // the warp task lists of every distinct (lmin, lmax), for the launch form
-    std::vector<int2> tasks;
+    // the chosen kernel's tiled task lists of every distinct (lmin, lmax), for the launch form
+    std::vector<int2> tasks, one;
     std::vector<std::pair<long long, std::pair<size_t, int>>> task_of;  // (lmin, lmax) key -> (offset, count)
     for (int i = 0; i < nprob; ++i) {
         const long long key = ((long long)probs[i].lmin << 32) | (unsigned)probs[i].lmax;
@@ -865,8 +923,8 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
         for (const auto& t : task_of) have = have || t.first == key;
         if (have) continue;
         const size_t off = tasks.size();
-        for (int l1 = probs[i].lmax; l1 >= probs[i].lmin; --l1)  // heaviest rows first
-            for (int l2 = l1; l2 <= probs[i].lmax; l2 += 32) tasks.push_back(make_int2(l1, l2));
+        tile_task_list(probs[i].lmin, probs[i].lmax, one);
+        tasks.insert(tasks.end(), one.begin(), one.end());
         task_of.push_back({key, {off, (int)(tasks.size() - off)}});
     }
     if ((st = dev_upload(c, &b.d_groups, groups)) || (st = dev_upload(c, &b.d_items, sorted)) ||

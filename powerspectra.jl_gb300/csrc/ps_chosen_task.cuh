@@ -339,13 +339,16 @@ __device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int
     tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
 }
 
+// The Xi of pair (l1, l2_0 + lane) into Xi[]; returns whether the lane holds a
+// pair to write (l1 <= l2 <= lmax).  Lanes outside clamp l2 into [l1, lmax] and
+// compute values nobody writes.
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
-__device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
-                                            float* sB, int2* raw, CoefTab& tb, const int lane)
+__device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1, const int l2_0, float* sF,
+                                          float* sB, int2* raw, CoefTab& tb, const int lane, double* Xi)
 {
     const int l2raw = l2_0 + lane;
-    const bool active = l2raw <= p.lmax;
-    const int l2 = active ? l2raw : p.lmax;
+    const bool active = l2raw >= l1 && l2raw <= p.lmax;
+    const int l2 = l2raw > p.lmax ? p.lmax : (l2raw < l1 ? l1 : l2raw);
     const int d = l2 - l1;
     const int jmin = d, jmax = l1 + l2;
     const int T = l1;
@@ -353,11 +356,9 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     const int jmin0 = l2_0 - l1, jmax0 = l2_0 + l1;  // lane 0's ends: lane i reads slot i + step
     const WinCfg<NWIN> wc = win_cfg<NWIN, SPEC>(p);
 
-    double Xi[kMaxWin];
     if (T == 0) {
         xi_single_term(p, l2, Xi);
-        if (active) write_pair(p, l1, l2, Xi);
-        return;
+        return active;
     }
 
     Sweep F, B;
@@ -501,7 +502,17 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
                 Xi[k] = fma(lam0 * lam2, BW[k], FW[k]) * inv02;
         }
     }
-    if (active) write_pair(p, l1, l2, Xi);
+    return active;
+}
+
+// One warp task with its own writes (the persistent batch kernel, whose items
+// hold l2_0 >= l1).
+template <int NWIN, bool N00, bool N22, uint32_t SPEC>
+__device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l1, const int l2_0, float* sF,
+                                            float* sB, int2* raw, CoefTab& tb, const int lane)
+{
+    double Xi[kMaxWin];
+    if (chosen_xi<NWIN, N00, N22, SPEC>(p, l1, l2_0, sF, sB, raw, tb, lane, Xi)) write_pair(p, l1, l2_0 + lane, Xi);
 }
 
 // n copies of one slot spec w (4 bits) in consecutive slots
@@ -520,15 +531,23 @@ constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 <
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
 {
-    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    __shared__ __align__(16) float sW[kWarpsPerBlock][2][NWIN][kSlots];
     __shared__ int2 sR[kWarpsPerBlock][2][NWIN][kSlots];
     __shared__ CoefTab sT[kWarpsPerBlock];
-    const int warp = threadIdx.x >> 5;
-    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-    if (gw >= p.ntasks) return;  // warp-uniform
-    const int2 task = p.tasks[gw];
-    chosen_task<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0], &sR[warp][0][0][0],
-                                      sT[warp], threadIdx.x & 31);
+    __shared__ TileRows rows;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // the task list is tiled: kTileRows tasks per block, rows outside [lmin, lmax] as l1 = -1
+    const int gw = (int)(blockIdx.x * (unsigned)kWarpsPerBlock) + warp;
+    const int2 task = gw < p.ntasks ? p.tasks[gw] : make_int2(-1, 0);
+    double Xi[kMaxWin];
+    bool active = false;
+    if (task.x >= 0)  // warp-uniform
+        active = chosen_xi<NWIN, N00, N22, SPEC>(p, task.x, task.y, &sW[warp][0][0][0], &sW[warp][1][0][0],
+                                                 &sR[warp][0][0][0], sT[warp], lane, Xi);
+    // each warp's slice staging area (2 NWIN kSlots floats) holds its [NWIN][32] row-half doubles
+    static_assert(2 * NWIN * kSlots >= 2 * NWIN * 32, "row-half staging fits the slice area");
+    write_tile<NWIN>(p, task.x, task.y, active, Xi, reinterpret_cast<double*>(&sW[0][0][0][0]), NWIN * kSlots, rows,
+                     warp, lane);
 }
 
 // families a compile-time window set needs

@@ -21,6 +21,7 @@ namespace ps {
 
 constexpr int kMaxWin = 8;       // windows (slots) per coupling launch
 constexpr int kWarpsPerBlock = 4;
+constexpr int kTileRows = 4;  // rows per tile of the chosen kernel's task list (one per warp)
 constexpr double kInv4Pi = 0.079577471545947667884;  // 1 / (4 pi)
 
 // Family product a window is contracted with.

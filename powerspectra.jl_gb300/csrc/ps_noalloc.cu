@@ -23,6 +23,7 @@ namespace {
 constexpr int kNoAllocMaxLmax = 4095;  // largest lmax the fixed scratch serves
 constexpr int kNoAllocMaxWlen = 2 * kNoAllocMaxLmax + 2;
 constexpr int kNoAllocMaxTasks = (kNoAllocMaxLmax + 1) * (kNoAllocMaxLmax + 2) / 64 + kNoAllocMaxLmax + 1;
+// (the tiled list at lmax 4095, lmin 0 holds 264192 tasks; fewer for any smaller range)
 
 // windows: 4 x wlen doubles, split copies: 4 x wlen int2, tasks: int2 each
 constexpr size_t kWinBytes = 4ull * kNoAllocMaxWlen * sizeof(double);
@@ -36,22 +37,30 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 static void* g_scratch_addr[kMaxDevices];
 
-// Sum over m = 1..M of ceil(m / 32): the number of warp tasks in rows whose
-// upper triangle holds 1..M pairs.
-__host__ __device__ inline long long tasks_upto(long long M)
+// The chosen kernel's tiled task list (the context path builds the same on
+// the host): with nb = ceil(n / 32) and o = lmax + 1 - 32 nb, tile (g, b)
+// holds rows o + 4g .. o + 4g + 3 (l1 = -1 below lmin) over the 32 columns
+// from o + 32 b, b = g / 8 .. nb - 1, for row groups g from 8 nb - 1 down to
+// (lmin - o) / 4.  tiles_below(m, nb) counts the tiles of row groups 0 .. m - 1:
+// the sum of nb - g / 8 over g < m.
+__host__ __device__ inline long long tiles_below(long long m, long long nb)
 {
-    long long q = M / 32, r = M % 32;
-    return 32 * q * (q + 1) / 2 + (q + 1) * r;
+    const long long q = m / 8, r = m % 8;
+    return m * nb - (4 * q * (q - 1) + r * q);
 }
 
-// Row l1 (one thread each) writes its tasks (l1, l2_0) in the order the context
-// path uses: rows by decreasing l1, 32 consecutive l2 per task.
-__global__ void k_fill_tasks(int2* __restrict__ tasks, int lmin, int lmax)
+// One thread per row group writes its tiles' tasks.
+__global__ void k_fill_tiles(int2* __restrict__ tasks, int lmin, int lmax)
 {
-    for (int l1 = lmin + blockIdx.x * blockDim.x + threadIdx.x; l1 <= lmax; l1 += gridDim.x * blockDim.x) {
-        long long off = tasks_upto(lmax - l1);
-        int q = 0;
-        for (int l2 = l1; l2 <= lmax; l2 += 32, ++q) tasks[off + q] = make_int2(l1, l2);
+    const int n = lmax - lmin + 1, NB = (n + 31) / 32, o = lmax + 1 - 32 * NB, glo = (lmin - o) / 4;
+    const long long top = tiles_below(8LL * NB, NB);
+    for (int g = glo + blockIdx.x * blockDim.x + threadIdx.x; g < 8 * NB; g += gridDim.x * blockDim.x) {
+        long long t = top - tiles_below(g + 1, NB);  // groups above g come first
+        for (int b = g / 8; b < NB; ++b, ++t)
+            for (int q = 0; q < 4; ++q) {
+                const int l1 = o + 4 * g + q;
+                tasks[4 * t + q] = make_int2(l1 >= lmin ? l1 : -1, o + 32 * b);
+            }
     }
 }
 
@@ -113,11 +122,14 @@ extern "C" int ps_mcm_multi_device_noalloc(unsigned cases, const double* const d
         ++K;
     }
     p.nwin = K;
-    const int rows = lmax - lmin + 1;
-    k_fill_tasks<<<(rows + 255) / 256, 256, 0, s>>>(tasks, lmin, lmax);
+    const int rows = lmax - lmin + 1, nb = (rows + 31) / 32, glo = (lmin - (lmax + 1 - 32 * nb)) / 4;
+    const int groups = 8 * nb - glo;
+    const long long ntasks = 4 * (tiles_below(8LL * nb, nb) - tiles_below(glo, nb));
+    if (ntasks > kNoAllocMaxTasks) return PS_ERR_ARG;  // cannot happen for lmax <= kNoAllocMaxLmax
+    k_fill_tiles<<<(groups + 255) / 256, 256, 0, s>>>(tasks, lmin, lmax);
     if (cudaGetLastError() != cudaSuccess) return PS_ERR_CUDA;
     p.tasks = tasks;
-    p.ntasks = (int)tasks_upto(rows);
+    p.ntasks = (int)ntasks;
     if (ps::launch_chosen(p, s) != cudaSuccess) return PS_ERR_CUDA;
     return PS_OK;
 }
