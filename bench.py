@@ -320,7 +320,7 @@ def run_ours(args):
     achieved = fl / (kms * 1e-3)
     # DRAM bytes per launch from one ncu capture of this kernel at this size
     # (profiles/coupling_chosen_all_spins_3071_dram.md); bench.py cannot run ncu itself
-    traffic = 2.500e8 if (wl["name"] == "all_spins_3071" and mode == "chosen") else None
+    traffic = 2.468e8 if (wl["name"] == "all_spins_3071" and mode == "chosen") else None
     roofline = {"bound": "fp64_fma_pipe" if mode == "plain" else "fp32_fma_pipe",
                 "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
                 "traffic": traffic,
