@@ -108,10 +108,23 @@ __device__ __forceinline__ int wpar(const CouplingParams& p, int k)
 
 // Per-direction recurrence state (float-float values; the 22 family is left
 // unnormalised between steps, see ff_add_raw).
+// n copies of one slot spec w (4 bits) in consecutive slots
+__host__ __device__ constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
+constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
+constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
+// the window sets of the mode-coupling and covariance entry points
+constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
+constexpr uint32_t S_PPMM = WPP | (WMM << 4);
+constexpr uint32_t S_PPMM2 = S_PPMM | (S_PPMM << 8);  // (++, --) of two windows
+constexpr uint32_t S_PPMM4 = S_PPMM2 | (S_PPMM2 << 16);  // (++, --) of four windows
+constexpr uint32_t S_MCM8 = S_MCM4 | (S_MCM4 << 16);     // TT, TE, ++, -- of two windows
+static_assert(((S_PPMM2 >> 8) & 0xffu) == S_PPMM && ((S_PPMM2 >> 4) & 0xfu) == WMM, "slot layout of S_PPMM2");
+constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
+
 struct Sweep {
     ff f2, f2o;   // 22 family at the current point and at the previous one
     ff f0;        // 00 family at the last even point
-    float w;      // 2j + 1 at the current point
+    float w;      // ws (2j + 1) at the current point, ws = 4 or 1 (exact in FP32)
 };
 
 // The window configuration one task uses, read from the parameters once: the
@@ -303,12 +316,19 @@ __device__ __forceinline__ void build_tables(CoefTab& tb, int t0, int T, int l1,
     }
 }
 
-// One table-driven step: f(next) = -(c (2j+1) f(cur) r + rho f(prev)), c = 4.
-template <bool N00, bool N22, bool ODD_STEP>
+// One table-driven step: f(next) = -(4 (2j+1) f(cur) r + rho f(prev)).  With
+// WS4 the sweep carries w = 4 (2j+1) and the step saves the multiply by 4.
+// Both forms give the same bits (4 (2j+1) is exact); which one a slot list
+// uses is a measured choice: the compiler schedules the all-spins list
+// (S_MCM4) about 1 % faster without it and every other list 1-3 % faster
+// with it.
+template <int NWIN, uint32_t SPEC>
+constexpr bool weight_times4() { return !(NWIN == 4 && SPEC == S_MCM4); }
+template <bool N00, bool N22, bool ODD_STEP, bool WS4>
 __device__ __forceinline__ void tab_step(Sweep& s, ff rho, ff r, float dw)
 {
     if (N22) {
-        ff u = ff_mul_raw(ff_mulf_raw(s.f2, 4.0f * s.w), r);
+        ff u = ff_mul_raw(ff_mulf_raw(s.f2, WS4 ? s.w : 4.0f * s.w), r);
         ff v = ff_mul_raw(rho, s.f2o);
         ff nf = ff_neg(ff_add_raw(u, v));
         s.f2o = s.f2;
@@ -318,17 +338,17 @@ __device__ __forceinline__ void tab_step(Sweep& s, ff rho, ff r, float dw)
     s.w += dw;
 }
 
-template <bool N00, bool N22, bool ODD_STEP>
+template <bool N00, bool N22, bool ODD_STEP, bool WS4>
 __device__ __forceinline__ void tab_fwd(Sweep& s, const CoefTab& tb, int st, int lane)
 {
     const int e = lane + (st >> 1);  // (u - t0) / 2; u - t0 = 2 lane + st has the parity of the step
     const ffpair g = tb.g[st], f = tb.fF[ODD_STEP][e];
     ff rho = ff_mul_raw(g.rho, f.rho);
     ff r = ff_mul_raw(g.r, f.r);
-    tab_step<N00, N22, ODD_STEP>(s, rho, r, 2.0f);
+    tab_step<N00, N22, ODD_STEP, WS4>(s, rho, r, WS4 ? 8.0f : 2.0f);
 }
 
-template <bool N00, bool N22, bool ODD_STEP>
+template <bool N00, bool N22, bool ODD_STEP, bool WS4>
 __device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int lane)
 {
     // v - (-t0 - 31) = 2 lane - st + 31: odd for even steps, half of it lane + 15 - st / 2
@@ -336,7 +356,7 @@ __device__ __forceinline__ void tab_bwd(Sweep& s, const CoefTab& tb, int st, int
     const ffpair g = tb.g[st], f = tb.fB[!ODD_STEP][e];
     ff rho = ff_mul_raw(g.rho, f.rho);
     ff r = ff_mul_raw(g.r, f.r);
-    tab_step<N00, N22, ODD_STEP>(s, rho, r, -2.0f);
+    tab_step<N00, N22, ODD_STEP, WS4>(s, rho, r, WS4 ? -8.0f : -2.0f);
 }
 
 // The Xi of pair (l1, l2_0 + lane) into Xi[]; returns whether the lane holds a
@@ -363,9 +383,11 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
 
     Sweep F, B;
     F.f2 = ff_make(1.0f); F.f2o = ff_make(0.0f); F.f0 = ff_make(1.0f);
-    F.w = (float)(2 * jmin + 1);
+    constexpr bool WS4 = weight_times4<NWIN, SPEC>();
+    constexpr int ws = WS4 ? 4 : 1;  // the norm sums below carry this factor
+    F.w = (float)(ws * (2 * jmin + 1));
     B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.f0 = ff_make(1.0f);
-    B.w = (float)(2 * jmax + 1);
+    B.w = (float)(ws * (2 * jmax + 1));
     double FW[NWIN], BW[NWIN];
 #pragma unroll
     for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
@@ -416,18 +438,18 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
         for (; s + 1 < steps; s += 2) {
             sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, false>(F, tb, s, lane);
-            tab_bwd<N00, N22, false>(B, tb, s, lane);
+            tab_fwd<N00, N22, false, WS4>(F, tb, s, lane);
+            tab_bwd<N00, N22, false, WS4>(B, tb, s, lane);
             sweep_acc<NWIN, N00, N22, SPEC, false>(wc, F, sF, lane + s + 1, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, false>(wc, B, sB, lane - s - 1 + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, true>(F, tb, s + 1, lane);
-            tab_bwd<N00, N22, true>(B, tb, s + 1, lane);
+            tab_fwd<N00, N22, true, WS4>(F, tb, s + 1, lane);
+            tab_bwd<N00, N22, true, WS4>(B, tb, s + 1, lane);
         }
         if (s < steps) {  // one even step left (T odd, last chunk)
             sweep_acc<NWIN, N00, N22, SPEC, true>(wc, F, sF, lane + s, cF, n0F, n2F);
             sweep_acc<NWIN, N00, N22, SPEC, true>(wc, B, sB, lane - s + kChunk - 1, cB, n0B, n2B);
-            tab_fwd<N00, N22, false>(F, tb, s, lane);
-            tab_bwd<N00, N22, false>(B, tb, s, lane);
+            tab_fwd<N00, N22, false, WS4>(F, tb, s, lane);
+            tab_bwd<N00, N22, false, WS4>(B, tb, s, lane);
         }
         // ---- FP64 flush of the chunk sums ----
 #pragma unroll
@@ -435,10 +457,17 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
             FW[k] = fma((double)cF[k], pow2d(eF[k]), FW[k]);
             BW[k] = fma((double)cB[k], pow2d(eB[k]), BW[k]);
         }
-        FN0 += (double)n0F;
-        FN2 += (double)n2F;
-        BN0 += (double)n0B;
-        BN2 += (double)n2B;
+        if (WS4) {
+            FN0 = fma((double)n0F, 0.25, FN0);
+            FN2 = fma((double)n2F, 0.25, FN2);
+            BN0 = fma((double)n0B, 0.25, BN0);
+            BN2 = fma((double)n2B, 0.25, BN2);
+        } else {
+            FN0 += (double)n0F;
+            FN2 += (double)n2F;
+            BN0 += (double)n0B;
+            BN2 += (double)n2B;
+        }
         __syncwarp();
     }
 
@@ -472,7 +501,7 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
         ff P1 = ff_mul_raw(two_prod(fT + 1.0f, (float)(2 * d + 1) + fT), two_prod((float)(2 * l1) - fT, (float)(2 * l2 + 2) + fT));
         ff rho, r;
         sqrt_ratio(P0, P1, rho, r);
-        if (N22) gm1 = ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mul_raw(F.f2, ff_make(4.0f * F.w)), r), ff_mul_raw(rho, F.f2o))));
+        if (N22) gm1 = ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mul_raw(F.f2, ff_make(WS4 ? F.w : 4.0f * F.w)), r), ff_mul_raw(rho, F.f2o))));
         g0s = (N00 && !evenT) ? ff_to_double(ff_neg(ff_mul(rho, F.f0))) : ff_to_double(F.f0);
     }
 
@@ -515,18 +544,6 @@ __device__ __forceinline__ void chosen_task(const CouplingParams& p, const int l
     if (chosen_xi<NWIN, N00, N22, SPEC>(p, l1, l2_0, sF, sB, raw, tb, lane, Xi)) write_pair(p, l1, l2_0 + lane, Xi);
 }
 
-// n copies of one slot spec w (4 bits) in consecutive slots
-__host__ __device__ constexpr uint32_t rep(uint32_t w, int n) { return n == 0 ? 0u : (w | (rep(w, n - 1) << 4)); }
-constexpr uint32_t W00 = wspec(PROD_00_00, PAR_ALL), W02 = wspec(PROD_00_22, PAR_EVEN);
-constexpr uint32_t WPP = wspec(PROD_22_22, PAR_EVEN), WMM = wspec(PROD_22_22, PAR_ODD);
-// the window sets of the mode-coupling and covariance entry points
-constexpr uint32_t S_MCM4 = W00 | (W02 << 4) | (WPP << 8) | (WMM << 12);
-constexpr uint32_t S_PPMM = WPP | (WMM << 4);
-constexpr uint32_t S_PPMM2 = S_PPMM | (S_PPMM << 8);  // (++, --) of two windows
-constexpr uint32_t S_PPMM4 = S_PPMM2 | (S_PPMM2 << 16);  // (++, --) of four windows
-constexpr uint32_t S_MCM8 = S_MCM4 | (S_MCM4 << 16);     // TT, TE, ++, -- of two windows
-static_assert(((S_PPMM2 >> 8) & 0xffu) == S_PPMM && ((S_PPMM2 >> 4) & 0xfu) == WMM, "slot layout of S_PPMM2");
-constexpr uint32_t S_TETE = W02 | (W00 << 4) | (W02 << 8) | (W02 << 12) | (W02 << 16);
 
 template <int NWIN, bool N00, bool N22, uint32_t SPEC>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 4) k_coupling_chosen(const CouplingParams p)
