@@ -25,7 +25,12 @@
 //    are added into FP64 totals with the factor 2^E;
 //  * FP64 is kept where stability and range need it: the last forward point,
 //    the least-squares match of the two sweeps, the normalisation, the sign and
-//    the totals.
+//    the totals;
+//  * the launch-per-call kernel (k_coupling_chosen) takes a tiled task list:
+//    the four warps of a block hold four consecutive rows over one 32-column
+//    block, and write the row halves of their pairs together as 32-byte runs
+//    (write_tile in ps_epilogue.cuh).  The persistent batch kernel writes per
+//    warp (chosen_task).
 #pragma once
 
 #include "ps_internal.cuh"

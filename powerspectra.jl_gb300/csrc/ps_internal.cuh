@@ -5,8 +5,10 @@
 //               (2 l3 + 1) * W_k[l3] for l3 < nW and 0 beyond, so every family
 //               read (l3 <= l1 + l2 <= 2 lmax) stays in bounds without a branch.
 //   * tasks:    int2 (l1, l2_0) per warp, 32 consecutive l2 of one l1 row,
-//               sorted by decreasing l1 (the family length is 2 l1 + 1) so
-//               the heaviest warps start first.
+//               heaviest rows first (the family length is 2 l1 + 1).  The
+//               plain kernel's list steps from l2 = l1 row by row; the chosen
+//               kernel's list is tiled, kTileRows consecutive rows per block
+//               over one 32-column block (see tile_task_list in ps_api.cu).
 //   * outputs:  column-major (Julia) matrices, element (l1, l2) at
 //               (l1 - lmin) + (l2 - lmin) * ld.
 #pragma once
