@@ -66,10 +66,14 @@ __global__ void __launch_bounds__(128) k_quickpol_fp64(const double* __restrict_
                                                        int bu, int nu1, int nu2, int s1, int s2, double* Xi,
                                                        long long ldx)
 {
-    const int lpp = 2 + blockIdx.y;  // row l''
-    const int lo = max(2, lpp - bl), hi = min(lmax, lpp + bu);
-    const int l = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (lpp > lmax || l > hi) return;
+    // one thread per band element (l'', l), numbered row by row from the top
+    // (the longest families first) so that every warp is full
+    const int width = bl + bu + 1;
+    const long long pidx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pidx >= (long long)(lmax - 1) * width) return;
+    const int lpp = lmax - (int)(pidx / width);  // row l''
+    const int l = lpp - bl + (int)(pidx % width);
+    if (l < 2 || l > lmax) return;
     const int l1 = l, l2 = lpp, jmax = l1 + l2;
     Fam F[2];
     F[0].m1 = -s1; F[0].m2 = -nu1; F[0].m3 = s1 + nu1;
@@ -156,9 +160,12 @@ cudaError_t launch_quickpol(const double* W, long long nW, int lmax, int bl, int
                             double* Xi, long long ldx, cudaStream_t s)
 {
     if (lmax < 2) return cudaSuccess;
+    // a band wider than the grid covers the same elements as one of width lmax
+    bl = bl < lmax ? bl : lmax;
+    bu = bu < lmax ? bu : lmax;
     const int width = bl + bu + 1;
-    dim3 grid((width + 127) / 128, lmax - 1);
-    k_quickpol_fp64<<<grid, 128, 0, s>>>(W, nW, lmax, bl, bu, nu1, nu2, s1, s2, Xi, ldx);
+    const long long total = (long long)(lmax - 1) * width;  // < 2^31 for lmax <= 16383
+    k_quickpol_fp64<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(W, nW, lmax, bl, bu, nu1, nu2, s1, s2, Xi, ldx);
     return cudaGetLastError();
 }
 

@@ -3,7 +3,8 @@
 // float-float, FP64 only where the FP64 kernel (ps_quickpol.cu) needs range or
 // one-off precision.
 //
-// Same mapping and algorithm as k_quickpol_fp64 (one thread per (l'', l); both
+// Same mapping and algorithm as k_quickpol_fp64 (one thread per band element (l'', l),
+// rows from the top; both
 // families forward from their own jmin and backward from jmax, matched at one
 // common point; here the two sweeps run interleaved in one loop), with:
 //   * P(j) = A(j)^2 = (j-|d|)(j+|d|)(s-j)(s+j)(j-|m3|)(j+|m3|) formed from its
@@ -124,14 +125,18 @@ __global__ void __launch_bounds__(1024) k_quickpol_stage(const double* __restric
     if (threadIdx.x == 0) *E_out = E;
 }
 
-__global__ void __launch_bounds__(128) k_quickpol_ff(const float* __restrict__ Wf, const int* __restrict__ E_in,
+__global__ void __launch_bounds__(128, 5) k_quickpol_ff(const float* __restrict__ Wf, const int* __restrict__ E_in,
                                                      long long nW, int lmax, int bl, int bu, int nu1, int nu2, int s1,
                                                      int s2, double* Xi, long long ldx)
 {
-    const int lpp = 2 + blockIdx.y;  // row l''
-    const int lo = max(2, lpp - bl), hi = min(lmax, lpp + bu);
-    const int l = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (lpp > lmax || l > hi) return;
+    // one thread per band element (l'', l), numbered row by row from the top
+    // (the longest families first) so that every warp is full
+    const int width = bl + bu + 1;
+    const long long pidx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pidx >= (long long)(lmax - 1) * width) return;
+    const int lpp = lmax - (int)(pidx / width);  // row l''
+    const int l = lpp - bl + (int)(pidx % width);
+    if (l < 2 || l > lmax) return;
     const int l1 = l, l2 = lpp, jmax = l1 + l2;
     const int ad = abs(l1 - l2), s = l1 + l2 + 1;
     const float adf = (float)ad, spf = (float)s;  // |d| and s as floats
@@ -252,9 +257,12 @@ cudaError_t launch_quickpol_ff(const double* W, long long nW, int lmax, int bl, 
     k_quickpol_stage<<<1, 1024, 0, st>>>(W, (int)nW, wf, e);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
+    // a band wider than the grid covers the same elements as one of width lmax
+    bl = bl < lmax ? bl : lmax;
+    bu = bu < lmax ? bu : lmax;
     const int width = bl + bu + 1;
-    dim3 grid((width + 127) / 128, lmax - 1);
-    k_quickpol_ff<<<grid, 128, 0, st>>>(wf, e, nW, lmax, bl, bu, nu1, nu2, s1, s2, Xi, ldx);
+    const long long total = (long long)(lmax - 1) * width;  // < 2^31 for lmax <= 16383
+    k_quickpol_ff<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(wf, e, nW, lmax, bl, bu, nu1, nu2, s1, s2, Xi, ldx);
     return cudaGetLastError();
 }
 

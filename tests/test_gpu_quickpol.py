@@ -95,6 +95,20 @@ def test_quickpol_chosen_large_l(ctx):
     assert np.max(np.abs(C - P)[mask] / A[mask]) < 1e-6
 
 
+@pytest.mark.parametrize("mode", ["plain", "chosen"])
+def test_quickpol_band_wider_than_grid(ctx, mode):
+    """Bandwidths beyond lmax cover the whole grid: the same matrix, bit for bit, as bl = bu = lmax."""
+    lmax = 70
+    rng = np.random.default_rng(9)
+    W = rng.random(2 * lmax + 1) * np.exp(-np.arange(2 * lmax + 1) / 30.0)
+    A = ctx.quickpol_xi(0, 0, 2, 2, W, lmax, lmax, lmax, mode=mode)
+    B = ctx.quickpol_xi(0, 0, 2, 2, W, lmax, 10 ** 6, 10 ** 6, mode=mode)
+    assert np.array_equal(A, B)
+    R = o.quickpol_xi(0, 0, 2, 2, W, lmax, lmax, lmax)
+    S = o.quickpol_xi(0, 0, 2, 2, W, lmax, lmax, lmax, absolute=True)
+    assert np.max(np.abs(A - R)[S > 0] / S[S > 0]) < (1e-10 if mode == "plain" else 1e-6)
+
+
 def test_quickpol_mode_error(ctx):
     import powerspectra_gpu as pg
     with pytest.raises(pg.PowerSpectraArgumentError):
