@@ -634,7 +634,8 @@ def run_quickpol(args):
     of the reference's QuickPol notebook.  The set is a 7.2 GB host array; only its rows with
     l <= 2 * 999 enter Xi (the 3j support), and those are seeded random values with a decaying
     envelope while the rest stay zero.  One step is one host call of ps_quickpol_xi_alm: packing
-    of the used rows, the copy, quickpolW and Xi on the GPU, and the copy back."""
+    of the used rows, the copy, quickpolW and Xi on the GPU, and the copy back into a page-locked Xi
+    (allocated once, as a caller registers its output matrix)."""
     import numpy as np
     import powerspectra_gpu as pg
     from oracle import oracle as o
@@ -651,17 +652,19 @@ def run_quickpol(args):
             / (1.0 + m)
     omega[:lw + 1] = omega[:lw + 1].real
     ctx = pg.Context(0)
+    import torch
+    Xout = torch.empty((lmax + 1, lmax + 1), dtype=torch.float64).pin_memory().numpy().T  # F-ordered, page-locked
 
     def timed(mode):
         for _ in range(max(args.warmup, 3)):
-            ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band, mode=mode)
+            ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band, mode=mode, out=Xout)
         ts, ks = [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            X = ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band, mode=mode)
+            X = ctx.quickpol_xi_alm(0, 0, 2, 2, omega, omega, alm_lmax, lmax, band, band, mode=mode, out=Xout)
             ts.append(time.perf_counter() - t0)
             ks.append(ctx.last_kernel_ms())
-        return X, statistics.median(ts), statistics.median(ks)
+        return X.copy(), statistics.median(ts), statistics.median(ks)
 
     Xp, t_plain, k_plain = timed("plain")
     clk = ClockSampler(0)
@@ -687,7 +690,8 @@ def run_quickpol(args):
             "config": {"workload": "quickpol_999", "lmax": lmax, "band": [band, band], "nu": [0, 0], "s": [2, 2],
                        "alm_lmax": alm_lmax, "alm_mmax": alm_lmax,
                        "used_rows": "l <= %d (the 3j support); the rest of the set is zero" % lw,
-                       "step": "ps_quickpol_xi_alm on host arrays: pack, copy, quickpolW + Xi kernels, copy back"},
+                       "step": "ps_quickpol_xi_alm on host arrays: pack, copy, quickpolW + Xi kernels, copy back "
+                               "into a page-locked Xi"},
             "e2e": {"value": t, "unit": "s", "h2d_bytes_per_step": 16 * o.n_alms(lw, lw),
                     "d2h_bytes_per_step": 8 * (lmax + 1) ** 2},
             "mode": args.mode, "kernel_ms": k_chosen,

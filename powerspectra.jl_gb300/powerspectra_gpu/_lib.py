@@ -56,6 +56,15 @@ class PSProblem(ctypes.Structure):
                 ("nW", ctypes.c_int64), ("W", _DPP), ("M", _DPP), ("ldm", ctypes.c_int64)]
 
 
+def _result_matrix(out, n):
+    """An (n, n) F-ordered float64 result: `out` if given (checked), else a new array."""
+    if out is None:
+        return np.empty((n, n), dtype=np.float64, order="F")
+    if out.shape != (n, n) or out.dtype != np.float64 or not out.flags.f_contiguous:
+        raise PowerSpectraArgumentError(PS_ERR_ARG, "out must be an F-ordered float64 array of shape (%d, %d)" % (n, n))
+    return out
+
+
 def load(path=None):
     """Load the shared library (no build, no fallback)."""
     global _lib
@@ -236,18 +245,21 @@ class Context:
         self.check(self.lib.ps_mcm_multi_device(self.handle, cases, dptr_array(wl), int(nW), lmin, lmax,
                                                 mode_code(mode), dptr_array(ml), int(ldm)))
 
-    def quickpol_xi(self, nu1, nu2, s1, s2, W, lmax, bl, bu, mode="plain"):
-        """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band."""
+    def quickpol_xi(self, nu1, nu2, s1, s2, W, lmax, bl, bu, mode="plain", out=None):
+        """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band.
+        `out` may supply the F-ordered float64 result (for example page-locked)."""
         W = np.ascontiguousarray(W, dtype=np.float64)
         n = lmax + 1
-        X = np.empty((n, n), dtype=np.float64, order="F")
+        X = _result_matrix(out, n)
         self.check(self.lib.ps_quickpol_xi(self.handle, int(nu1), int(nu2), int(s1), int(s2), dptr(W), len(W), lmax,
                                            int(bl), int(bu), mode_code(mode), dptr(X), n))
         return X
 
-    def quickpol_xi_alm(self, nu1, nu2, s1, s2, omega1, omega2, alm_lmax, lmax, bl, bu, alm_mmax=None, mode="plain"):
+    def quickpol_xi_alm(self, nu1, nu2, s1, s2, omega1, omega2, alm_lmax, lmax, bl, bu, alm_mmax=None, mode="plain",
+                        out=None):
         """quickpolXi!(Xi, nu1, nu2, s1, s2, omega1, omega2) (src/beam.jl:72-109): W = quickpolW(omega1,
-        omega2) and Xi on the GPU, from complex128 scan-weight coefficient sets (HEALPix order)."""
+        omega2) and Xi on the GPU, from complex128 scan-weight coefficient sets (HEALPix order).  `out` may
+        supply the F-ordered float64 result (for example page-locked)."""
         alm_mmax = alm_lmax if alm_mmax is None else alm_mmax
         nalm = (alm_mmax + 1) * (alm_mmax + 2) // 2 + (alm_mmax + 1) * (alm_lmax - alm_mmax)
         o1 = np.ascontiguousarray(omega1, dtype=np.complex128)
@@ -255,7 +267,7 @@ class Context:
         if o1.shape != (nalm,) or o2.shape != (nalm,):
             raise PowerSpectraArgumentError(PS_ERR_ARG, "a coefficient set needs %d entries" % nalm)
         n = lmax + 1
-        X = np.empty((n, n), dtype=np.float64, order="F")
+        X = _result_matrix(out, n)
         self.check(self.lib.ps_quickpol_xi_alm(self.handle, int(nu1), int(nu2), int(s1), int(s2),
                                                dptr(o1.view(np.float64)), dptr(o2.view(np.float64)), alm_lmax,
                                                alm_mmax, lmax, int(bl), int(bu), mode_code(mode), dptr(X), n))

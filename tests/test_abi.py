@@ -114,3 +114,14 @@ def test_bench_work_accounting_matches_oracle():
     assert wl["nW"] == 6143 and sorted(wl["Ws"]) == [0, 1, 2, 3]
     # fixed accounting: 9 (00) + 16 (22) + 3 per distinct spectrum
     assert bench.flops_per_launch(wl, 1) == 9 + 16 + 3 * 3
+
+
+def test_result_matrix_checks_caller_outputs():
+    import numpy as np
+    from powerspectra_gpu import _lib as L
+    ok = np.empty((3, 3), order="F")
+    assert L._result_matrix(ok, 3) is ok
+    assert L._result_matrix(None, 4).shape == (4, 4)
+    for bad in (np.empty((3, 3)), np.empty((3, 4), order="F"), np.empty((3, 3), dtype=np.float32, order="F")):
+        with pytest.raises(L.PowerSpectraArgumentError):
+            L._result_matrix(bad, 3)

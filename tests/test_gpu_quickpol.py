@@ -109,6 +109,25 @@ def test_quickpol_band_wider_than_grid(ctx, mode):
     assert np.max(np.abs(A - R)[S > 0] / S[S > 0]) < (1e-10 if mode == "plain" else 1e-6)
 
 
+def test_quickpol_into_caller_output(ctx):
+    """A caller-supplied (page-locked) output receives the whole matrix, zeros outside the band included."""
+    torch = pytest.importorskip("torch")
+    lmax = 50
+    W = np.exp(-np.arange(2 * lmax + 1) / 20.0)
+    out = torch.full((lmax + 1, lmax + 1), float("nan"), dtype=torch.float64).pin_memory().numpy().T
+    for mode in ("plain", "chosen"):
+        out[:] = np.nan
+        A = ctx.quickpol_xi(0, 0, 2, 2, W, lmax, 6, 6, mode=mode, out=out)
+        assert A is out
+        assert np.array_equal(A, ctx.quickpol_xi(0, 0, 2, 2, W, lmax, 6, 6, mode=mode))
+    rng = np.random.default_rng(3)
+    om = rng.normal(size=o.n_alms(30, 30)) + 1j * rng.normal(size=o.n_alms(30, 30))
+    out2 = torch.full((21, 21), float("nan"), dtype=torch.float64).pin_memory().numpy().T
+    B = ctx.quickpol_xi_alm(0, 0, 2, 2, om, om, 30, 20, 4, 4, mode="chosen", out=out2)
+    assert B is out2
+    assert np.array_equal(B, ctx.quickpol_xi_alm(0, 0, 2, 2, om, om, 30, 20, 4, 4, mode="chosen"))
+
+
 def test_quickpol_mode_error(ctx):
     import powerspectra_gpu as pg
     with pytest.raises(pg.PowerSpectraArgumentError):
