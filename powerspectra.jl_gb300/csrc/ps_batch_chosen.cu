@@ -27,7 +27,7 @@ struct BatchSets<8> {
 template <int NWIN>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, NWIN <= 4 ? 5 : 3) k_batch_chosen(const BatchParams bp)
 {
-    __shared__ float sW[kWarpsPerBlock][2][NWIN][kSlots];
+    __shared__ __align__(16) float sW[kWarpsPerBlock][2][NWIN][kSlots];  // 16-byte slot reads (4-slot bodies)
     // each warp's copy of its current group's parameters: read in the inner
     // loops, so they live in shared memory rather than behind global loads
     __shared__ CouplingParams sG[kWarpsPerBlock];

@@ -78,7 +78,7 @@ __device__ __forceinline__ void fetch_slice(int2* raw, const int2* __restrict__ 
 __device__ __forceinline__ void fetch_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void fetch_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-__device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane)
+__device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane, int stride = 1)
 {
     int2 v[kStagePerLane];
     int emax = kZeroExp;
@@ -89,9 +89,18 @@ __device__ __forceinline__ int scale_slice(float* dst, const int2* raw, int lane
     }
     emax = __reduce_max_sync(0xffffffffu, emax);
 #pragma unroll
-    for (int q = 0; q < kStagePerLane; ++q) dst[lane + 32 * q] = __int_as_float(v[q].x) * pow2f_or_zero(v[q].y - emax);
+    for (int q = 0; q < kStagePerLane; ++q)
+        dst[(lane + 32 * q) * stride] = __int_as_float(v[q].x) * pow2f_or_zero(v[q].y - emax);
     return emax;
 }
+
+// The scaled slices of a 4-slot kernel are interleaved as [slot][window], so
+// that a step reads the values of all its windows with one 16-byte load; other
+// kernels keep [window][slot].  Measured: the interleaving makes the 4-slot
+// kernels 0.2-4 % faster and the 8-slot ones (two 16-byte loads per step) up
+// to 16 % slower.
+template <int NWIN>
+constexpr bool slots_interleaved() { return NWIN == 4; }
 
 // Window configuration: 4 bits per window, product + 1 in bits 0-1 (so a used
 // window is never 0) and parity in bits 2-3.  A non-zero SPEC fixes the
@@ -159,6 +168,14 @@ template <int NWIN, bool N00, bool N22, uint32_t SPEC, bool EVEN>
 __device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s, const float* sw, int slot,
                                           float* c, float& n0, float& n2)
 {
+    float wv[NWIN];  // this slot's scaled value of each window
+    if constexpr (slots_interleaved<NWIN>()) {  // sw is 16-byte aligned (the callers' __align__(16) arrays)
+        const float4 t = *reinterpret_cast<const float4*>(sw + slot * NWIN);
+        wv[0] = t.x; wv[1] = t.y; wv[2] = t.z; wv[3] = t.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NWIN; ++k) wv[k] = sw[k * kSlots + slot];
+    }
     const float g2 = N22 ? __fadd_rn(s.f2.h, s.f2.l) : 0.0f;  // the value rounded to one float
     float x22 = __fmul_rn(g2, g2);
     if (N22) n2 = __fmaf_rn(s.w, x22, n2);
@@ -172,14 +189,14 @@ __device__ __forceinline__ void sweep_acc(const WinCfg<NWIN>& p, const Sweep& s,
             if (k < p.nwin && p.par[k] != PAR_ODD) {
                 const int pr = p.prod[k];
                 float x = pr == PROD_00_00 ? x00 : (pr == PROD_22_22 ? x22 : x02);
-                c[k] = __fmaf_rn(x, sw[k * kSlots + slot], c[k]);
+                c[k] = __fmaf_rn(x, wv[k], c[k]);
             }
         }
     } else if (N22) {
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
             if (k < p.nwin && p.prod[k] == PROD_22_22 && p.par[k] != PAR_EVEN)
-                c[k] = __fmaf_rn(x22, sw[k * kSlots + slot], c[k]);
+                c[k] = __fmaf_rn(x22, wv[k], c[k]);
         }
     }
 }
@@ -416,8 +433,13 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
             if (k < p.nwin) {
-                eF[k] = scale_slice(sF + k * kSlots, rF + k * kSlots, lane);
-                eB[k] = scale_slice(sB + k * kSlots, rB + k * kSlots, lane);
+                if constexpr (slots_interleaved<NWIN>()) {
+                    eF[k] = scale_slice(sF + k, rF + k * kSlots, lane, NWIN);
+                    eB[k] = scale_slice(sB + k, rB + k * kSlots, lane, NWIN);
+                } else {
+                    eF[k] = scale_slice(sF + k * kSlots, rF + k * kSlots, lane);
+                    eB[k] = scale_slice(sB + k * kSlots, rB + k * kSlots, lane);
+                }
             } else {
                 eF[k] = eB[k] = kZeroExp;
             }
