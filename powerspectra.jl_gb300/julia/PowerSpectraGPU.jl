@@ -2,7 +2,7 @@
 # libpowerspectra_gpu.so (the C ABI in include/powerspectra_gpu.h).
 #
 # Loading this module after PowerSpectra adds more specific methods for
-# Float64 matrix-backed SpectralArrays to
+# Float64 SpectralArrays (any dense column-major storage) to
 #     inner_mcm⁰⁰!, inner_mcm⁰²!, inner_mcm⁺⁺!, inner_mcm⁻⁻!   (src/modecoupling.jl:78-159)
 #     loop_covTTTT!, loop_covEEEE!, loop_covTTTE!, loop_covTETE!,
 #     loop_covTEEE!, loop_covTEEE_planck!, loop_covTTEE!        (src/covariance.jl:92-446)
@@ -30,8 +30,11 @@ const PS_MODE_CHOSEN = Cint(1)
 const COV = Dict(:TTTT => Cint(0), :EEEE => Cint(1), :TTTE => Cint(2), :TETE => Cint(3),
                  :TEEE => Cint(4), :TEEE_planck => Cint(5), :TTEE => Cint(6))
 
-# arithmetic used by the overrides; PS_MODE_PLAIN_FP64 reproduces the FP64 loops
-const MODE = Ref(PS_MODE_CHOSEN)
+# Arithmetic used by the overrides.  The default, PS_MODE_PLAIN_FP64, runs the
+# recurrences in FP64 and matches the reference's Float64 loops to 1e-12
+# relative.  PS_MODE_CHOSEN (FP32-pipe recurrences, <= 1e-6 relative) is
+# opt-in: `PowerSpectraGPU.MODE[] = PowerSpectraGPU.PS_MODE_CHOSEN`.
+const MODE = Ref(PS_MODE_PLAIN_FP64)
 # one library context per Julia thread (a context is not thread-safe)
 const CTXS = Dict{Int,Ptr{Cvoid}}()
 const CTX_LOCK = ReentrantLock()
@@ -54,19 +57,46 @@ function check(st, c)
     st == 1 ? throw(ArgumentError(msg)) : error("powerspectra_gpu error $st: $msg")
 end
 
-const FMat = SpectralArray{Float64,2,Matrix{Float64}}
+# Every override takes a SpectralArray{Float64,2} whatever its storage type.
+# `mcm` and `coupledcov` allocate with spectralzeros(lmin:lmax, lmin:lmax)
+# (src/spectralarray.jl:74), whose parent is an OffsetArray over a Matrix, so a
+# signature pinned to a Matrix parent would never be selected and the
+# reference's CPU loops would run instead.
+const FMat = SpectralArray{Float64,2}
+
+# The innermost array under the SpectralArray / OffsetArray wrappers.
+function storage(A)
+    P = parent(A)
+    return P === A ? A : storage(P)
+end
+
+# Column-major memory the library can write for 𝐌 and its leading dimension.
+# Dense column-major storage is passed as is; any other storage goes through a
+# Matrix that `writeback!` copies into it after the call.
+function dense_out(𝐌)
+    M = storage(𝐌)
+    if M isa StridedMatrix{Float64} && stride(M, 1) == 1
+        return M, stride(M, 2), false
+    end
+    X = Matrix{Float64}(undef, size(𝐌))
+    return X, size(X, 1), true
+end
+writeback!(𝐌, X, copied) = (copied && copyto!(storage(𝐌), X); 𝐌)
+
+# A spectrum's values as a plain 0-indexed Vector (W[1] is l = 0).
+spectrum(V) = collect(Float64, storage(V))
 
 function gpu_mcm!(spin::Cint, 𝐌::FMat, V::SpectralVector{Float64})
     @assert axes(𝐌, 1) == axes(𝐌, 2)
     lmin, lmax = first(axes(𝐌, 1)), last(axes(𝐌, 1))
-    M = parent(𝐌)          # column-major Matrix{Float64}, element (l1,l2) at [l1-lmin+1, l2-lmin+1]
-    W = collect(parent(V))  # 0-indexed spectrum: W[1] is l = 0
+    M, ld, copied = dense_out(𝐌)  # element (l1,l2) at [l1-lmin+1, l2-lmin+1]
+    W = spectrum(V)
     c = ctx()
     st = ccall((:ps_mcm, libps), Cint,
                (Ptr{Cvoid}, Cint, Ptr{Float64}, Int64, Cint, Cint, Cint, Ptr{Float64}, Int64),
-               c, spin, W, length(W), lmin, lmax, MODE[], M, stride(M, 2))
+               c, spin, W, length(W), lmin, lmax, MODE[], M, ld)
     check(st, c)
-    return 𝐌
+    return writeback!(𝐌, M, copied)
 end
 
 PowerSpectra.inner_mcm⁰⁰!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!(PS_SPIN_00, 𝐌, V)
@@ -77,11 +107,11 @@ PowerSpectra.inner_mcm⁻⁻!(𝐌::FMat, V::SpectralVector{Float64}) = gpu_mcm!
 function gpu_cov!(kind::Symbol, 𝐂::FMat, spectra, ratios, windows)
     @assert axes(𝐂, 1) == axes(𝐂, 2)
     lmin, lmax = first(axes(𝐂, 1)), last(axes(𝐂, 1))
-    S = [collect(parent(x)) for x in spectra]
-    R = [collect(parent(x)) for x in ratios]
-    W = [collect(parent(x)) for x in windows]
+    S = [spectrum(x) for x in spectra]
+    R = [spectrum(x) for x in ratios]
+    W = [spectrum(x) for x in windows]
     nW = minimum(length, W)
-    C = parent(𝐂)
+    C, ld, copied = dense_out(𝐂)
     c = ctx()
     GC.@preserve S R W begin
         Sp = [pointer(x) for x in S]
@@ -90,10 +120,10 @@ function gpu_cov!(kind::Symbol, 𝐂::FMat, spectra, ratios, windows)
         st = ccall((:ps_coupledcov, libps), Cint,
                    (Ptr{Cvoid}, Cint, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Ptr{Ptr{Float64}}, Int64,
                     Cint, Cint, Cint, Ptr{Float64}, Int64),
-                   c, COV[kind], Sp, Rp, Wp, nW, lmin, lmax, MODE[], C, stride(C, 2))
+                   c, COV[kind], Sp, Rp, Wp, nW, lmin, lmax, MODE[], C, ld)
     end
     check(st, c)
-    return 𝐂
+    return writeback!(𝐂, C, copied)
 end
 
 const SV = SpectralVector{Float64}
@@ -121,17 +151,18 @@ PowerSpectra.loop_covTTEE!(𝐂::FMat, TEip::SV, TEiq::SV, TEjq::SV, TEjp::SV, W
 # ---- rows downstream and upstream of the loops ----------------------------------------------
 
 # decouple_covmat (src/covariance.jl:8-14): B1^-1 Y B2^-T by two FP64 LU solves on the GPU
-function PowerSpectra.decouple_covmat(Y::FMat, B1::FMat, B2::FMat)
+# (the same diagonal signature as the reference's, with T = Float64, so it is the more specific method)
+function PowerSpectra.decouple_covmat(Y::SA, B1::SA, B2::SA) where {SA<:FMat}
     M = deepcopy(Y)
-    C = parent(M)
-    n = size(C, 1)
-    Yp, B1p, B2p = collect(parent(Y)), collect(parent(B1)), collect(parent(B2))  # dense, ld = n
+    n = size(M, 1)
+    Yp, B1p, B2p = (collect(Float64, storage(x)) for x in (Y, B1, B2))  # dense, ld = n
+    C, ld, copied = dense_out(M)
     c = ctx()
     st = ccall((:ps_decouple_covmat, libps), Cint,
                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64, Int64, Ptr{Float64}, Int64),
-               c, Yp, B1p, B2p, n, n, C, stride(C, 2))
+               c, Yp, B1p, B2p, n, n, C, ld)
     check(st, c)
-    return M
+    return writeback!(M, C, copied)
 end
 
 # quickpolΞ! (src/beam.jl:72-109): quickpolW and the banded Ξ on the GPU; the band is copied
