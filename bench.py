@@ -1,18 +1,27 @@
 #!/usr/bin/env python
 """Benchmark of the mode-coupling hot path: coupling elements per second.
 
-Workload (default, --config all_spins_3071): every spin case of one (l1, l2)
-grid at lmax 3071 with nW = 6143 -- M00 (TT) on the temperature mask spectrum,
-M02 (TE) on the TxP cross-spectrum, M++ and M-- (EE/BB blocks) on the
-polarisation mask spectrum: 4 matrices of 3072 x 3072 FP64 per step.  One step
-is one pass of the hot path over that workload (one ps_mcm_multi_device call).
+Workload (default, --config large_8191): the large coupling set at lmax 8191,
+nW 16383 -- 20 seeded mask spectra, spectrum k giving TT (M00, k % 3 == 0),
+EE (M++, k % 3 == 1) or BB (M--, k % 3 == 2): 20 matrices of 8192 x 8192 FP64
+(10.7 GB) per step, computed by ONE ps_mcm_set_device call (the (window, case)
+slots not wanted are NULL).  --config all_spins_3071 is the secondary headline:
+every spin case of one grid at lmax 3071 (M00, M02, M++, M--) through one
+ps_mcm_multi_device call.
 
   value     whole-job elements/s with the spectra resident in HBM
-  e2e       the same through the host-pointer C ABI call (ps_mcm_multi):
-            pinned host spectra in, pinned host matrices out, copies timed
-  roofline  the coupling kernel: algorithmic flops per launch / its CUDA-event
-            time, against this GPU's FMA-pipe peak measured live by the
-            library's probe kernel
+  e2e       the same through the host-pointer C ABI call (ps_mcm_set /
+            ps_mcm_multi): pinned host spectra in, pinned host matrices out,
+            copies inside the timed region
+  roofline  the coupling kernels: algorithmic flops per step / their
+            CUDA-event time, against this GPU's FMA-pipe peak measured live by
+            the library's probe kernel
+  plain_fp64  the plain FP64 kernels on the same workload, the chosen/plain
+            ratio, and the max relative error of every chosen matrix against
+            its FP64 counterpart (relative to |FP64| -- all terms are >= 0 -- or,
+            for TE, to the Cauchy-Schwarz bound of its sum of |terms|; no floor)
+  decoupled  max relative error of the decoupled spectrum M \\ pCl solved with
+            the chosen M against the FP64 M (ps_solve), pCl = M_fp64 C_true
   cpu_baseline  the C/OpenMP oracle (the reference algorithm restated) on a
             row sample of the same workload, on the host cores
 
@@ -57,22 +66,39 @@ def l3_terms(lmin, lmax, nW):
 
 
 def workload(name, rank=0):
+    """The headline workloads.  kind "multi": one ps_mcm_multi call, spin case s on window Ws[s];
+    kind "set": one ps_mcm_set call over `windows` with the (window, case) `slots`."""
     from powerspectra_gpu import synthetic as syn
     if name.startswith("all_spins_"):
-        L = int(name.rsplit("_", 1)[1])  # all_spins_3071 is the benchmark; smaller ones are profiling cases
+        L = int(name.rsplit("_", 1)[1])  # all_spins_3071 is configuration 2; smaller ones are profiling cases
         c = syn.all_spins(L, seed=1 + 10 * rank)
         Ws = {0: c["WT"], 1: c["WTP"], 2: c["WP"], 3: c["WP"]}
-        return {"name": name, "lmin": 0, "lmax": L, "nW": c["nW"], "Ws": Ws, "spectra": 3,
-                "cases": ["TT (M00, W_T)", "TE (M02, W_TxP)", "EE/BB diagonal (M++, W_P)", "EE/BB off-diagonal (M--, W_P)"]}
+        return {"name": name, "kind": "multi", "lmin": 0, "lmax": L, "nW": c["nW"], "Ws": Ws, "spectra": 3,
+                "slots": [(s, s) for s in range(4)], "windows": [Ws[s] for s in range(4)],
+                "cases": ["TT (M00, W_T)", "TE (M02, W_TxP)", "EE/BB diagonal (M++, W_P)",
+                          "EE/BB off-diagonal (M--, W_P)"]}
     if name == "tt_767":
         c = syn.tt_767(seed=rank)
-        return {"name": name, "lmin": 0, "lmax": 767, "nW": len(c["W"]), "Ws": {0: c["W"]}, "spectra": 1,
-                "cases": ["TT (M00)"]}
+        return {"name": name, "kind": "multi", "lmin": 0, "lmax": 767, "nW": len(c["W"]), "Ws": {0: c["W"]},
+                "spectra": 1, "slots": [(0, 0)], "windows": [c["W"]], "cases": ["TT (M00)"]}
+    if name.startswith("large_"):
+        L = int(name.rsplit("_", 1)[1])  # large_8191 is configuration 5; smaller ones are profiling cases
+        big = syn.large_set(lmax=L, seed=5 + 10 * rank)
+        slots = [(k, (0, 2, 3)[k % 3]) for k in range(len(big["W"]))]
+        return {"name": name, "kind": "set", "lmin": 0, "lmax": L, "nW": big["nW"], "windows": big["W"],
+                "spectra": len(big["W"]), "slots": slots, "cases_mask": 0xD,
+                "cases": ["%d spectra: TT (M00) for k %% 3 == 0, EE (M++) for k %% 3 == 1, BB (M--) for k %% 3 == 2"
+                          % len(big["W"])]}
     raise SystemExit("unknown --config %s" % name)
 
 
-def flops_per_launch(wl, terms):
-    spins = set(wl["Ws"])
+CASE_NAMES = {0: "TT", 1: "TE", 2: "EE_pp", 3: "BB_mm"}
+
+
+def flops_per_step(wl, terms):
+    """Canonical flops of one step: each family the slots need once per l3-term, and the contraction
+    once per distinct spectrum (++ and -- of one spectrum split its terms by parity)."""
+    spins = set(s for _, s in wl["slots"])
     f = 0
     if spins & {0, 1}:
         f += FLOP_SPIN0
@@ -80,6 +106,18 @@ def flops_per_launch(wl, terms):
         f += FLOP_SPIN2
     f += FLOP_CONTRACT * wl["spectra"]
     return f * terms
+
+
+def _profile_traffic(workload_name, mode):
+    """DRAM bytes per step of the coupling kernels from a committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        rec = json.load(open(path)).get(workload_name, {}).get(mode)
+    except (OSError, ValueError):
+        return None, None
+    if not rec:
+        return None, None
+    return rec["bytes_per_step"], "profiles/dram_traffic.json: " + rec["command"]
 
 
 class ClockSampler:
@@ -127,45 +165,58 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(wl, budget_rows_stride, nthreads=0):
-    """Oracle (reference algorithm: one family fill + dot per pair and spin case, OpenMP
-    dynamic rows) on every stride-th l1 row; elements/s extrapolated by l3-term share."""
+def cpu_baseline(wl, stride, nthreads=0, offset=0):
+    """Oracle (reference algorithm: one family fill + dot per pair and (window, spin case) slot,
+    OpenMP dynamic rows) on every stride-th l1 row from lmin + offset; elements/s scaled by the
+    l3-term share of the sampled rows."""
     from oracle import oracle as o
     lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
-    rows = list(range(lmin, lmax + 1, budget_rows_stride))
+    rows = list(range(lmin + offset % stride, lmax + 1, stride))
     t0 = time.perf_counter()
-    for s, W in wl["Ws"].items():
-        o.inner_mcm(s, W, lmin, lmax, rows=rows, nthreads=nthreads)
+    for k, s in wl["slots"]:
+        o.inner_mcm(s, wl["windows"][k], lmin, lmax, rows=rows, nthreads=nthreads)
     dt = time.perf_counter() - t0
     share = o.l3_terms(lmin, lmax, nW, rows) / o.l3_terms(lmin, lmax, nW)
     n = lmax - lmin + 1
-    elements = len(wl["Ws"]) * n * n
+    elements = len(wl["slots"]) * n * n
     threads = nthreads or o.max_threads()
     return {"value": elements * share / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "every %d-th l1 row (%d rows, %.2f%% of the l3-terms), %d spin cases as separate passes, "
-                      "%.1f s, scaled by l3-term share" % (budget_rows_stride, len(rows), 100 * share,
-                                                            len(wl["Ws"]), dt)}
+            "seconds": dt, "sampled_fraction": share,
+            "sample": "every %d-th l1 row (%d rows, %.3f%% of the l3-terms), %d (window, spin case) slots as "
+                      "separate passes, %.1f s, scaled by l3-term share" % (stride, len(rows), 100 * share,
+                                                                          len(wl["slots"]), dt)}
+
+
+# l1-row stride of the oracle samples: (cpu_baseline leg of our arm, one step of the reference arm)
+CPU_STRIDE = {"tt_767": (1, 2), "all_spins_3071": (3, 16), "large_8191": (512, 2048)}
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference algorithm on the same workload.
+    Each step times a bounded row sample (the sampled rows rotate from step to step); `value` is
+    the sampled elements/s scaled by the l3-term share, and `ms_per_step` is the time a step
+    actually took.  The full-step time is extrapolated and marked so."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     wl = workload(args.config)
-    stride = {"tt_767": 2}.get(args.config, 16)
-    for _ in range(args.warmup):
-        cpu_baseline(wl, stride)
-    vals = [cpu_baseline(wl, stride) for _ in range(args.steps)]
+    stride = CPU_STRIDE.get(args.config, (3, 16))[1]
+    for i in range(args.warmup):
+        cpu_baseline(wl, stride, offset=7 * i)
+    vals = [cpu_baseline(wl, stride, offset=7 * (args.warmup + i)) for i in range(args.steps)]
     value = statistics.median(v["value"] for v in vals)
     n = wl["lmax"] - wl["lmin"] + 1
-    ms = len(wl["Ws"]) * n * n / value * 1e3
+    timed_s = sum(v["seconds"] for v in vals)
     cb = dict(vals[-1])
     cb["value"] = value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": timed_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": wl["name"], "lmax": wl["lmax"], "nW": wl["nW"], "cases": wl["cases"],
                        "implementation": "C/OpenMP restatement of the reference algorithm (Julia is not installed)"},
+            "timed_seconds": timed_s, "extrapolated": True,
+            "sampled_fraction": statistics.mean(v["sampled_fraction"] for v in vals),
+            "ms_per_full_step_extrapolated": len(wl["slots"]) * n * n / value * 1e3,
             "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -173,24 +224,79 @@ def run_reference(args):
 
 
 def _accuracy(ctx, wl, got, ref):
-    """Max elementwise relative error of `got` (chosen) against `ref` (plain FP64) per spin
-    case, on the device.  TE elements are measured against the Cauchy-Schwarz bound of
-    their sum of |terms|, sqrt(M00(|W|) (M++(|W|) + M--(|W|))), computed in FP64."""
+    """Max elementwise relative error of `got` (chosen) against `ref` (plain FP64), per (window,
+    case) slot, on the device, with no floor: relative to |ref| (every term of a squared family
+    on a non-negative window is >= 0, so |ref| is the sum of |terms|), and for TE to the
+    Cauchy-Schwarz bound of its sum of |terms|, sqrt(M00(|W|) (M++(|W|) + M--(|W|))), in FP64."""
+    import numpy as np
     import torch
     out = {}
-    names = {0: "TT", 1: "TE", 2: "EE_BB_pp", 3: "EE_BB_mm"}
-    for s in sorted(got):
-        den = ref[s].abs()
-        if s == 1:
-            import numpy as np
-            A = np.abs(wl["Ws"][1])
-            n = wl["lmax"] - wl["lmin"] + 1
+    n = wl["lmax"] - wl["lmin"] + 1
+    for slot in wl["slots"]:
+        k, s = slot
+        den = ref[slot].abs()
+        if s == 1 or (wl["windows"][k] < 0).any():
+            A = np.abs(wl["windows"][k])
             m = ctx.mcm_multi({0: A, 2: A, 3: A}, wl["lmin"], wl["lmax"], mode="plain")
-            b = torch.from_numpy(np.sqrt(np.abs(m[0] * (m[2] + m[3]))).T.copy()).to(ref[s].device)
-            den = torch.maximum(den, b.reshape(n, n))
+            b = m[s] if s != 1 else np.sqrt(np.abs(m[0] * (m[2] + m[3])))
+            den = torch.maximum(den, torch.from_numpy(b.T.copy()).to(ref[slot].device).reshape(n, n))
         den = torch.where(den == 0, torch.ones_like(den), den)
-        out[names[s]] = float(((got[s] - ref[s]).abs() / den).max().item())
+        out[slot] = float(((got[slot] - ref[slot]).abs() / den).max().item())
     return out
+
+
+def _decoupled(ctx, wl, got, ref, extra):
+    """Max relative error of decoupled spectra: pCl = M_fp64 C_true, then M \\ pCl by ps_solve
+    (FP64 LU on the GPU) with the chosen M and with the FP64 M (src/modecoupling.jl:358,
+    src/blockspectralmatrix.jl:124-129).  TT: M00 of the first TT slot.  EE/BB: the block
+    [[M++, M--], [M--, M++]] of one spectrum on l >= 2 (the 2x2 block of mcm(:EE_BB),
+    src/modecoupling.jl:210-216).  TE: M02 on l >= 2.  `extra(k, s, mode)` supplies a missing
+    block of spectrum k as a device tensor."""
+    import numpy as np
+    lmin, lmax = wl["lmin"], wl["lmax"]
+    ls = np.arange(lmin, lmax + 1, dtype=np.float64)
+    base = ((ls + 2.0) / 80.0) ** -2.4
+    C = {"TT": 1000.0 * base, "EE": 40.0 * base, "BB": 4.0 * base, "TE": 0.3 * np.sqrt(1000.0 * 40.0) * base}
+
+    def host(t):  # the device tensor holds the column-major matrix: its transpose is M
+        return np.asfortranarray(t.cpu().numpy().T)
+
+    def err(Mc, Mp, c):
+        p = Mp @ c
+        xc, xp = ctx.solve(Mc, p), ctx.solve(Mp, p)
+        return {"max_rel_err_chosen_vs_fp64": float(np.max(np.abs(xc - xp) / np.abs(xp))),
+                "max_rel_err_fp64_vs_truth": float(np.max(np.abs(xp - c) / np.abs(c)))}
+
+    res = {}
+    tt = [sl for sl in wl["slots"] if sl[1] == 0]
+    if tt:
+        r = err(host(got[tt[0]]), host(ref[tt[0]]), C["TT"])
+        r["system"] = "M00 of spectrum %d, l = %d..%d" % (tt[0][0], lmin, lmax)
+        res["TT"] = r
+    cut = max(0, 2 - lmin)
+    te = [sl for sl in wl["slots"] if sl[1] == 1]
+    if te:
+        r = err(host(got[te[0]])[cut:, cut:], host(ref[te[0]])[cut:, cut:], C["TE"][cut:])
+        r["system"] = "M02 of spectrum %d, l = %d..%d" % (te[0][0], lmin + cut, lmax)
+        res["TE"] = r
+    pp = [sl for sl in wl["slots"] if sl[1] == 2]
+    if pp:
+        k = pp[0][0]
+        mats = {}
+        for mode, src in (("chosen", got), ("plain", ref)):
+            Mpp = host(src[k, 2])[cut:, cut:]
+            Mmm = host(src[k, 3] if (k, 3) in src else extra(k, 3, mode))[cut:, cut:]
+            mats[mode] = np.block([[Mpp, Mmm], [Mmm, Mpp]])
+        c = np.concatenate([C["EE"][cut:], C["BB"][cut:]])
+        r = err(np.asfortranarray(mats["chosen"]), np.asfortranarray(mats["plain"]), c)
+        m = len(c) // 2
+        p = mats["plain"] @ c
+        xc, xp = ctx.solve(np.asfortranarray(mats["chosen"]), p), ctx.solve(np.asfortranarray(mats["plain"]), p)
+        rel = np.abs(xc - xp) / np.abs(xp)
+        r.update({"EE": float(rel[:m].max()), "BB": float(rel[m:].max()),
+                  "system": "[[M++, M--], [M--, M++]] of spectrum %d, l = %d..%d" % (k, lmin + cut, lmax)})
+        res["EE_BB"] = r
+    return res
 
 
 def run_ours(args):
@@ -222,7 +328,8 @@ def run_ours(args):
     wl = workload(args.config, rank)
     lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
     n = lmax - lmin + 1
-    spins = sorted(wl["Ws"])
+    slots = wl["slots"]
+    K = len(wl["windows"])
     mode = args.mode
     ctx = pg.Context(local)
     # one real (non-default) stream shared by torch and the library, so the CUDA
@@ -231,20 +338,31 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
-    dW = {s: torch.tensor(wl["Ws"][s], device="cuda") for s in spins}
-    dM = {s: torch.empty((n, n), dtype=torch.float64, device="cuda") for s in spins}
+    dW = [torch.tensor(w, device="cuda") for w in wl["windows"]]
+    dM = {sl: torch.empty((n, n), dtype=torch.float64, device="cuda") for sl in slots}
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    wptr = {s: dW[s].data_ptr() for s in spins}
-    mptr = {s: dM[s].data_ptr() for s in spins}
 
-    def step(m=mode, outp=mptr):
-        ctx.mcm_multi_device(wptr, nW, lmin, lmax, outp, n, mode=m)
+    def ptrs(mats):
+        if wl["kind"] == "multi":
+            return {s: mats[k, s].data_ptr() for k, s in slots}
+        out = [0] * (4 * K)
+        for k, s in slots:
+            out[4 * k + s] = mats[k, s].data_ptr()
+        return out
 
+    def step(m=mode, mats=dM, outp=None):
+        outp = outp or ptrs(mats)
+        if wl["kind"] == "multi":
+            ctx.mcm_multi_device({s: dW[k].data_ptr() for k, s in slots}, nW, lmin, lmax, outp, n, mode=m)
+        else:
+            ctx.mcm_set_device(wl["cases_mask"], [d.data_ptr() for d in dW], nW, lmin, lmax, outp, n, mode=m)
+
+    mptr = ptrs(dM)
     peak64 = ctx.fma_peak(fp64=True)
     peak32 = ctx.fma_peak(fp64=False)
     for _ in range(max(args.warmup, 3)):
         flush.zero_()
-        step()
+        step(outp=mptr)
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -256,24 +374,23 @@ def run_ours(args):
     t0.record(stream)
     for _ in range(args.steps):
         flush.zero_()
-        step()
-        kernel_ms.append(ctx.last_kernel_ms())  # coupling kernel only, events on this stream
+        step(outp=mptr)
+        kernel_ms.append(ctx.last_kernel_ms())  # the coupling kernels of this call, events on this stream
     t1.record(stream)
     barrier()
     launches = ctx.launch_count() - n_launch0
     clk = clocks.stop()
     elapsed = max_over_ranks(t0.elapsed_time(t1) / 1e3)
-    elements = len(spins) * n * n
+    elements = len(slots) * n * n
     value = world * elements * args.steps / elapsed
 
-    # the plain FP64 kernel on the same workload (the chosen form's comparison point)
-    plain = None
+    # the plain FP64 kernels on the same workload (the chosen form's comparison point): one timed
+    # step (the kernels run for seconds, so no warm-up), then every chosen matrix against it
+    plain = decoupled = None
     if mode == "chosen" and not args.no_plain:
-        pM = {s: torch.empty((n, n), dtype=torch.float64, device="cuda") for s in spins}
-        pptr = {s: pM[s].data_ptr() for s in spins}
-        step("plain", pptr)
-        torch.cuda.synchronize()
-        ksteps = max(1, min(args.steps, 2))
+        pM = {sl: torch.empty((n, n), dtype=torch.float64, device="cuda") for sl in slots}
+        pptr = ptrs(pM)
+        ksteps = 1 if lmax > 4095 else max(1, min(args.steps, 2))
         pk = []
         barrier()
         p0 = torch.cuda.Event(enable_timing=True)
@@ -281,32 +398,57 @@ def run_ours(args):
         p0.record(stream)
         for _ in range(ksteps):
             flush.zero_()
-            step("plain", pptr)
+            step("plain", outp=pptr)
             pk.append(ctx.last_kernel_ms())
         p1.record(stream)
         barrier()
         pel = max_over_ranks(p0.elapsed_time(p1) / 1e3)
-        acc = _accuracy(ctx, wl, dM, pM) if rank == 0 else None
-        plain = {"value": world * elements * ksteps / pel, "unit": UNIT, "kernel_ms_per_launch": statistics.mean(pk),
-                 "steps": ksteps}
+        plain = {"value": world * elements * ksteps / pel, "unit": UNIT, "kernel_ms_per_step": statistics.mean(pk),
+                 "ms_per_step": pel / ksteps * 1e3, "steps": ksteps}
         plain["chosen_over_plain"] = value / plain["value"]
-        plain["max_rel_err_chosen_vs_fp64"] = acc
+        if rank == 0:
+            acc = _accuracy(ctx, wl, dM, pM)
+            per_case = {}
+            for (k, s), e in acc.items():
+                per_case[CASE_NAMES[s]] = max(per_case.get(CASE_NAMES[s], 0.0), e)
+            plain["max_rel_err_chosen_vs_fp64"] = per_case
+            plain["max_rel_err_per_matrix"] = [{"spectrum": k, "case": CASE_NAMES[s], "max_rel_err": acc[k, s]}
+                                               for k, s in slots]
+            plain["error_measure"] = ("max over all elements of |chosen - fp64| / |fp64| (TE: / Cauchy-Schwarz "
+                                      "bound of the sum of |terms|); no floor")
+            if not args.no_decoupled:
+                def extra(k, s, m):
+                    t = torch.empty((n, n), dtype=torch.float64, device="cuda")
+                    ctx.mcm_multi_device({s: dW[k].data_ptr()}, nW, lmin, lmax, {s: t.data_ptr()}, n, mode=m)
+                    torch.cuda.synchronize()
+                    return t
+                decoupled = _decoupled(ctx, wl, dM, pM, extra)
         del pM
 
-    # end to end through the host-pointer ABI: pinned spectra in, pinned matrices out
-    hW = {s: torch.from_numpy(np.ascontiguousarray(wl["Ws"][s])).pin_memory().numpy() for s in spins}
-    hM = {s: torch.empty((n, n), dtype=torch.float64).pin_memory().numpy().T for s in spins}  # F-ordered views
+    # end to end through the host-pointer ABI: pinned spectra in, pinned matrices out, every step
+    hW = [torch.from_numpy(np.ascontiguousarray(w)).pin_memory().numpy() for w in wl["windows"]]
+    hM = {sl: torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy().T for sl in slots}  # F-ordered
     ctx.set_stream(0)
-    ctx.mcm_multi(hW, lmin, lmax, mode=mode, outs=hM)  # warm the host path
+
+    def host_step():
+        if wl["kind"] == "multi":
+            ctx.mcm_multi({s: hW[k] for k, s in slots}, lmin, lmax, mode=mode, outs={s: hM[k, s] for k, s in slots})
+        else:
+            ctx.mcm_set(wl["cases_mask"], hW, lmin, lmax, mode=mode, outs=hM, slots=set(slots))
+    host_step()  # warm the host path
     barrier()
     e0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.mcm_multi(hW, lmin, lmax, mode=mode, outs=hM)
+        host_step()
     barrier()
     e_el = max_over_ranks(time.perf_counter() - e0)
+    nuse = min(nW, 2 * lmax + 1)
     e2e = {"value": world * elements * args.steps / e_el, "unit": UNIT,
-           "h2d_bytes_per_step": int(sum(min(len(hW[s]), 2 * lmax + 1) * 8 for s in spins)),
-           "d2h_bytes_per_step": int(elements * 8)}
+           "h2d_bytes_per_step": int(len(set(k for k, _ in slots)) * nuse * 8),
+           "d2h_bytes_per_step": int(elements * 8),
+           "call": "ps_mcm_multi" if wl["kind"] == "multi" else "ps_mcm_set",
+           "how": "pinned host spectra in; pinned host matrices out, written by the kernel in place"}
+    del hM
 
     if rank != 0:
         if dist is not None:
@@ -314,35 +456,35 @@ def run_ours(args):
         return 0
 
     terms = l3_terms(lmin, lmax, nW)
-    fl = flops_per_launch(wl, terms)
+    fl = flops_per_step(wl, terms)
     kms = statistics.mean(kernel_ms)
     peak = peak64 if mode == "plain" else peak32
     achieved = fl / (kms * 1e-3)
-    # DRAM bytes per launch from one ncu capture of this kernel at this size
-    # (profiles/coupling_chosen_all_spins_3071_dram.md); bench.py cannot run ncu itself
-    traffic = 2.468e8 if (wl["name"] == "all_spins_3071" and mode == "chosen") else None
+    traffic, traffic_src = _profile_traffic(wl["name"], mode)
     roofline = {"bound": "fp64_fma_pipe" if mode == "plain" else "fp32_fma_pipe",
                 "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture of the same kernel "
-                                  "and workload" if traffic else None,
+                "traffic": traffic, "traffic_source": traffic_src,
                 "peak_source": "measured live by the library's FMA-chain probe kernel (MEASURED_PEAKS.json has no "
                                "CUDA-core FP64/FP32 figure)",
-                "algorithmic_flops_per_launch": fl, "l3_terms_per_family": terms,
-                "flops_per_l3_term": fl / terms, "kernel_ms_per_launch": kms}
+                "algorithmic_flops_per_step": fl, "l3_terms_per_family": terms,
+                "flops_per_l3_term": fl / terms, "kernel_ms_per_step": kms,
+                "kernels": "the coupling kernels of one call (CUDA events around them on the launching stream)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if mode == "plain" else "f32",
             "data": "synthetic",
-            "config": {"workload": wl["name"], "lmax": lmax, "nW": nW, "matrices_per_step": len(spins),
+            "config": {"workload": wl["name"], "lmax": lmax, "nW": nW, "matrices_per_step": len(slots),
                        "cases": wl["cases"], "mode": mode, "per_rank": "independent problem per GPU",
+                       "call": "ps_mcm_multi_device" if wl["kind"] == "multi" else "ps_mcm_set_device",
                        "l2": "256 MiB buffer written between timed steps"},
             "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
             "fma_peaks_tflops": {"fp64": peak64 / 1e12, "fp32": peak32 / 1e12}}
     if plain is not None:
         line["plain_fp64"] = plain
+    if decoupled is not None:
+        line["decoupled"] = decoupled
     if world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(wl, {"tt_767": 1}.get(args.config, 3))
+        line["cpu_baseline"] = cpu_baseline(wl, CPU_STRIDE.get(args.config, (3, 16))[0])
     print(json.dumps(line))
     ctx.close()
     if dist is not None:
@@ -350,7 +492,7 @@ def run_ours(args):
     return 0
 
 
-SET_CONFIGS = ("batched_64", "large_8191", "cov_2508")
+SET_CONFIGS = ("batched_64", "large_set", "cov_2508")
 
 
 def _set_problems(name, lmax=0):
@@ -358,8 +500,9 @@ def _set_problems(name, lmax=0):
 
     batched_64: 64 problems, lmax drawn from {511, ..., 6143}, K in 1..16 seeded mask
       spectra each, spin 0 (M00 per spectrum) or spin 2 (M++ and M-- per spectrum).
-    large_8191: lmax 8191, nW 16383, K = 20 spectra; spectrum k gives TT (k % 3 == 0),
-      EE = M++ (k % 3 == 1) or BB = M-- (k % 3 == 2): 20 matrices of 8192^2, 10.7 GB.
+    large_set: the large_8191 workload (lmax 8191, nW 16383, K = 20 spectra; spectrum k gives
+      TT (k % 3 == 0), EE = M++ (k % 3 == 1) or BB = M-- (k % 3 == 2): 20 matrices of 8192^2,
+      10.7 GB) as one ps_mcm_set_device call per spin case, against the persistent batch graph.
     """
     from powerspectra_gpu import synthetic as syn
     if name == "batched_64":
@@ -368,7 +511,7 @@ def _set_problems(name, lmax=0):
             out.append({"lmin": 0, "lmax": pr["lmax"], "cases": 0x1 if pr["spin"] == 0 else 0xC,
                         "nW": pr["lmax"] + 1, "W": pr["W"]})
         return out
-    if name == "large_8191":
+    if name == "large_set":
         big = syn.large_set(lmax=lmax or 8191)
         groups = {0x1: [], 0x4: [], 0x8: []}
         for k, W in enumerate(big["W"]):
@@ -471,13 +614,13 @@ def run_set(args):
                                    mode="chosen")
         line["config"].update({"problems": len(probs), "matrices": len(mats),
                                "lmax": sorted(set(p["lmax"] for p in probs)), "autotune": tune})
-        # the set of spectra on one grid (large_8191) runs as one ps_mcm_set_device call per spin case;
+        # the set of spectra on one grid (large_set) runs as one ps_mcm_set_device call per spin case;
         # the uneven batch (batched_64) as one persistent launch replayed from a CUDA graph, with
         # the per-problem ps_mcm_set_device calls timed beside it
-        chosen = sequential_chosen if args.config == "large_8191" else ctx.batch_graph_launch
-        other = ctx.batch_graph_launch if args.config == "large_8191" else sequential_chosen
-        other_name = "batched_graph" if args.config == "large_8191" else "sequential_chosen"
-        line["config"]["chosen_path"] = ("ps_mcm_set_device per spin case" if args.config == "large_8191"
+        chosen = sequential_chosen if args.config == "large_set" else ctx.batch_graph_launch
+        other = ctx.batch_graph_launch if args.config == "large_set" else sequential_chosen
+        other_name = "batched_graph" if args.config == "large_set" else "sequential_chosen"
+        line["config"]["chosen_path"] = ("ps_mcm_set_device per spin case" if args.config == "large_set"
                                          else "ps_batch_graph_launch (persistent kernel)")
         for _ in range(args.warmup):
             other()
@@ -491,8 +634,7 @@ def run_set(args):
         d = 0.0
         for (c, _), r in zip(mats, seq_rows):
             b = c[[0, c.shape[0] // 2, c.shape[0] - 1]]
-            den = torch.maximum(r.abs(), 1e-9 * r.abs().max())
-            den = torch.where(den == 0, torch.ones_like(den), den)
+            den = torch.where(r == 0, torch.ones_like(r), r.abs())
             d = max(d, float(((b - r).abs() / den).max().item()))
         line[other_name]["max_rel_diff_vs_timed_path"] = d
     line.update({"metric": METRIC, "value": elements / t_c, "ms_per_step": t_c * 1e3, "steps": args.steps,
@@ -500,13 +642,33 @@ def run_set(args):
     if not args.no_plain:
         plain()
         t_p = ev_time(plain, 1)
+        # strict error, no floor: |fp64| where every term is >= 0 (squared families on non-negative
+        # windows, and the covariance blocks whose windows all use squared families); the TETE
+        # block's 00x22 windows cancel, so it is measured on sampled rows against the oracle's
+        # sum of |terms| of each element
         errs = []
-        for c, q in mats:
-            den = torch.maximum(q.abs(), 1e-9 * q.abs().max())
-            den = torch.where(den == 0, torch.ones_like(den), den)
+        for i, (c, q) in enumerate(mats):
+            if args.config == "cov_2508" and jobs[i][0] == "TETE":
+                from oracle import oracle as o
+                kind, S, R, Ws = jobs[i]
+                rows = [0, 1, 2, 300, 1254, 2000, 2508]
+                h = lambda t: t.cpu().numpy()
+                sc = o.loop_cov(kind, [h(x) for x in S], [h(x) for x in R], [h(x) for x in Ws], 0, L, rows=rows,
+                                absolute=True)
+                cc, qq = h(c).T, h(q).T
+                e = 0.0
+                for r in rows:  # the oracle fills row r from the diagonal on
+                    den = np.maximum(np.abs(qq[r, r:]), sc[r, r:])
+                    den = np.where(den == 0, 1.0, den)
+                    e = max(e, float(np.max(np.abs(cc[r, r:] - qq[r, r:]) / den)))
+                errs.append(e)
+                continue
+            den = torch.where(q == 0, torch.ones_like(q), q.abs())
             errs.append(float(((c - q).abs() / den).max().item()))
         line["plain_fp64"] = {"value": elements / t_p, "ms_per_step": t_p * 1e3, "steps": 1,
-                              "chosen_over_plain": t_p / t_c, "max_rel_err_chosen_vs_fp64": max(errs)}
+                              "chosen_over_plain": t_p / t_c, "max_rel_err_chosen_vs_fp64": max(errs),
+                              "error_measure": "|chosen - fp64| / |fp64| per element, no floor (TETE: sampled "
+                                               "rows against the oracle's sum of |terms|)"}
     print(json.dumps(line))
     ctx.close()
     return 0
@@ -714,11 +876,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--config", default="all_spins_3071")
+    ap.add_argument("--config", default="large_8191")
     ap.add_argument("--mode", default="chosen", choices=("plain", "chosen"),
                     help="chosen: FP32-pipe recurrence with compensation (the product path); plain: FP64")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 kernel")
+    ap.add_argument("--no-decoupled", action="store_true", help="skip the decoupled-spectrum error leg")
     ap.add_argument("--lmax", type=int, default=0,
                     help="window_W_8191 and large_8191: another lmax (a smaller case for profiling)")
     args = ap.parse_args()

@@ -124,11 +124,12 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
 
 /* Many mask spectra on one (l1, l2) grid: for window k and every spin case s
  * selected in `cases`, dM[4*k + s] receives the matrix (entries of unselected
- * cases are ignored).  This is `mcm` for a set of spectra (the reference calls
- * inner_mcm*! once per spectrum and case, src/modecoupling.jl:192-246).  The
- * (window, case) slots are processed in groups (up to 4 in chosen mode, 8 in
- * plain FP64) sharing one generation of the families per pair.  Device pointers; enqueued on the
- * context stream. */
+ * cases are ignored, and a NULL entry of a selected case skips that (window,
+ * case) slot; at least one slot must remain).  This is `mcm` for a set of
+ * spectra (the reference calls inner_mcm*! once per spectrum and case,
+ * src/modecoupling.jl:192-246).  The (window, case) slots are processed in
+ * groups of up to 8, each sharing one generation of the families per pair.
+ * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
 /* The same with host spectra and host matrices: returns when every M is
@@ -249,8 +250,9 @@ int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best
 int ps_mcm_multi_device_noalloc(unsigned cases, const double *const dW[4], int64_t nW, int lmin, int lmax,
                                 double *const dM[4], int64_t ldm, void *stream);
 
-/* Instrumentation: device time of the last coupling kernel (CUDA events on the
- * launching stream), number of kernels this context has launched, and a
+/* Instrumentation: device time of the coupling kernels of the last call (CUDA
+ * events on the launching stream, from the first coupling launch of the call
+ * to the end of its last), number of kernels this context has launched, and a
  * measured FMA-pipe peak (flop/s, FMA = 2 flops) of this GPU in FP64 (fp64=1)
  * or FP32 (fp64=0). */
 double ps_last_kernel_ms(const ps_ctx *ctx);

@@ -270,22 +270,26 @@ void cov_window_spec(int kind, int k, int* product, int* parity)
 }
 }  // namespace ps
 
-// Launch the coupling kernel with event timing on the context stream.
-static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode)
+// Launch the coupling kernel with event timing on the context stream.  A call
+// that launches several groups passes first/last so that the two events
+// bracket all of its coupling kernels (ps_last_kernel_ms).
+static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode, bool first = true, bool last = true)
 {
     const bool chosen = mode == PS_MODE_CHOSEN;
     int st = chosen ? ensure_tiles(c, p.lmin, p.lmax) : ensure_tasks(c, p.lmin, p.lmax);
     if (st) return st;
     p.tasks = chosen ? c->d_tiles : c->d_tasks;
     p.ntasks = chosen ? c->ntiles : c->ntasks;
-    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    if (first) PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
     if (mode == PS_MODE_CHOSEN)
         PS_CUDA(c, ps::launch_chosen(p, c->stream));
     else
         PS_CUDA(c, ps::launch_plain_fp64(p, c->stream));
     c->launches++;
-    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-    c->timed = true;
+    if (last) {
+        PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+        c->timed = true;
+    }
     return PS_OK;
 }
 
@@ -371,18 +375,46 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 }
 
 // Split (window, case) slots of one grid into groups of at most `gs` slots.
+// `used(k, s)` says whether slot (k, s) has an output.  When every selected
+// slot does, the groups take the slots window by window, so the cases of one
+// window (TT, TE, ++, -- of one spectrum) share a group.  A sparse set (some
+// outputs NULL) is grouped by the families its slots need instead: the TT
+// slots (00 family only), then the ++ and -- slots interleaved (22 family
+// only; the (++, --) slot pattern has compile-time kernels whatever the
+// windows), then the TE slots (both families), so no group generates a family
+// that only some of its slots use.
 struct Slot {
     int k, s;
 };
-static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs)
+template <typename Used>
+static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {
     std::vector<Slot> all;
+    bool dense = true;
     for (int k = 0; k < K; ++k)
         for (int s = 0; s < 4; ++s)
-            if (cases & (1u << s)) all.push_back(Slot{k, s});
+            if (cases & (1u << s)) {
+                if (used(k, s)) all.push_back(Slot{k, s});
+                else dense = false;
+            }
     std::vector<std::vector<Slot>> out;
-    for (size_t i = 0; i < all.size(); i += (size_t)gs)
-        out.emplace_back(all.begin() + i, all.begin() + std::min(all.size(), i + (size_t)gs));
+    auto chunk = [&](const std::vector<Slot>& v) {
+        for (size_t i = 0; i < v.size(); i += (size_t)gs)
+            out.emplace_back(v.begin() + i, v.begin() + std::min(v.size(), i + (size_t)gs));
+    };
+    if (dense) {
+        chunk(all);
+        return out;
+    }
+    std::vector<Slot> tt, te, pp, mm, pm;
+    for (const Slot& q : all) (q.s == PS_SPIN_00 ? tt : q.s == PS_SPIN_02 ? te : q.s == PS_SPIN_PP ? pp : mm).push_back(q);
+    for (size_t i = 0; i < std::max(pp.size(), mm.size()); ++i) {
+        if (i < pp.size()) pm.push_back(pp[i]);
+        if (i < mm.size()) pm.push_back(mm[i]);
+    }
+    chunk(tt);
+    chunk(pm);
+    chunk(te);
     return out;
 }
 
@@ -728,11 +760,12 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
     if ((st = check_mode(c, mode))) return st;
     if (cases == 0 || (cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "cases mask 0x%x must select bits 0..3", cases);
     if (K < 1 || !dW || !dM) return set_err(c, PS_ERR_ARG, "K >= 1 and W, M arrays required");
+    int nused = 0;
     for (int k = 0; k < K; ++k) {
         if (!dW[k]) return set_err(c, PS_ERR_ARG, "W[%d] is NULL", k);
-        for (int s = 0; s < 4; ++s)
-            if ((cases & (1u << s)) && !dM[4 * k + s]) return set_err(c, PS_ERR_ARG, "M[%d] is NULL", 4 * k + s);
+        for (int s = 0; s < 4; ++s) nused += (cases & (1u << s)) && dM[4 * k + s];
     }
+    if (nused == 0) return set_err(c, PS_ERR_ARG, "every selected output M[4k+s] is NULL");
     PS_CUDA(c, cudaSetDevice(c->device));
     // all K windows are padded (and split) once; each group points into them
     ps::CouplingParams base;
@@ -760,7 +793,9 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
         }
         base.wlen = wlen;
         const int gs = ps::kMaxWin;  // one generation of the families serves up to 8 slots
-        for (const auto& grp : group_slots(cases, K, gs)) {
+        const auto groups = group_slots(cases, K, gs, [&](int k, int s) { return dM[4 * k + s] != nullptr; });
+        for (size_t g = 0; g < groups.size(); ++g) {
+            const auto& grp = groups[g];
             ps::CouplingParams p = base;
             p.nwin = (int)grp.size();
             for (size_t i = 0; i < grp.size(); ++i) {
@@ -769,7 +804,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                 p.out[i] = dM[4 * grp[i].k + grp[i].s];
             }
             p.ldo = ldm;
-            if ((st = run_coupling(c, p, mode))) return st;
+            if ((st = run_coupling(c, p, mode, g == 0, g + 1 == groups.size()))) return st;
         }
     }
     return PS_OK;
@@ -783,11 +818,12 @@ int ps_mcm_set(ps_ctx* c, unsigned cases, const double* const* W, int K, int64_t
     if ((st = check_mode(c, mode))) return st;
     if (cases == 0 || (cases & ~0xFu)) return set_err(c, PS_ERR_ARG, "cases mask 0x%x must select bits 0..3", cases);
     if (K < 1 || !W || !M) return set_err(c, PS_ERR_ARG, "K >= 1 and W, M arrays required");
+    int nused = 0;
     for (int k = 0; k < K; ++k) {
         if (!W[k]) return set_err(c, PS_ERR_ARG, "W[%d] is NULL", k);
-        for (int s = 0; s < 4; ++s)
-            if ((cases & (1u << s)) && !M[4 * k + s]) return set_err(c, PS_ERR_ARG, "M[%d] is NULL", 4 * k + s);
+        for (int s = 0; s < 4; ++s) nused += (cases & (1u << s)) && M[4 * k + s];
     }
+    if (nused == 0) return set_err(c, PS_ERR_ARG, "every selected output M[4k+s] is NULL");
     PS_CUDA(c, cudaSetDevice(c->device));
     // spectra in: only the entries the families can reach (l3 <= 2 lmax)
     const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
@@ -803,7 +839,7 @@ int ps_mcm_set(ps_ctx* c, unsigned cases, const double* const* W, int K, int64_t
     std::vector<double*> dM(4 * (size_t)K, nullptr);
     std::vector<int> staged;
     for (int i = 0; i < 4 * K; ++i) {
-        if (!(cases & (1u << (i & 3)))) continue;
+        if (!(cases & (1u << (i & 3))) || !M[i]) continue;
         if (!(dM[i] = mapped_host(M[i]))) staged.push_back(i);
     }
     if (!staged.empty()) {

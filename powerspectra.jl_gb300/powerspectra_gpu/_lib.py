@@ -341,16 +341,17 @@ class Context:
                                                  dptr_array([int(x) for x in dR]), dptr_array([int(x) for x in dW]),
                                                  int(nW), lmin, lmax, mode_code(mode), dptr(int(dC)), int(ldc)))
 
-    def mcm_set(self, cases, Ws, lmin, lmax, mode="chosen", outs=None):
+    def mcm_set(self, cases, Ws, lmin, lmax, mode="chosen", outs=None, slots=None):
         """mcm for a set of host spectra on one grid: returns {(k, s): matrix} for window k and each spin
-        case s selected in `cases` (F-ordered float64; `outs` may supply them, e.g. page-locked)."""
+        case s selected in `cases` (F-ordered float64; `outs` may supply them, e.g. page-locked).  With
+        `slots` (a set of (k, s)), only those (window, case) slots are computed."""
         Ws = [np.ascontiguousarray(w, dtype=np.float64) for w in Ws]
         n = lmax - lmin + 1
         nW = min(len(w) for w in Ws)
         res, ml = {}, []
         for k in range(len(Ws)):
             for s in range(4):
-                if cases & (1 << s):
+                if cases & (1 << s) and (slots is None or (k, s) in slots):
                     m = outs[k, s] if outs is not None else np.empty((n, n), dtype=np.float64, order="F")
                     res[k, s] = m
                     ml.append(m)

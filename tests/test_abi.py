@@ -113,7 +113,12 @@ def test_bench_work_accounting_matches_oracle():
     wl = bench.workload("all_spins_3071")
     assert wl["nW"] == 6143 and sorted(wl["Ws"]) == [0, 1, 2, 3]
     # fixed accounting: 9 (00) + 16 (22) + 3 per distinct spectrum
-    assert bench.flops_per_launch(wl, 1) == 9 + 16 + 3 * 3
+    assert bench.flops_per_step(wl, 1) == 9 + 16 + 3 * 3
+    # the default workload: 20 spectra at lmax 8191, TT / ++ / -- by k % 3, 20 matrices
+    big = bench.workload("large_8191")
+    assert big["lmax"] == 8191 and big["nW"] == 16383 and len(big["windows"]) == 20
+    assert [s for _, s in big["slots"]] == [(0, 2, 3)[k % 3] for k in range(20)]
+    assert bench.flops_per_step(big, 1) == 9 + 16 + 3 * 20
 
 
 def test_result_matrix_checks_caller_outputs():

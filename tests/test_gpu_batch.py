@@ -166,3 +166,52 @@ def test_batch_launch_form_in_a_graph(ctx):
             _check(refs)
     finally:
         ctx.set_stream(0)
+
+
+@pytest.mark.parametrize("mode,tol", [("plain", 1e-12), ("chosen", 1e-6)])
+def test_mcm_set_sparse_slots(ctx, mode, tol):
+    """A set where each spectrum gets only some spin cases (NULL outputs skip their slots), like
+    the large set: TT of spectra 0, 3, ..., ++ of 1, 4, ..., -- of 2, 5, ..., and one TE slot.
+    The skipped outputs stay untouched."""
+    L, K = 70, 10
+    Ws = [_W(2 * L + 1, seed=20 + k) for k in range(K)]
+    dW = [_dev(w) for w in Ws]
+    n = L + 1
+    want = {(k, (0, 2, 3)[k % 3]) for k in range(K)} | {(4, 1)}
+    dM = {(k, s): torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda")
+          for k in range(K) for s in range(4)}
+    ptrs = [dM[k, s].data_ptr() if (k, s) in want else 0 for k in range(K) for s in range(4)]
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        ctx.mcm_set_device(0xF, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, ptrs, n, mode=mode)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_stream(0)
+    for k in range(K):
+        for s in range(4):
+            got = dM[k, s].cpu().numpy().T
+            if (k, s) not in want:
+                assert np.isnan(got).all(), (k, s)
+                continue
+            ref = o.inner_mcm(s, Ws[k], 0, L)
+            assert max_err_scaled(got, ref, cond_scale(s, Ws[k], 0, L)) < tol, (k, s)
+
+
+def test_mcm_set_host_sparse_slots(ctx):
+    """ps_mcm_set with a slot filter: only the chosen (window, case) slots are returned."""
+    L, K = 60, 4
+    Ws = [_W(2 * L + 1, seed=40 + k) for k in range(K)]
+    slots = {(0, 0), (1, 2), (2, 3), (3, 2), (3, 3)}
+    got = ctx.mcm_set(0xD, Ws, 0, L, mode="chosen", slots=slots)
+    assert set(got) == slots
+    for (k, s), M in got.items():
+        ref = o.inner_mcm(s, Ws[k], 0, L)
+        assert max_err_scaled(M, ref, cond_scale(s, Ws[k], 0, L)) < 1e-6, (k, s)
+
+
+def test_mcm_set_all_slots_null_is_an_error(ctx):
+    import powerspectra_gpu as pg
+    L = 10
+    dW = [_dev(_W(2 * L + 1, seed=1))]
+    with pytest.raises(pg.PowerSpectraArgumentError):
+        ctx.mcm_set_device(0x1, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, [0, 0, 0, 0], L + 1)
