@@ -241,12 +241,15 @@ int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best
  * no context and no allocation: its scratch (padded windows and the work list,
  * 2.6 MB) is a fixed array in the library's device image, which every GPU that
  * loads the library keeps until the process exits.  Limits: lmax <= 4095 (a
- * larger lmax returns PS_ERR_ARG); all arguments are checked as for
- * ps_mcm_multi_device.  The first call on a device looks up the array's device
- * address, so make that first call before any stream capture.  Every call
- * rewrites the whole scratch; calls whose GPU work overlaps (other streams or
- * host threads) share it and race, so serialise them.  Returns a PS_* code
- * only (there is no context to hold a message). */
+ * larger lmax returns PS_ERR_ARG); `stream` must belong to the current device
+ * (PS_ERR_ARG otherwise); all arguments are checked as for ps_mcm_multi_device.
+ * Each call made outside stream capture looks up the array's device address
+ * on the current device (so a device reset needs nothing special); a call
+ * made during stream capture reuses the address that the last uncaptured
+ * call on that device found, so make one call before capturing (PS_ERR_CUDA
+ * otherwise).  Every call rewrites the whole scratch; calls whose GPU work
+ * overlaps (other streams or host threads) share it and race, so serialise
+ * them.  Returns a PS_* code only (there is no context to hold a message). */
 int ps_mcm_multi_device_noalloc(unsigned cases, const double *const dW[4], int64_t nW, int lmin, int lmax,
                                 double *const dM[4], int64_t ldm, void *stream);
 

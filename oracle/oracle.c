@@ -56,7 +56,18 @@ static inline double sg_B(int j, int l1, int l2, int m1, int m2, int m3)
     return -(2.0 * j + 1.0) * t;
 }
 
+/* The family with the forward and backward sweeps matched at (jm_req, jm_req + 1)
+ * instead of the family's own midpoint (jm_req < 0).  A match point past
+ * jmax - 1 is clamped to jmax - 1; one before jmin leaves no forward part, and
+ * the family is then the backward sweep alone, from jmax down to jmin. */
+static int w3j_family_at(int l1, int l2, int m1, int m2, int jm_req, double *out, int *jmin_out);
+
 int or_w3j_family(int l1, int l2, int m1, int m2, double *out, int *jmin_out)
+{
+    return w3j_family_at(l1, l2, m1, m2, -1, out, jmin_out);
+}
+
+static int w3j_family_at(int l1, int l2, int m1, int m2, int jm_req, double *out, int *jmin_out)
 {
     int m3 = -m1 - m2;
     int jmin = abs(l1 - l2);
@@ -68,10 +79,22 @@ int or_w3j_family(int l1, int l2, int m1, int m2, double *out, int *jmin_out)
     memset(out, 0, sizeof(double) * (size_t)n);
     if (abs(m1) > l1 || abs(m2) > l2) return n; /* identically zero family */
 
+    int jm = jm_req < 0 ? jmin + (n - 1) / 2 : jm_req; /* match at jm and jm+1 */
+    if (jm > jmax - 1) jm = jmax - 1;
     if (n == 1) {
         out[0] = 1.0;
+    } else if (jm < jmin) {
+        /* backward only: h(jmax) = 1 down to h(jmin) */
+        double h_next = 0.0, h_cur = 1.0;
+        out[n - 1] = 1.0;
+        for (int j = jmax; j > jmin; --j) {
+            double prv = -(sg_B(j, l1, l2, m1, m2, m3) * h_cur + (double)j * sg_A(j + 1, l1, l2, m3) * h_next) /
+                         ((j + 1.0) * sg_A(j, l1, l2, m3));
+            out[j - 1 - jmin] = prv;
+            h_next = h_cur;
+            h_cur = prv;
+        }
     } else {
-        int jm = jmin + (n - 1) / 2; /* match at jm and jm+1 */
         /* forward: g(jmin) = 1, produce g up to jm+1 */
         out[0] = 1.0;
         for (int j = jmin; j <= jm; ++j) {
@@ -433,7 +456,7 @@ int or_loop_cov_abs(int kind, const double *const *S, const double *const *R, co
  * sgn = (-1)^(s1+s2+nu1+nu2).  Xi is dense column-major (lmax+1)^2; entries
  * outside the band are left untouched. */
 static int quickpol_xi_impl(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
-                            double *Xi, long ldx, int nthreads, int absmode)
+                            double *Xi, long ldx, int nthreads, int absmode, int common)
 {
     if (lmax < 0 || bl < 0 || bu < 0 || ldx < lmax + 1) return 1;
     int nt = nthreads_or_default(nthreads);
@@ -454,9 +477,16 @@ static int quickpol_xi_impl(int nu1, int nu2, int s1, int s2, const double *W, l
             int lo = lpp - bl > 2 ? lpp - bl : 2, hi = lpp + bu < lmax ? lpp + bu : lmax;
             for (int l = lo; l <= hi; ++l) {
                 /* (l' l l''; s+nu, -s, -nu) = (l l'' l'; -s, -nu, s+nu): the family over the third column */
-                int j1, j2;
-                int n1 = or_w3j_family(l, lpp, -s1, -nu1, f1, &j1);
-                int n2 = or_w3j_family(l, lpp, -s2, -nu2, f2, &j2);
+                int j1, j2, jm = -1;
+                if (common) {
+                    /* both families matched at one point: the larger of their midpoints */
+                    int jmax = l + lpp, a1 = abs(s1 + nu1), a2 = abs(s2 + nu2), d = abs(l - lpp);
+                    int jmin1 = d > a1 ? d : a1, jmin2 = d > a2 ? d : a2;
+                    int m1 = (jmin1 + jmax) / 2, m2 = (jmin2 + jmax) / 2;
+                    jm = m1 > m2 ? m1 : m2;
+                }
+                int n1 = w3j_family_at(l, lpp, -s1, -nu1, jm, f1, &j1);
+                int n2 = w3j_family_at(l, lpp, -s2, -nu2, jm, f2, &j2);
                 int a = j1 > j2 ? j1 : j2;
                 int b1 = j1 + n1 - 1, b2 = j2 + n2 - 1;
                 int b = b1 < b2 ? b1 : b2;
@@ -478,12 +508,24 @@ static int quickpol_xi_impl(int nu1, int nu2, int s1, int s2, const double *W, l
 int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu, double *Xi,
                    long ldx, int nthreads)
 {
-    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 0);
+    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 0, 0);
 }
 
 /* The same sums over |W f1 f2| (the sum of |terms| behind each element). */
 int or_quickpol_xi_abs(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
                        double *Xi, long ldx, int nthreads)
 {
-    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 1);
+    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 1, 0);
+}
+
+/* quickpolXi! with both families of an element matched at one common point, the
+ * larger of their midpoints (each family's forward sweep from its own jmin, one
+ * backward sweep from the common jmax; a family whose support starts past that
+ * point is the backward sweep alone).  The same 3j values as or_quickpol_xi up
+ * to the recurrences' conditioning; this is the match the GPU kernel uses, so
+ * the two agree to rounding. */
+int or_quickpol_xi_common(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
+                          double *Xi, long ldx, int nthreads)
+{
+    return quickpol_xi_impl(nu1, nu2, s1, s2, W, nW, lmax, bl, bu, Xi, ldx, nthreads, 0, 1);
 }

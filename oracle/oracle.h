@@ -43,6 +43,9 @@ int or_quickpol_xi(int nu1, int nu2, int s1, int s2, const double *W, long nW, i
 /* The same sums over |W f1 f2|: the sum of |terms| behind each element. */
 int or_quickpol_xi_abs(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
                        double *Xi, long ldx, int nthreads);
+/* or_quickpol_xi with both families matched at the larger of their midpoints (the GPU kernel's match). */
+int or_quickpol_xi_common(int nu1, int nu2, int s1, int s2, const double *W, long nW, int lmax, int bl, int bu,
+                          double *Xi, long ldx, int nthreads);
 
 int or_cov_nwindows(int kind);
 int or_max_threads(void);

@@ -59,6 +59,8 @@ def _load():
         lib.or_quickpol_xi.restype = ci
         lib.or_quickpol_xi_abs.argtypes = [ci, ci, ci, ci, dp, cl, ci, ci, ci, dp, cl, ci]
         lib.or_quickpol_xi_abs.restype = ci
+        lib.or_quickpol_xi_common.argtypes = [ci, ci, ci, ci, dp, cl, ci, ci, ci, dp, cl, ci]
+        lib.or_quickpol_xi_common.restype = ci
         lib.or_xi.argtypes = [ci, ci, dp, cl, ci, ci, dp, cl, ci]
         lib.or_xi.restype = ci
         lib.or_loop_cov.argtypes = [ci, ctypes.POINTER(dp), ctypes.POINTER(dp), ctypes.POINTER(dp), cl, ci, ci, dp, cl,
@@ -159,14 +161,18 @@ def l3_terms(lmin, lmax, nW, rows=None):
     return _load().or_l3_terms(lmin, lmax, nW, rp, nr)
 
 
-def quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, nthreads=0, absolute=False):
+def quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, nthreads=0, absolute=False, common_match=False):
     """quickpolXi! (src/beam.jl:72-109) as a dense (lmax+1)^2 matrix, zeros outside the band.
-    absolute=True: the sums over |W f1 f2| (sum of |terms|, no sign)."""
+    absolute=True: the sums over |W f1 f2| (sum of |terms|, no sign).  common_match=True: both
+    families of an element matched at the larger of their midpoints, as the GPU kernel does (the
+    default matches each family at its own midpoint)."""
     lib = _load()
     W = np.ascontiguousarray(W, dtype=np.float64)
     n = lmax + 1
     X = np.zeros((n, n), dtype=np.float64, order="F")
-    fn = lib.or_quickpol_xi_abs if absolute else lib.or_quickpol_xi
+    if absolute and common_match:
+        raise ValueError("absolute sums do not depend on the match point")
+    fn = lib.or_quickpol_xi_abs if absolute else (lib.or_quickpol_xi_common if common_match else lib.or_quickpol_xi)
     st = fn(int(nu1), int(nu2), int(s1), int(s2), _dptr(W), len(W), lmax, bl, bu, _dptr(X), n,
                             nthreads)
     if st:

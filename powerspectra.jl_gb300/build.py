@@ -31,7 +31,8 @@ def _stale(srcs, target):
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)
-    deps = srcs + glob.glob(os.path.join(CSRC, "*.cuh")) + [os.path.join(HERE, "..", "include", "powerspectra_gpu.h")]
+    deps = srcs + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
+        [os.path.join(HERE, "..", "include", "powerspectra_gpu.h")]
     return any(os.path.getmtime(s) > t for s in deps if os.path.exists(s))
 
 

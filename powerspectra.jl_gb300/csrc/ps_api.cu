@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "ps_internal.cuh"
+#include "ps_tiles.h"
 
 // Dense solves (ps_linalg.cu)
 struct ps_linalg;
@@ -148,27 +149,15 @@ static void row_task_list(int lmin, int lmax, std::vector<int2>& t)
         for (int l2 = l1; l2 <= lmax; l2 += 32) t.push_back(make_int2(l1, l2));
 }
 
-// The chosen kernel's warp tasks, in tiles of kTileRows (one block).  Rows and
-// columns are counted from o = lmax + 1 - 32 nb (nb = ceil(n / 32)), so that
-// the last 32-column block ends at lmax: tile (g, b) holds rows o + 4g ..
-// o + 4g + 3 (l1 = -1 below lmin) over the 32 columns from l2_0 = o + 32 b,
-// for b from the block that holds row o + 4g to the last.  Every row then has
-// the same warp tasks as 32-column steps from l1 would give, and the only idle
-// lanes are those left of the diagonal.  Row groups from the top (longest
-// families first).  The kernel writes each tile's row halves as runs of four
-// doubles.
+// The chosen kernel's warp tasks, in tiles of kTileRows (one block): the
+// closed-form list of ps_tiles.h.  The kernel writes each tile's row halves as
+// runs of four doubles.
 static void tile_task_list(int lmin, int lmax, std::vector<int2>& t)
 {
     static_assert(ps::kTileRows == 4 && 32 % ps::kTileRows == 0, "tiles of four rows inside one 32-column block");
-    const int n = lmax - lmin + 1, NB = (n + 31) / 32, o = lmax + 1 - 32 * NB, glo = (lmin - o) / 4;
     t.clear();
-    t.reserve((size_t)32 * NB * NB);
-    for (int g = 8 * NB - 1; g >= glo; --g)
-        for (int b = g / 8; b < NB; ++b)
-            for (int q = 0; q < 4; ++q) {
-                const int l1 = o + 4 * g + q;
-                t.push_back(make_int2(l1 >= lmin ? l1 : -1, o + 32 * b));
-            }
+    t.reserve((size_t)ps_tiles::task_count(lmin, lmax));
+    ps_tiles::for_each_task(lmin, lmax, [&](int l1, int l2_0) { t.push_back(make_int2(l1, l2_0)); });
 }
 
 static int upload_tasks(ps_ctx* c, const std::vector<int2>& t, int2** d, size_t* cap)

@@ -14,7 +14,9 @@
 // has to start at zero, but every call on a device shares this one array:
 // calls whose GPU work overlaps (on different streams or threads) race.
 #include "ps_internal.cuh"
+#include "ps_tiles.h"
 
+#include <atomic>
 #include <stdint.h>
 #include <string.h>
 
@@ -22,46 +24,58 @@ namespace {
 
 constexpr int kNoAllocMaxLmax = 4095;  // largest lmax the fixed scratch serves
 constexpr int kNoAllocMaxWlen = 2 * kNoAllocMaxLmax + 2;
-constexpr int kNoAllocMaxTasks = (kNoAllocMaxLmax + 1) * (kNoAllocMaxLmax + 2) / 64 + kNoAllocMaxLmax + 1;
-// (the tiled list at lmax 4095, lmin 0 holds 264192 tasks; fewer for any smaller range)
+// The task list is longest for lmin = 0 (n = 4096 rows, 128 column blocks, all
+// 1024 row groups); any other range with lmax <= 4095 has at most as many tiles.
+constexpr long long kNoAllocMaxTasks = ps_tiles::task_count(0, kNoAllocMaxLmax);
+static_assert(kNoAllocMaxTasks == 264192, "4 tasks per tile, 66048 tiles at lmax 4095");
 
 // windows: 4 x wlen doubles, split copies: 4 x wlen int2, tasks: int2 each
 constexpr size_t kWinBytes = 4ull * kNoAllocMaxWlen * sizeof(double);
 constexpr size_t kBfBytes = 4ull * kNoAllocMaxWlen * sizeof(int2);
 constexpr size_t kTaskBytes = (size_t)kNoAllocMaxTasks * sizeof(int2);
 constexpr size_t kScratchBytes = kWinBytes + kBfBytes + kTaskBytes;  // 2.6 MB
+static_assert(kWinBytes % 256 == 0 && kBfBytes % 256 == 0, "each scratch region starts 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// Device address of g_scratch per device, looked up once with that device current.
+// Device address of g_scratch per device.  It is looked up with the device
+// current on every call whose stream is not capturing (cheap, and correct
+// again after a device reset reloads the library image); a call made during
+// stream capture uses the address the last uncaptured call on that device
+// found.  Atomic, so host threads may make their first calls concurrently.
 constexpr int kMaxDevices = 64;
-static void* g_scratch_addr[kMaxDevices];
+static std::atomic<void*> g_scratch_addr[kMaxDevices];
 
-// The chosen kernel's tiled task list (the context path builds the same on
-// the host): with nb = ceil(n / 32) and o = lmax + 1 - 32 nb, tile (g, b)
-// holds rows o + 4g .. o + 4g + 3 (l1 = -1 below lmin) over the 32 columns
-// from o + 32 b, b = g / 8 .. nb - 1, for row groups g from 8 nb - 1 down to
-// (lmin - o) / 4.  tiles_below(m, nb) counts the tiles of row groups 0 .. m - 1:
-// the sum of nb - g / 8 over g < m.
-__host__ __device__ inline long long tiles_below(long long m, long long nb)
-{
-    const long long q = m / 8, r = m % 8;
-    return m * nb - (4 * q * (q - 1) + r * q);
-}
-
-// One thread per row group writes its tiles' tasks.
+// One thread per row group writes its tiles' tasks (the list of ps_tiles.h).
 __global__ void k_fill_tiles(int2* __restrict__ tasks, int lmin, int lmax)
 {
-    const int n = lmax - lmin + 1, NB = (n + 31) / 32, o = lmax + 1 - 32 * NB, glo = (lmin - o) / 4;
-    const long long top = tiles_below(8LL * NB, NB);
-    for (int g = glo + blockIdx.x * blockDim.x + threadIdx.x; g < 8 * NB; g += gridDim.x * blockDim.x) {
-        long long t = top - tiles_below(g + 1, NB);  // groups above g come first
-        for (int b = g / 8; b < NB; ++b, ++t)
-            for (int q = 0; q < 4; ++q) {
-                const int l1 = o + 4 * g + q;
-                tasks[4 * t + q] = make_int2(l1 >= lmin ? l1 : -1, o + 32 * b);
+    const ps_tiles::Geometry G = ps_tiles::geometry(lmin, lmax);
+    for (int g = G.glo + blockIdx.x * blockDim.x + threadIdx.x; g < 8 * G.nb; g += gridDim.x * blockDim.x) {
+        long long t = ps_tiles::group_offset(G, g);
+        for (int b = g / 8; b < G.nb; ++b)
+            for (int q = 0; q < 4; ++q, ++t) {
+                const int l1 = G.o + 4 * g + q;
+                tasks[t] = make_int2(l1 >= lmin ? l1 : -1, G.o + 32 * b);
             }
     }
+}
+
+// The scratch address on the current device `dev`, or nullptr.
+void* scratch_address(int dev, cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return g_scratch_addr[dev].load();
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_scratch) != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    g_scratch_addr[dev].store(ptr);
+    return ptr;
 }
 
 }  // namespace
@@ -74,26 +88,26 @@ extern "C" int ps_mcm_multi_device_noalloc(unsigned cases, const double* const d
     if (lmax > kNoAllocMaxLmax) return PS_ERR_ARG;  // beyond what the fixed scratch holds
     for (int s = 0; s < 4; ++s)
         if ((cases & (1u << s)) && (!dW[s] || !dM[s])) return PS_ERR_ARG;
+    const long long ntasks = ps_tiles::task_count(lmin, lmax);
+    if (ntasks > kNoAllocMaxTasks) return PS_ERR_ARG;  // bounded by the static_assert above for lmax <= 4095
 
-    int dev = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sdev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
         return PS_ERR_CUDA;
     }
-    // First call on this device: find where g_scratch lives in its memory.
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_scratch) != cudaSuccess || !ptr) {
-            cudaGetLastError();
-            return PS_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = ptr;
+    // the scratch lives on the current device: a stream of another device is an argument error
+    if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+        cudaGetLastError();
+        return PS_ERR_ARG;
     }
-    unsigned char* base = (unsigned char*)g_scratch_addr[dev];
+    if (sdev != dev) return PS_ERR_ARG;
+    unsigned char* base = (unsigned char*)scratch_address(dev, s);
+    if (!base) return PS_ERR_CUDA;  // no lookup yet on this device (first call made during capture) or CUDA error
     double* win = (double*)base;
     int2* bf = (int2*)(base + kWinBytes);
     int2* tasks = (int2*)(base + kWinBytes + kBfBytes);
-    cudaStream_t s = (cudaStream_t)stream;
 
     ps::CouplingParams p;
     memset(&p, 0, sizeof(p));
@@ -122,10 +136,8 @@ extern "C" int ps_mcm_multi_device_noalloc(unsigned cases, const double* const d
         ++K;
     }
     p.nwin = K;
-    const int rows = lmax - lmin + 1, nb = (rows + 31) / 32, glo = (lmin - (lmax + 1 - 32 * nb)) / 4;
-    const int groups = 8 * nb - glo;
-    const long long ntasks = 4 * (tiles_below(8LL * nb, nb) - tiles_below(glo, nb));
-    if (ntasks > kNoAllocMaxTasks) return PS_ERR_ARG;  // cannot happen for lmax <= kNoAllocMaxLmax
+    const ps_tiles::Geometry G = ps_tiles::geometry(lmin, lmax);
+    const int groups = 8 * G.nb - G.glo;
     k_fill_tiles<<<(groups + 255) / 256, 256, 0, s>>>(tasks, lmin, lmax);
     if (cudaGetLastError() != cudaSuccess) return PS_ERR_CUDA;
     p.tasks = tasks;

@@ -208,3 +208,19 @@ def test_quickpolW_is_alm2cl_times_2l_plus_1():
         direct = abs(a[o.alm_index(l, 0, lmax)]) ** 2 + sum(2 * abs(a[o.alm_index(l, m, lmax)]) ** 2
                                                             for m in range(1, l + 1))
         assert abs(W[l] - direct) < 1e-12 * direct
+
+
+def test_quickpol_common_match_agrees_with_own_midpoints():
+    """The oracle's two QuickPol matches (each family at its own midpoint, as a family fill does;
+    both families at the larger midpoint, as the GPU kernel does) give the same Xi up to the
+    recurrences' conditioning, relative to the sum of |W f1 f2| behind each element."""
+    rng = np.random.default_rng(5)
+    lmax, bl, bu = 150, 12, 7
+    W = rng.random(2 * lmax + 1) * np.exp(-np.arange(2 * lmax + 1) / 60.0)
+    for (nu1, nu2, s1, s2) in ((0, 0, 2, 2), (1, -1, 2, 0), (-3, 1, 2, -2), (4, -4, 0, 2)):
+        A = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu)
+        B = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, common_match=True)
+        S = o.quickpol_xi(nu1, nu2, s1, s2, W, lmax, bl, bu, absolute=True)
+        m = S > 0
+        assert np.max(np.abs(A - B)[m] / S[m]) < 1e-9, (nu1, nu2, s1, s2)
+        assert np.array_equal(A == 0, B == 0)  # the same band and the same zero families

@@ -30,15 +30,31 @@ def _noalloc_fn():
     return fn, L
 
 
-def _case(L, lmin, seed):
+def _case(L, lmin, seed, cases=0xF):
     from powerspectra_gpu import synthetic as syn
     nW = 2 * L + 1
     Ws = [syn.mask_spectrum(nW, 0.5 + 0.1 * s, 0.3 * L + 20, seed=seed + s) for s in range(4)]
     n = L - lmin + 1
     dW = [torch.tensor(w, device="cuda") for w in Ws]
-    outs_new = [torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda") for _ in range(4)]
-    outs_ref = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+    used = [s for s in range(4) if cases & (1 << s)]
+    outs_new = {s: torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda") for s in used}
+    outs_ref = {s: torch.zeros((n, n), dtype=torch.float64, device="cuda") for s in used}
     return nW, n, dW, outs_new, outs_ref
+
+
+def _compare(fn, L, ctx, stream, lmax, lmin, seed, cases):
+    nW, n, dW, new, ref = _case(lmax, lmin, seed, cases)
+    ptr = lambda d: L.dptr_array([d[s].data_ptr() if s in d else 0 for s in range(4)])
+    st = fn(cases, L.dptr_array([d.data_ptr() for d in dW]), nW, lmin, lmax, ptr(new), n,
+            ctypes.c_void_p(stream.cuda_stream))
+    assert st == 0
+    ctx.mcm_multi_device({s: dW[s].data_ptr() for s in new}, nW, lmin, lmax, {s: ref[s].data_ptr() for s in ref}, n,
+                         mode="chosen")
+    torch.cuda.synchronize()
+    for s in new:
+        a, b = new[s].cpu().numpy(), ref[s].cpu().numpy()
+        assert np.all(np.isfinite(a)), (lmax, lmin, s)  # every element written (NaN sentinel)
+        assert max_err_scaled(a, b, np.abs(b)) < TOL, (lmax, lmin, s)
 
 
 def test_noalloc_matches_context_path_twice(ctx):
@@ -47,17 +63,20 @@ def test_noalloc_matches_context_path_twice(ctx):
     ctx.set_stream(stream.cuda_stream)
     try:
         for (lmax, lmin, seed) in ((300, 0, 11), (173, 2, 29)):
-            nW, n, dW, new, ref = _case(lmax, lmin, seed)
-            st = fn(0xF, L.dptr_array([d.data_ptr() for d in dW]), nW, lmin, lmax,
-                    L.dptr_array([m.data_ptr() for m in new]), n, ctypes.c_void_p(stream.cuda_stream))
-            assert st == 0
-            ctx.mcm_multi_device({s: dW[s].data_ptr() for s in range(4)}, nW, lmin, lmax,
-                                 {s: ref[s].data_ptr() for s in range(4)}, n, mode="chosen")
-            torch.cuda.synchronize()
-            for s in range(4):
-                a, b = new[s].cpu().numpy(), ref[s].cpu().numpy()
-                assert np.all(np.isfinite(a))
-                assert max_err_scaled(a, b, np.abs(b)) < TOL, (lmax, s)
+            _compare(fn, L, ctx, stream, lmax, lmin, seed, 0xF)
+    finally:
+        ctx.set_stream(0)
+
+
+@pytest.mark.parametrize("lmin", [0, 37])
+def test_noalloc_at_its_largest_lmax(ctx, lmin):
+    """lmax 4095, the limit of the fixed scratch: with lmin = 0 the windows, their split copies
+    and the task list fill their regions completely (264192 tasks)."""
+    fn, L = _noalloc_fn()
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    try:
+        _compare(fn, L, ctx, stream, 4095, lmin, 3 + lmin, 0x1)
     finally:
         ctx.set_stream(0)
 
