@@ -426,6 +426,27 @@ def run_ours(args):
         del pM
 
     # end to end through the host-pointer ABI: pinned spectra in, pinned matrices out, every step
+    e2e = None
+    if args.no_e2e:
+        pass
+    else:
+        e2e = _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    return _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, value, clk, launches, plain,
+                   decoupled, e2e, dist)
+
+
+def _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements):
+    """e2e leg: the host-pointer ABI call with pinned spectra in and pinned matrices out."""
+    import numpy as np
+    import torch
+    lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
+    n = lmax - lmin + 1
+    slots = wl["slots"]
+    mode = args.mode
     hW = [torch.from_numpy(np.ascontiguousarray(w)).pin_memory().numpy() for w in wl["windows"]]
     hM = {sl: torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy().T for sl in slots}  # F-ordered
     ctx.set_stream(0)
@@ -449,12 +470,13 @@ def run_ours(args):
            "call": "ps_mcm_multi" if wl["kind"] == "multi" else "ps_mcm_set",
            "how": "pinned host spectra in; pinned host matrices out, written by the kernel in place"}
     del hM
+    return e2e
 
-    if rank != 0:
-        if dist is not None:
-            dist.destroy_process_group()
-        return 0
 
+def _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, value, clk, launches, plain, decoupled,
+            e2e, dist):
+    lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
+    slots = wl["slots"]
     terms = l3_terms(lmin, lmax, nW)
     fl = flops_per_step(wl, terms)
     kms = statistics.mean(kernel_ms)
@@ -882,6 +904,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain FP64 kernel")
     ap.add_argument("--no-decoupled", action="store_true", help="skip the decoupled-spectrum error leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--lmax", type=int, default=0,
                     help="window_W_8191 and large_8191: another lmax (a smaller case for profiling)")
     args = ap.parse_args()
