@@ -384,6 +384,31 @@ def run_ours(args):
     elements = len(slots) * n * n
     value = world * elements * args.steps / elapsed
 
+    # the same chosen-mode call with the tensor-core kernels switched off (CUDA-core contraction in
+    # groups of up to 8 slots): two timed steps, for the comparison of the two contraction paths
+    cuda_cores = None
+    if mode == "chosen" and wl["kind"] == "set" and not args.no_plain:
+        ctx.set_tensor_cores(False)
+        step(outp=mptr)
+        ck = []
+        barrier()
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        for _ in range(2):
+            flush.zero_()
+            step(outp=mptr)
+            ck.append(ctx.last_kernel_ms())
+        c1.record(stream)
+        barrier()
+        ctx.set_tensor_cores(True)
+        cel = max_over_ranks(c0.elapsed_time(c1) / 1e3)
+        cuda_cores = {"value": world * elements * 2 / cel, "unit": UNIT, "ms_per_step": cel / 2 * 1e3,
+                      "kernel_ms_per_step": statistics.mean(ck), "steps": 2,
+                      "what": "the same ps_mcm_set_device call with ps_set_tensor_cores(ctx, 0)"}
+        step(outp=mptr)  # the timed path's results again, for the accuracy legs below
+        torch.cuda.synchronize()
+
     # the plain FP64 kernels on the same workload (the chosen form's comparison point): one timed
     # step (the kernels run for seconds, so no warm-up), then every chosen matrix against it
     plain = decoupled = None
@@ -436,7 +461,7 @@ def run_ours(args):
             dist.destroy_process_group()
         return 0
     return _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, value, clk, launches, plain,
-                   decoupled, e2e, dist)
+                   decoupled, e2e, dist, cuda_cores)
 
 
 def _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements):
@@ -474,7 +499,7 @@ def _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements):
 
 
 def _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, value, clk, launches, plain, decoupled,
-            e2e, dist):
+            e2e, dist, cuda_cores=None):
     lmin, lmax, nW = wl["lmin"], wl["lmax"], wl["nW"]
     slots = wl["slots"]
     terms = l3_terms(lmin, lmax, nW)
@@ -501,6 +526,9 @@ def _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, valu
                        "l2": "256 MiB buffer written between timed steps"},
             "roofline": roofline, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
             "fma_peaks_tflops": {"fp64": peak64 / 1e12, "fp32": peak32 / 1e12}}
+    if cuda_cores is not None:
+        line["cuda_core_contraction"] = cuda_cores
+        line["cuda_core_contraction"]["tensor_core_over_cuda_core"] = value / cuda_cores["value"]
     if plain is not None:
         line["plain_fp64"] = plain
     if decoupled is not None:

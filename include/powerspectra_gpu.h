@@ -132,6 +132,13 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
+/* In chosen mode, the TT slots of a set with at least 5 of them, and its ++
+ * and -- slots when there are at least 5 of those, are computed by the
+ * tensor-core kernels: one generation of the (0 0 0) or (2 -2 0) family for
+ * up to 15 windows, contracted by BF16 tcgen05 MMAs in a three-part split with
+ * FP32 accumulators and float-float totals (same 1e-6 bar).  Their waits on
+ * the tensor core are bounded: a wait that gives up is reported as
+ * PS_ERR_TIMEOUT by the next ps_synchronize or host-pointer call. */
 /* The same with host spectra and host matrices: returns when every M is
  * filled (page-locked matrices are written by the kernel in place). */
 int ps_mcm_set(ps_ctx *ctx, unsigned cases, const double *const *W, int K, int64_t nW, int lmin, int lmax, int mode,
@@ -252,6 +259,10 @@ int ps_batch_autotune(ps_ctx *ctx, const ps_problem *probs, int nprob, int *best
  * them.  Returns a PS_* code only (there is no context to hold a message). */
 int ps_mcm_multi_device_noalloc(unsigned cases, const double *const dW[4], int64_t nW, int lmin, int lmax,
                                 double *const dM[4], int64_t ldm, void *stream);
+
+/* Chosen-mode sets use the tensor-core kernels where they apply (enable = 1,
+ * the default) or the CUDA-core kernels only (enable = 0). */
+int ps_set_tensor_cores(ps_ctx *ctx, int enable);
 
 /* Instrumentation: device time of the coupling kernels of the last call (CUDA
  * events on the launching stream, from the first coupling launch of the call

@@ -79,6 +79,13 @@ struct ps_ctx {
         int2* d_tasks = nullptr;
     } batch;
     int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
+    // tensor-core kernels: their block list for the current (lmin, lmax) and the status of their bounded waits
+    int2* d_mtiles = nullptr;
+    size_t mtiles_cap = 0;
+    int nmtiles = 0, mtile_lmin = -1, mtile_lmax = -1;
+    unsigned* d_status = nullptr;
+    bool status_pending = false;  // a tensor-core launch whose status is not yet checked
+    bool tensor_cores = true;
     ps_linalg* la = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool timed = false;
@@ -202,6 +209,35 @@ static int ensure_tiles(ps_ctx* c, int lmin, int lmax)
     c->ntiles = (int)t.size();
     c->tile_lmin = lmin;
     c->tile_lmax = lmax;
+    return PS_OK;
+}
+
+namespace ps {
+void mma_tile_list(int lmin, int lmax, std::vector<int2>& t);  // ps_mma.cu
+}
+
+static int ensure_mtiles(ps_ctx* c, int lmin, int lmax)
+{
+    if (c->mtile_lmin == lmin && c->mtile_lmax == lmax && c->d_mtiles) return PS_OK;
+    std::vector<int2> t;
+    ps::mma_tile_list(lmin, lmax, t);
+    c->mtile_lmin = c->mtile_lmax = -1;
+    if (int st = upload_tasks(c, t, &c->d_mtiles, &c->mtiles_cap)) return st;
+    c->nmtiles = (int)t.size();
+    c->mtile_lmin = lmin;
+    c->mtile_lmax = lmax;
+    return PS_OK;
+}
+
+// Status of the tensor-core kernels' bounded waits since the last check (the
+// stream must have been synchronised).
+static int check_status(ps_ctx* c)
+{
+    if (!c->status_pending || !c->d_status) return PS_OK;
+    unsigned h = 0;
+    PS_CUDA(c, cudaMemcpy(&h, c->d_status, sizeof(h), cudaMemcpyDeviceToHost));
+    c->status_pending = false;
+    if (h) return set_err(c, PS_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its MMAs (status %u)", h);
     return PS_OK;
 }
 
@@ -375,6 +411,8 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 struct Slot {
     int k, s;
 };
+// Fewest slots of one kind (TT, or ++ and --) for which a chosen-mode set takes a tensor-core kernel.
+constexpr int kMmaMinSlots = 5;
 template <typename Used>
 static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {
@@ -490,6 +528,8 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_alm);
     cudaFree(c->d_part);
     cudaFree(c->d_qp);
+    cudaFree(c->d_mtiles);
+    cudaFree(c->d_status);
     cudaFreeHost(c->h_pack);
     batch_release(c);
     ps_linalg_free(c->la);
@@ -513,6 +553,13 @@ int ps_synchronize(ps_ctx* c)
     if (!c) return PS_ERR_ARG;
     PS_CUDA(c, cudaSetDevice(c->device));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_status(c);
+}
+
+int ps_set_tensor_cores(ps_ctx* c, int enable)
+{
+    if (!c) return PS_ERR_ARG;
+    c->tensor_cores = enable != 0;
     return PS_OK;
 }
 
@@ -781,8 +828,61 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
             }
         }
         base.wlen = wlen;
+        // chosen mode: the TT slots (00 family) and the ++ / -- slots (22 family) of a set, each
+        // kind with at least kMmaMinSlots slots, go to the tensor-core kernels, up to kMmaMaxSlots
+        // windows per launch
+        std::vector<Slot> mma00, mma22;
+        if (mode == PS_MODE_CHOSEN && c->tensor_cores)
+            for (int k = 0; k < K; ++k)
+                for (int s = 0; s < 4; ++s)
+                    if ((cases & (1u << s)) && dM[4 * k + s] && s != PS_SPIN_02)
+                        (s == PS_SPIN_00 ? mma00 : mma22).push_back(Slot{k, s});
+        if ((int)mma00.size() < kMmaMinSlots) mma00.clear();
+        if ((int)mma22.size() < kMmaMinSlots) mma22.clear();
         const int gs = ps::kMaxWin;  // one generation of the families serves up to 8 slots
-        const auto groups = group_slots(cases, K, gs, [&](int k, int s) { return dM[4 * k + s] != nullptr; });
+        const auto groups = group_slots(cases, K, gs, [&](int k, int s) {
+            if (!dM[4 * k + s]) return false;
+            if (s == PS_SPIN_00) return mma00.empty();
+            return s == PS_SPIN_02 || mma22.empty();
+        });
+        PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+        if (!mma00.empty() || !mma22.empty()) {
+            if ((st = ensure_mtiles(c, lmin, lmax))) return st;
+            if (!c->d_status) {
+                cudaError_t e = cudaMalloc((void**)&c->d_status, sizeof(unsigned));
+                if (e != cudaSuccess) {
+                    cudaGetLastError();
+                    c->d_status = nullptr;
+                    return set_err(c, PS_ERR_OOM, "cudaMalloc of the status word failed: %s", cudaGetErrorString(e));
+                }
+            }
+            if (!c->status_pending) PS_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(unsigned), c->stream));
+            c->status_pending = true;
+        }
+        for (const std::vector<Slot>* list : {&mma00, &mma22}) {
+            for (size_t i0 = 0; i0 < list->size(); i0 += ps::kMmaMaxSlots) {
+                ps::MmaParams mp;
+                memset(&mp, 0, sizeof(mp));
+                mp.lmin = lmin;
+                mp.lmax = lmax;
+                mp.nslot = (int)std::min(list->size() - i0, (size_t)ps::kMmaMaxSlots);
+                for (int i = 0; i < mp.nslot; ++i) {
+                    const Slot q = (*list)[i0 + i];
+                    mp.bf[i] = descs[q.k].bf;
+                    mp.wW[i] = descs[q.k].wW;
+                    mp.parity[i] = q.s == PS_SPIN_00 ? ps::PAR_ALL : (q.s == PS_SPIN_PP ? ps::PAR_EVEN : ps::PAR_ODD);
+                    mp.out[i] = dM[4 * q.k + q.s];
+                }
+                mp.ldo = ldm;
+                mp.wlen = wlen;
+                mp.epilogue = ps::EPI_MCM;
+                mp.tiles = c->d_mtiles;
+                mp.ntiles = c->nmtiles;
+                mp.status = c->d_status;
+                PS_CUDA(c, ps::launch_mma(mp, list == &mma00, c->stream));
+                c->launches++;
+            }
+        }
         for (size_t g = 0; g < groups.size(); ++g) {
             const auto& grp = groups[g];
             ps::CouplingParams p = base;
@@ -793,8 +893,10 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                 p.out[i] = dM[4 * grp[i].k + grp[i].s];
             }
             p.ldo = ldm;
-            if ((st = run_coupling(c, p, mode, g == 0, g + 1 == groups.size()))) return st;
+            if ((st = run_coupling(c, p, mode, false, false))) return st;
         }
+        PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+        c->timed = true;
     }
     return PS_OK;
 }
@@ -840,7 +942,7 @@ int ps_mcm_set(ps_ctx* c, unsigned cases, const double* const* W, int K, int64_t
         PS_CUDA(c, cudaMemcpy2DAsync(M[i], (size_t)ldm * sizeof(double), dM[i], (size_t)ldm * sizeof(double),
                                      n * sizeof(double), n, cudaMemcpyDeviceToHost, c->stream));
     PS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return PS_OK;
+    return check_status(c);
 }
 
 int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int bps)

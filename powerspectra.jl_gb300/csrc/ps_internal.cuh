@@ -112,6 +112,29 @@ int alm2cl_chunks(int mmax);
 cudaError_t launch_alm2cl(const AlmParams& p, double scale, bool per_l, double* W, cudaStream_t s,
                           cudaEvent_t after_partial = nullptr);
 
+// Tensor-core coupling kernels for sets of windows (ps_mma.cu): up to
+// kMmaMaxSlots windows per launch, all with the squared (2 -2 0) family (each
+// with a parity) or all with the squared (0 0 0) family (PAR_ALL), contracted
+// on the tensor cores; one more MMA column forms the normalisation.
+constexpr int kMmaCols = 16;
+constexpr int kMmaMaxSlots = kMmaCols - 1;
+struct MmaParams {
+    int lmin, lmax;
+    int nslot;                          // 1 .. kMmaMaxSlots
+    const int2* bf[kMmaMaxSlots];       // split windows (mantissa, exponent), length wlen
+    const double* wW[kMmaMaxSlots];     // padded windows (2 l3 + 1) W[l3]: the last forward point in FP64
+    int parity[kMmaMaxSlots];           // PAR_ALL / PAR_EVEN / PAR_ODD of l1 + l2 + l3
+    double* out[kMmaMaxSlots];
+    long long ldo;
+    int wlen;
+    int epilogue;                       // EPI_MCM or EPI_XI
+    const int2* tiles;                  // (r0, c0): rows r0 + 2w, columns c0 + 2i
+    int ntiles;
+    unsigned* status;                   // set to 1 when a bounded wait gives up
+};
+// fam00: the (0 0 0) family (every slot PAR_ALL); otherwise the (2 -2 0) family
+cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s);
+
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);
 int cov_nratios(int kind);

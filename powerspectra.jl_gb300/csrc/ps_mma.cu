@@ -1,0 +1,453 @@
+// ps_mma.cu -- coupling kernels for sets of windows with the window
+// contraction on the tensor cores (tcgen05, BF16 in, FP32 out).
+//
+// One launch computes up to 15 windows of one family product with ONE
+// generation of the family per pair, where the chosen kernel contracts at most
+// 8 windows per generation on the CUDA cores:
+//   * the (2 -2 0) family squared, with each window's parity of l1 + l2 + l3:
+//     M++ (EE/BB diagonal blocks, even), M-- (off-diagonal, odd) and the
+//     all-parity Xi (src/modecoupling.jl:123-159 per window);
+//   * the (0 0 0) family squared: M00, TT (src/modecoupling.jl:78-95).
+// (src/covariance.jl:92-183 contracts 8 windows against one family.)
+//
+// Mapping.  A block holds 4 rows l1 = r0 + 2w (one per warp) and 32 columns
+// l2 = c0 + 2i (one per lane): 128 pairs, the M = 128 rows of the MMA.  The
+// sweeps run in registers in float-float arithmetic as in the chosen kernel,
+// but time-skewed: at time step tau, lane (w, i) takes forward step
+// tF = tau - 6 - 2i + 2w (point l3 = l2 - l1 + tF) and backward step
+// tB = tau + 2w + 2i - 68 (point l3 = l1 + l2 - tB).  Then every pair of the
+// block is at the same forward l3 = c0 - r0 - 6 + tau and the same backward
+// l3 = r0 + c0 + 68 - tau, and every step has the parity of tau, so the
+// contraction over one block of 16 time steps is a dense product
+//     D[pair, slot] = sum_tau x[pair, tau] B[tau, slot],
+// x = f^2 (the family value squared) and B = the windows at that tau, with the
+// parity of each slot applied to B's rows.  A 16th column of B holds 2 l3 + 1
+// and gives the normalisation sum.  Each lane runs at most 68 idle steps at
+// the ramps (lanes start and finish at different tau).
+//
+// Precision.  x and B are split into three BF16 parts (hi + mid + lo carries
+// 24 bits) and D is formed from six products (all but the three smallest),
+// ordered so that the hi x hi product is added last: the tensor core rounds
+// its FP32 accumulation toward zero, so each 16-step D starts from zero and
+// takes one such rounding at full scale.  Each D is added into float-float
+// totals on the CUDA cores.  B is scaled per 16-step block by a running power
+// of two (block floating point; windows span 1e-45), the same role the slice
+// exponents play in the chosen kernel.  The last forward point, the match of
+// the two sweeps, the normalisation and the outputs are FP64.
+//
+// Pipeline per 16-step block q: the lanes write x (three planes, two steps per
+// 32-bit column) into tensor memory; at the block end one thread issues the
+// 12 MMAs of q (6 per sweep) and commits them to an mbarrier; the lanes go on
+// with block q + 1 into the other A buffer, and at its end wait (bounded) for
+// q's MMAs, read D and fold it into the totals.  B tiles are built in shared
+// memory one block ahead.  A wait that gives up sets *p.status.
+#include "ps_internal.cuh"
+#include "ps_epilogue.cuh"
+#include "ps_ff.cuh"
+#include "ps_umma.cuh"
+
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <vector>
+
+namespace ps {
+namespace {
+
+constexpr int kK = 16;            // time steps per MMA (BF16 K)
+constexpr int kPlanes = 3;        // hi, mid, lo BF16 parts
+constexpr int kLead = 6;          // forward skew offset: tF = tau - kLead - 2i + 2w
+constexpr int kRamp = 68;         // extra time steps of a block beyond r0 (both sweeps)
+constexpr uint32_t kTmemCols = 128;
+constexpr int kBPlane = kMmaCols * kK * 2;  // bytes of one BF16 B plane: 16 columns x 16 steps
+constexpr int kWaitLimit = 1 << 22;
+constexpr uint32_t kIdesc = umma::idesc_bf16(128, kMmaCols);
+// six of the nine products of the three-part split, small first, hi x hi last:
+// (A part, B part)
+__device__ constexpr int kPass[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
+
+// tensor memory columns: D forward [0, 16), D backward [16, 32), then A[buf][sweep][plane], 8 columns each
+__device__ __forceinline__ uint32_t a_col(int buf, int sweep, int plane)
+{
+    return 2u * kMmaCols + (uint32_t)(((buf * 2 + sweep) * kPlanes + plane) * (kK / 2));
+}
+
+struct __align__(128) Smem {
+    unsigned char B[2][2][kPlanes][kBPlane];  // [buffer][sweep][part]: K-major BF16, core matrices 8 x 16 B
+    float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
+    int ref[2][kMmaCols];                     // running exponent of B's scale per sweep and column
+    uint64_t mbar;
+    uint32_t tmem;
+};
+
+__device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 below the normal range
+{
+    return d < -126 ? 0.0f : __int_as_float((d + 127) << 23);
+}
+
+// Byte offset of element (column n, step k) in a B plane: K-major core matrices,
+// 128 B between the two along K (LBO), 256 B between 8-column groups (SBO).
+__device__ __forceinline__ int b_off(int n, int k) { return (n >> 3) * 256 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2; }
+
+__device__ __forceinline__ uint32_t bf2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+
+// Three-part BF16 split of two values (low half: a, high half: b).
+__device__ __forceinline__ void split3(float a, float b, uint32_t (&w)[kPlanes])
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float ra = a - __low2float(h), rb = b - __high2float(h);
+    const __nv_bfloat162 m = __floats2bfloat162_rn(ra, rb);
+    const float qa = ra - __low2float(m), qb = rb - __high2float(m);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(qa, qb);
+    w[0] = bf2_bits(h);
+    w[1] = bf2_bits(m);
+    w[2] = bf2_bits(l);
+}
+
+// B of block q into buffer q & 1 (all 128 threads: thread = sweep x column x 4 steps).
+__device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int r0, int c0, int tid)
+{
+    const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
+    float m[4];
+    int e[4];
+    int emax = kZeroExp;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int tau = q * kK + 4 * qd + u;
+        const int l3 = s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+        m[u] = 0.0f;
+        e[u] = kZeroExp;
+        if (l3 >= 0 && l3 < p.wlen) {
+            if (n < p.nslot) {
+                const int par = p.parity[n];
+                if (par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0)) {
+                    const int2 v = __ldg(p.bf[n] + l3);
+                    m[u] = __int_as_float(v.x);
+                    e[u] = v.y;
+                }
+            } else if (n == p.nslot) {  // the normalisation column: 2 l3 + 1
+                m[u] = frexpf((float)(2 * l3 + 1), &e[u]);
+            }
+        }
+        emax = max(emax, e[u]);
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
+    int rold = qd == 0 ? sm.ref[s][n] : 0;
+    rold = __shfl_sync(0xffffffffu, rold, lane & ~3);
+    const int rnew = max(rold, emax);
+    if (qd == 0) {
+        sm.ref[s][n] = rnew;
+        sm.rescale[q % 3][s][n] = rold == rnew ? 1.0f : pow2f_or_zero(rold - rnew);
+    }
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = m[u] * pow2f_or_zero(e[u] - rnew);
+    uint32_t w01[kPlanes], w23[kPlanes];
+    split3(v[0], v[1], w01);
+    split3(v[2], v[3], w23);
+    const int off = b_off(n, 4 * qd);
+#pragma unroll
+    for (int pl = 0; pl < kPlanes; ++pl)
+        *reinterpret_cast<uint2*>(&sm.B[q & 1][s][pl][off]) = make_uint2(w01[pl], w23[pl]);
+}
+
+struct Sweep22 {
+    ff f, fo, a;  // f at the current point, at the previous one, and a = sqrt(P) at the current point
+    float w;      // 4 (2 j + 1)
+};
+
+// f(j+1) = -(4 (2j+1) f(j) + a(j) f(j-1)) / a(j+1), a(j+1)^2 = P given as two exact integer products
+__device__ __forceinline__ void sweep_step(Sweep22& S, ff u, ff v, float dw)
+{
+    const ff P = ff_mul_raw(u, v);
+    const ff r = ff_rsqrt(P);
+    const ff rho = ff_mul_raw(S.a, r);
+    S.a = ff_mul(P, r);
+    const ff x = ff_mul_raw(ff_mulf_raw(S.f, S.w), r);
+    const ff y = ff_mul_raw(rho, S.fo);
+    S.fo = S.f;
+    S.f = ff_neg(ff_add_raw(x, y));
+    S.w += dw;
+}
+// forward step t (j = l2 - l1 + t): P(j+1) = (t+1)(2d+t+1) (2l1-t)(2l2+t+2)
+__device__ __forceinline__ void fwd_step(Sweep22& S, int t, int d, int l1, int l2)
+{
+    sweep_step(S, two_prod((float)(t + 1), (float)(2 * d + t + 1)), two_prod((float)(2 * l1 - t), (float)(2 * l2 + t + 2)),
+               8.0f);
+}
+// backward step t (j = l1 + l2 - t): P(j) = (2l1-t)(2l2-t) (1+t)(2l1+2l2+1-t)
+__device__ __forceinline__ void bwd_step(Sweep22& S, int t, int l1, int l2)
+{
+    sweep_step(S, two_prod((float)(2 * l1 - t), (float)(2 * l2 - t)), two_prod((float)(1 + t), (float)(2 * l1 + 2 * l2 + 1 - t)),
+               -8.0f);
+}
+
+// (0 0 0) family: f(j+1) = -(a(j) / a(j+1)) f(j-1), taken at the odd steps
+// (the family vanishes at odd points).  rho = sqrt(X / Y) from two exact integer
+// products each; two reciprocal square roots keep every product below 2^64.
+__device__ __forceinline__ ff rho00(ff X, ff Y)
+{
+    return ff_mul(ff_mul_raw(X, ff_rsqrt(X)), ff_rsqrt(Y));
+}
+// forward odd step t: X = P(jmin + t) = t(2d+t)(2l1+1-t)(2l2+t+1), Y = P(jmin + t + 1)
+__device__ __forceinline__ void fwd_step00(ff& f0, int t, int d, int l1, int l2)
+{
+    const ff X = ff_mul_raw(two_prod((float)t, (float)(2 * d + t)), two_prod((float)(2 * l1 + 1 - t), (float)(2 * l2 + t + 1)));
+    const ff Y = ff_mul_raw(two_prod((float)(t + 1), (float)(2 * d + t + 1)), two_prod((float)(2 * l1 - t), (float)(2 * l2 + t + 2)));
+    f0 = ff_neg(ff_mul_raw(rho00(X, Y), f0));
+}
+// backward odd step t (point j = l1 + l2 - t): X = P(j + 1), Y = P(j)
+__device__ __forceinline__ void bwd_step00(ff& f0, int t, int l1, int l2)
+{
+    const ff X = ff_mul_raw(two_prod((float)(2 * l1 - t + 1), (float)(2 * l2 - t + 1)),
+                            two_prod((float)t, (float)(2 * l1 + 2 * l2 + 2 - t)));
+    const ff Y = ff_mul_raw(two_prod((float)(2 * l1 - t), (float)(2 * l2 - t)), two_prod((float)(1 + t), (float)(2 * l1 + 2 * l2 + 1 - t)));
+    f0 = ff_neg(ff_mul_raw(rho00(X, Y), f0));
+}
+
+__device__ __forceinline__ float sq(const ff& f)
+{
+    const float g = __fadd_rn(f.h, f.l);
+    return __fmul_rn(g, g);
+}
+
+// totals += D * rescale (Knuth two-sum on the high words)
+__device__ __forceinline__ void fold(ff& T, float d, float resc)
+{
+    if (resc != 1.0f) {  // the same for every thread: a uniform branch, rarely taken
+        T.h *= resc;
+        T.l *= resc;
+    }
+    const float s = __fadd_rn(T.h, d);
+    const float bb = __fsub_rn(s, T.h);
+    const float err = __fadd_rn(__fsub_rn(T.h, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    T.h = s;
+    T.l = __fadd_rn(T.l, err);
+}
+
+template <bool F00>
+__global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
+{
+    __shared__ Smem sm;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int2 tile = p.tiles[blockIdx.x];
+    const int r0 = tile.x, c0 = tile.y;
+    const int l1 = r0 + 2 * warp, l2 = c0 + 2 * lane;
+    const bool writes = l1 >= p.lmin && l1 <= p.lmax && l2 >= l1 && l2 <= p.lmax;
+    const bool runs = writes && (F00 || l1 >= 2);  // the (2 -2 0) family vanishes for l1 < 2
+    const int T = runs ? l1 : 0;
+    const int d = l2 - l1;
+    const int nk = (r0 + kRamp + kK - 1) / kK;  // 16-step blocks of the skewed sweeps (block-uniform)
+    const int ncols = p.nslot + 1;
+
+    if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
+    if (tid < 2 * kMmaCols) sm.ref[tid / kMmaCols][tid % kMmaCols] = kZeroExp;
+    if (tid == 0) umma::mbar_init(&sm.mbar);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tbase = sm.tmem;
+    const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
+    build_B(p, sm, 0, r0, c0, tid);
+
+    // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
+    Sweep22 F, B;
+    F.f = ff_make(1.0f); F.fo = ff_make(0.0f); F.a = ff_make(0.0f); F.w = 4.0f * (float)(2 * d + 1);
+    B.f = ff_make(1.0f); B.fo = ff_make(0.0f); B.a = ff_make(0.0f); B.w = 4.0f * (float)(2 * (l1 + l2) + 1);
+    ff tot[2][kMmaCols];
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+        for (int n = 0; n < kMmaCols; ++n) tot[s][n] = ff_make(0.0f);
+    bool ok = true;
+
+    auto flush = [&](int q) {
+        ok &= umma::mbar_wait(&sm.mbar, (uint32_t)(q & 1), kWaitLimit);
+        umma::fence_after_sync();
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            float dv[kMmaCols];
+            umma::ld_x16(tlane + (uint32_t)(s * kMmaCols), dv);
+#pragma unroll
+            for (int n = 0; n < kMmaCols; ++n)
+                if (n < ncols) fold(tot[s][n], dv[n], sm.rescale[q % 3][s][n]);
+        }
+    };
+
+    const int fofs = -kLead - 2 * lane + 2 * warp;  // tF = tau + fofs
+    const int bofs = 2 * warp + 2 * lane - kRamp;   // tB = tau + bofs
+    for (int q = 0; q < nk; ++q) {
+        const int buf = q & 1;
+#pragma unroll 1
+        for (int s2 = 0; s2 < kK; s2 += 2) {
+            float xf[2], xb[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
+                const int tau = q * kK + s2 + e;
+                const int tf = tau + fofs, tb = tau + bofs;
+                xf[e] = 0.0f;
+                xb[e] = 0.0f;
+                if (tf >= 0 && tf < T) {
+                    if (F00) {
+                        if (e == 0) xf[e] = sq(F.f);
+                        else fwd_step00(F.f, tf, d, l1, l2);
+                    } else {
+                        xf[e] = sq(F.f);
+                        fwd_step(F, tf, d, l1, l2);
+                    }
+                }
+                if (tb >= 0 && tb < T) {
+                    if (F00) {
+                        if (e == 0) xb[e] = sq(B.f);
+                        else bwd_step00(B.f, tb, l1, l2);
+                    } else {
+                        xb[e] = sq(B.f);
+                        bwd_step(B, tb, l1, l2);
+                    }
+                }
+            }
+            uint32_t wf[kPlanes], wb[kPlanes];
+            split3(xf[0], xf[1], wf);
+            split3(xb[0], xb[1], wb);
+#pragma unroll
+            for (int pl = 0; pl < kPlanes; ++pl) {
+                umma::st_x1(tlane + a_col(buf, 0, pl) + (uint32_t)(s2 >> 1), wf[pl]);
+                umma::st_x1(tlane + a_col(buf, 1, pl) + (uint32_t)(s2 >> 1), wb[pl]);
+            }
+        }
+        // ---- block boundary ----
+        if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
+        if (q + 1 < nk) build_B(p, sm, q + 1, r0, c0, tid);
+        umma::wait_st();
+        umma::fence_smem_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        if (tid == 0) {
+#pragma unroll
+            for (int s = 0; s < 2; ++s)
+#pragma unroll
+                for (int ps = 0; ps < 6; ++ps) {
+                    const uint64_t bd = umma::smem_desc(umma::smem_addr(&sm.B[buf][s][kPass[ps][1]][0]), 128u, 256u);
+                    umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(buf, s, kPass[ps][0]), bd, kIdesc,
+                                      ps > 0);
+                }
+            umma::mma_commit(&sm.mbar);
+        }
+    }
+    flush(nk - 1);
+    if (!ok) atomicExch(p.status, 1u);
+
+    // ---- the last forward point, match, normalisation (FP64) ----
+    double Xi[kMmaMaxSlots];
+#pragma unroll
+    for (int k = 0; k < kMmaMaxSlots; ++k) Xi[k] = 0.0;
+    if (runs) {
+        double FW[kMmaMaxSlots + 1], BW[kMmaMaxSlots + 1];
+#pragma unroll
+        for (int n = 0; n <= kMmaMaxSlots; ++n) {
+            FW[n] = BW[n] = 0.0;
+            if (n < ncols) {
+                FW[n] = ldexp((double)tot[0][n].h + (double)tot[0][n].l, sm.ref[0][n]);
+                BW[n] = ldexp((double)tot[1][n].h + (double)tot[1][n].l, sm.ref[1][n]);
+            }
+        }
+        const int jm = l2;  // jmin + T: the last forward point, in FP64; its parity is that of T
+        const bool evenT = (T & 1) == 0;
+        double gm0, lam;
+        double x = 0.0;
+        if (F00) {
+            // the 00 family is non-zero at points of the parity of jmin: jm when T is even, jm + 1
+            // otherwise; both sweeps end there and are matched at that one point
+            gm0 = ff_to_double(F.f);
+            if (evenT) {
+                x = gm0 * gm0;
+            } else {
+                const ff X = ff_mul_raw(two_prod((float)T, (float)(2 * d + T)),
+                                        two_prod((float)(2 * l1 + 1 - T), (float)(2 * l2 + T + 1)));
+                const ff Y = ff_mul_raw(two_prod((float)(T + 1), (float)(2 * d + T + 1)),
+                                        two_prod((float)(2 * l1 - T), (float)(2 * l2 + T + 2)));
+                gm0 = ff_to_double(ff_neg(ff_mul(rho00(X, Y), F.f)));
+            }
+            lam = gm0 / ff_to_double(B.f);
+        } else {
+            gm0 = ff_to_double(F.f);
+            x = gm0 * gm0;
+            // one more forward step for f(jm + 1): P(jm + 1) = (T+1)(2d+T+1)(2l1-T)(2l2+T+2)
+            const ff P1 = ff_mul_raw(two_prod((float)(T + 1), (float)(2 * d + T + 1)),
+                                     two_prod((float)(2 * l1 - T), (float)(2 * l2 + T + 2)));
+            const ff r = ff_rsqrt(P1);
+            const double gm1 =
+                ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mulf_raw(F.f, F.w), r), ff_mul_raw(ff_mul_raw(F.a, r), F.fo))));
+            const double hm0 = ff_to_double(B.f), hm1 = ff_to_double(B.fo);
+            lam = (gm0 * hm0 + gm1 * hm1) / (hm0 * hm0 + hm1 * hm1);
+        }
+        const double FN = FW[p.nslot] + (2.0 * jm + 1.0) * x;
+        const double BN = BW[p.nslot];
+#pragma unroll
+        for (int k = 0; k < kMmaMaxSlots; ++k) {
+            if (k < p.nslot) {
+                const int par = p.parity[k];
+                if (par == PAR_ALL || (par == PAR_EVEN) == evenT) FW[k] = fma(x, __ldg(p.wW[k] + jm), FW[k]);
+            }
+        }
+        const double lam2 = lam * lam;
+        const double inv = kInv4Pi / fma(lam2, BN, FN);
+#pragma unroll
+        for (int k = 0; k < kMmaMaxSlots; ++k)
+            if (k < p.nslot) Xi[k] = fma(lam2, BW[k], FW[k]) * inv;
+    }
+    if (writes) {
+        const long long ra = l1 - p.lmin, rb = l2 - p.lmin;
+        const bool mcm = p.epilogue == EPI_MCM;
+#pragma unroll
+        for (int k = 0; k < kMmaMaxSlots; ++k) {
+            if (k < p.nslot) {
+                p.out[k][ra + rb * p.ldo] = mcm ? (2.0 * l2 + 1.0) * Xi[k] : Xi[k];
+                p.out[k][rb + ra * p.ldo] = mcm ? (2.0 * l1 + 1.0) * Xi[k] : Xi[k];
+            }
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tbase, kTmemCols);
+}
+
+// Shared memory requested per block beyond the static part: caps residency at
+// four blocks per SM, so the four blocks' tensor memory (4 x 128 columns) fits
+// the SM's 512 columns and no allocation has to wait.
+constexpr int kOccupancySmem = 40 * 1024;
+
+}  // namespace
+
+// The blocks of one grid: rows r0 + 2w (w = 0..3) by columns c0 + 2i (i = 0..31),
+// in four classes of (row parity, column parity), heaviest (largest r0) first.
+void mma_tile_list(int lmin, int lmax, std::vector<int2>& t)
+{
+    t.clear();
+    for (int pr = 0; pr < 2; ++pr) {
+        const int rmax = lmax - ((lmax - pr) & 1);
+        for (int r0 = rmax - 6; r0 + 6 >= lmin; r0 -= 8) {
+            int lo = r0;  // lowest row of the tile that exists
+            while (lo < lmin || lo < 0) lo += 2;
+            for (int pc = 0; pc < 2; ++pc) {
+                const int cmax = lmax - ((lmax - pc) & 1);
+                for (int c0 = cmax - 62; c0 + 62 >= lo; c0 -= 64) t.push_back(make_int2(r0, c0));
+            }
+        }
+    }
+    std::stable_sort(t.begin(), t.end(), [](int2 a, int2 b) { return a.x > b.x; });
+}
+
+cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s)
+{
+    if (p.ntiles <= 0) return cudaSuccess;
+    static_assert(kOccupancySmem <= 48 * 1024, "within the default dynamic shared memory limit");
+    if (fam00)
+        k_coupling_mma<true><<<(unsigned)p.ntiles, 128, kOccupancySmem, s>>>(p);
+    else
+        k_coupling_mma<false><<<(unsigned)p.ntiles, 128, kOccupancySmem, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace ps

@@ -29,7 +29,7 @@ EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_sync
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
            "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device",
-           "ps_quickpol_xi_alm", "ps_mcm_set")
+           "ps_quickpol_xi_alm", "ps_mcm_set", "ps_set_tensor_cores")
 
 
 class PowerSpectraGPUError(RuntimeError):
@@ -87,6 +87,8 @@ def load(path=None):
         lib.ps_set_stream.restype = ci
         lib.ps_synchronize.argtypes = [vp]
         lib.ps_synchronize.restype = ci
+        lib.ps_set_tensor_cores.argtypes = [vp, ci]
+        lib.ps_set_tensor_cores.restype = ci
         lib.ps_mcm.argtypes = [vp, ci, _DP, i64, ci, ci, ci, _DP, i64]
         lib.ps_mcm.restype = ci
         lib.ps_mcm_multi.argtypes = [vp, ctypes.c_uint, _DPP, i64, ci, ci, ci, _DPP, i64]
@@ -192,6 +194,10 @@ class Context:
 
     def set_stream(self, stream_handle):
         self.check(self.lib.ps_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0)))
+
+    def set_tensor_cores(self, enable):
+        """Chosen-mode sets: use the tensor-core kernels where they apply (True, the default) or not."""
+        self.check(self.lib.ps_set_tensor_cores(self.handle, 1 if enable else 0))
 
     def synchronize(self):
         self.check(self.lib.ps_synchronize(self.handle))
