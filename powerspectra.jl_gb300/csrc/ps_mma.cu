@@ -263,6 +263,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 
     auto flush = [&](int q) {
         ok &= umma::mbar_wait(&sm.mbar, (uint32_t)(q & 1), kWaitLimit);
+        __syncwarp();  // lanes leave the wait at different polls; the loads below are warp-collective
         umma::fence_after_sync();
 #pragma unroll
         for (int s = 0; s < 2; ++s) {
@@ -309,6 +310,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             uint32_t wf[kPlanes], wb[kPlanes];
             split3(xf[0], xf[1], wf);
             split3(xb[0], xb[1], wb);
+            __syncwarp();  // the stores below are warp-collective (.sync.aligned)
 #pragma unroll
             for (int pl = 0; pl < kPlanes; ++pl) {
                 umma::st_x1(tlane + a_col(buf, 0, pl) + (uint32_t)(s2 >> 1), wf[pl]);
