@@ -57,6 +57,10 @@ constexpr int kK = 16;            // time steps per MMA (BF16 K)
 constexpr int kPlanes = 3;        // hi, mid, lo BF16 parts
 constexpr int kLead = 6;          // forward skew offset: tF = tau - kLead - 2i + 2w
 constexpr int kRamp = 68;         // extra time steps of a block beyond r0 (both sweeps)
+// From tau = kSteady to tau = r0 + kLead - 1 every lane of the block that runs is inside both of
+// its sweeps: the forward sweep of lane (w, i) spans tau = 6 + 2i - 2w .. r0 + 5 + 2i and the
+// backward one tau = 68 - 2w - 2i .. r0 + 67 - 2i.
+constexpr int kSteady = 68;
 constexpr uint32_t kTmemCols = 128;
 constexpr int kBPlane = kMmaCols * kK * 2;  // bytes of one BF16 B plane: 16 columns x 16 steps
 constexpr int kWaitLimit = 1 << 22;
@@ -183,11 +187,14 @@ __device__ __forceinline__ void bwd_step(Sweep22& S, int t, int l1, int l2)
 }
 
 // (0 0 0) family: f(j+1) = -(a(j) / a(j+1)) f(j-1), taken at the odd steps
-// (the family vanishes at odd points).  rho = sqrt(X / Y) from two exact integer
-// products each; two reciprocal square roots keep every product below 2^64.
+// (the family vanishes at odd points).  rho = sqrt(X / Y) = X' / sqrt(X' Y) 2^16
+// with X' = X 2^-32 (exact): X and Y reach 2^64 at the largest lmax, and the
+// scaling keeps X' Y within the FP32 range.
 __device__ __forceinline__ ff rho00(ff X, ff Y)
 {
-    return ff_mul(ff_mul_raw(X, ff_rsqrt(X)), ff_rsqrt(Y));
+    const ff Xs = ff{X.h * 0x1p-32f, X.l * 0x1p-32f};
+    const ff r = ff_mul(Xs, ff_rsqrt(ff_mul_raw(Xs, Y)));
+    return ff{r.h * 0x1p16f, r.l * 0x1p16f};
 }
 // forward odd step t: X = P(jmin + t) = t(2d+t)(2l1+1-t)(2l2+t+1), Y = P(jmin + t + 1)
 __device__ __forceinline__ void fwd_step00(ff& f0, int t, int d, int l1, int l2)
@@ -211,13 +218,9 @@ __device__ __forceinline__ float sq(const ff& f)
     return __fmul_rn(g, g);
 }
 
-// totals += D * rescale (Knuth two-sum on the high words)
-__device__ __forceinline__ void fold(ff& T, float d, float resc)
+// totals += D (Knuth two-sum on the high words)
+__device__ __forceinline__ void fold(ff& T, float d)
 {
-    if (resc != 1.0f) {  // the same for every thread: a uniform branch, rarely taken
-        T.h *= resc;
-        T.l *= resc;
-    }
     const float s = __fadd_rn(T.h, d);
     const float bb = __fsub_rn(s, T.h);
     const float err = __fadd_rn(__fsub_rn(T.h, __fsub_rn(s, bb)), __fsub_rn(d, bb));
@@ -269,9 +272,28 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         for (int s = 0; s < 2; ++s) {
             float dv[kMmaCols];
             umma::ld_x16(tlane + (uint32_t)(s * kMmaCols), dv);
+            // the totals move to block q's scale where its exponent grew (the same for every
+            // thread: a uniform branch, taken only when some window's scale changed)
+            const float4* rs = reinterpret_cast<const float4*>(&sm.rescale[q % 3][s][0]);
+            float resc[kMmaCols];
+#pragma unroll
+            for (int v = 0; v < kMmaCols / 4; ++v) {
+                const float4 r4 = rs[v];
+                resc[4 * v] = r4.x; resc[4 * v + 1] = r4.y; resc[4 * v + 2] = r4.z; resc[4 * v + 3] = r4.w;
+            }
+            bool any = false;
+#pragma unroll
+            for (int n = 0; n < kMmaCols; ++n) any |= resc[n] != 1.0f;
+            if (any) {
+#pragma unroll
+                for (int n = 0; n < kMmaCols; ++n) {
+                    tot[s][n].h *= resc[n];
+                    tot[s][n].l *= resc[n];
+                }
+            }
 #pragma unroll
             for (int n = 0; n < kMmaCols; ++n)
-                if (n < ncols) fold(tot[s][n], dv[n], sm.rescale[q % 3][s][n]);
+                if (n < ncols) fold(tot[s][n], dv[n]);
         }
     };
 
@@ -282,6 +304,29 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll 1
         for (int s2 = 0; s2 < kK; s2 += 2) {
             float xf[2], xb[2];
+            const int tau0 = q * kK + s2;
+            if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
+                // steady state: every lane that runs is inside both sweeps, so both steps run
+                // unconditionally (their two dependency chains interleave); lanes that do not
+                // run compute values that are masked out of x and never written
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
+                    if (F00) {
+                        xf[e] = e == 0 && runs ? sq(F.f) : 0.0f;
+                        xb[e] = e == 0 && runs ? sq(B.f) : 0.0f;
+                        if (e == 1) {
+                            fwd_step00(F.f, tf, d, l1, l2);
+                            bwd_step00(B.f, tb, l1, l2);
+                        }
+                    } else {
+                        xf[e] = runs ? sq(F.f) : 0.0f;
+                        xb[e] = runs ? sq(B.f) : 0.0f;
+                        fwd_step(F, tf, d, l1, l2);
+                        bwd_step(B, tb, l1, l2);
+                    }
+                }
+            } else {
 #pragma unroll
             for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
                 const int tau = q * kK + s2 + e;
@@ -306,6 +351,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                         bwd_step(B, tb, l1, l2);
                     }
                 }
+            }
             }
             uint32_t wf[kPlanes], wb[kPlanes];
             split3(xf[0], xf[1], wf);
