@@ -156,60 +156,121 @@ __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int
 }
 
 struct Sweep22 {
-    ff f, fo, a;  // f at the current point, at the previous one, and a = sqrt(P) at the current point
-    float w;      // 4 (2 j + 1)
+    ff f, fo;  // f at the current point and at the previous one
+    float w;   // 4 (2 j + 1)
 };
 
-// f(j+1) = -(4 (2j+1) f(j) + a(j) f(j-1)) / a(j+1), a(j+1)^2 = P given as two exact integer products
-__device__ __forceinline__ void sweep_step(Sweep22& S, ff u, ff v, float dw)
+// ---- recurrence coefficient rings -------------------------------------------
+// For the pair (l1, l2) the recurrence coefficient factorises as
+//   forward step t (point j = l2 - l1 + t):  P(j) = G(t) F(v),   v = 2 l2 + t,
+//     G(t) = t (2 l1 + 1 - t),  F(v) = (v - 2 l1)(v + 1);
+//   backward step t (point j = l1 + l2 - t): P(j) = G(t + 1) Fb(u),  u = 2 l2 - t,
+//     Fb(u) = u (2 l1 + 1 + u).
+// So rho = a(j)/a(j+1) and r = 1/a(j+1) of a forward step are products of a G
+// entry and an F entry,
+//   g[t]  = (sqrt(G(t)/G(t+1)), 1/sqrt(G(t+1))),  f[v] = (sqrt(F(v)/F(v+1)), 1/sqrt(F(v+1))),
+// and rho = a(j+1)/a(j), r = 1/a(j) of a backward step of g[t] and
+//   fb[u] = (sqrt(Fb(u+1)/Fb(u)), 1/sqrt(Fb(u))).
+// Each warp (one row l1) keeps the three tables as rings of 64 entries per
+// parity.  In the skewed frame t, v and u all have the parity of tau, lane i
+// reads entry (index / 2) of consecutive lanes' neighbours (no bank conflicts),
+// and the forward and backward sweeps share g (t of the backward sweep of lane
+// i is t of the forward sweep of lane 31 - i).  A 16-step block reads 78
+// consecutive values of each table (39 per parity); the next block needs 16 new
+// ones per table, built at the block boundary.
+constexpr int kRing = 64;
+struct ffpair {
+    ff rho, r;
+};
+struct __align__(16) CoefRing {
+    ffpair g[2][kRing], f[2][kRing], fb[2][kRing];
+};
+__device__ __forceinline__ int ring_slot(int x) { return (x >> 1) & (kRing - 1); }
+
+// (sqrt(X / Y), 1 / sqrt(Y)) of two exact integer products; rho is 0 where X is
+__device__ __forceinline__ ffpair ratio_entry(ff X, ff Y)
 {
-    const ff P = ff_mul_raw(u, v);
-    const ff r = ff_rsqrt(P);
-    const ff rho = ff_mul_raw(S.a, r);
-    S.a = ff_mul(P, r);
+    const ff r = ff_rsqrt(Y);
+    const ff rho = X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
+    return ffpair{rho, r};
+}
+__device__ __forceinline__ void ring_g(CoefRing& R, int t, int l1)
+{
+    R.g[t & 1][ring_slot(t)] = ratio_entry(two_prod((float)t, (float)(2 * l1 + 1 - t)),
+                                           two_prod((float)(t + 1), (float)(2 * l1 - t)));
+}
+__device__ __forceinline__ void ring_f(CoefRing& R, int v, int l1)
+{
+    R.f[v & 1][ring_slot(v)] = ratio_entry(two_prod((float)(v - 2 * l1), (float)(v + 1)),
+                                           two_prod((float)(v + 1 - 2 * l1), (float)(v + 2)));
+}
+__device__ __forceinline__ void ring_fb(CoefRing& R, int u, int l1)
+{
+    R.fb[u & 1][ring_slot(u)] = ratio_entry(two_prod((float)(u + 1), (float)(2 * l1 + 2 + u)),
+                                            two_prod((float)u, (float)(2 * l1 + 1 + u)));
+}
+
+// one step of the (2 -2 0) family: f(next) = -(w f r + rho f(prev))
+__device__ __forceinline__ void step22(Sweep22& S, ff rho, ff r, float dw)
+{
     const ff x = ff_mul_raw(ff_mulf_raw(S.f, S.w), r);
     const ff y = ff_mul_raw(rho, S.fo);
     S.fo = S.f;
     S.f = ff_neg(ff_add_raw(x, y));
     S.w += dw;
 }
-// forward step t (j = l2 - l1 + t): P(j+1) = (t+1)(2d+t+1) (2l1-t)(2l2+t+2)
-__device__ __forceinline__ void fwd_step(Sweep22& S, int t, int d, int l1, int l2)
+// forward step t of lane l2 (parity p of t): g[t] and f[2 l2 + t]
+__device__ __forceinline__ void fwd_step(Sweep22& S, const CoefRing& R, int p, int t, int l2)
 {
-    sweep_step(S, two_prod((float)(t + 1), (float)(2 * d + t + 1)), two_prod((float)(2 * l1 - t), (float)(2 * l2 + t + 2)),
-               8.0f);
+    const ffpair g = R.g[p][ring_slot(t)], f = R.f[p][ring_slot(2 * l2 + t)];
+    step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), 8.0f);
 }
-// backward step t (j = l1 + l2 - t): P(j) = (2l1-t)(2l2-t) (1+t)(2l1+2l2+1-t)
-__device__ __forceinline__ void bwd_step(Sweep22& S, int t, int l1, int l2)
+// backward step t: g[t] and fb[2 l2 - t]
+__device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, int t, int l2)
 {
-    sweep_step(S, two_prod((float)(2 * l1 - t), (float)(2 * l2 - t)), two_prod((float)(1 + t), (float)(2 * l1 + 2 * l2 + 1 - t)),
-               -8.0f);
+    const ffpair g = R.g[p][ring_slot(t)], f = R.fb[p][ring_slot(2 * l2 - t)];
+    step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), -8.0f);
+}
+// (0 0 0) family at an odd step t: f(j+1) = -rho f(j-1), rho = a(j)/a(j+1) (forward) or
+// a(j+1)/a(j) (backward), the same ring entries as the (2 -2 0) step
+__device__ __forceinline__ void fwd_step00(ff& f0, const CoefRing& R, int t, int l2)
+{
+    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][ring_slot(t)].rho, R.f[1][ring_slot(2 * l2 + t)].rho), f0));
+}
+__device__ __forceinline__ void bwd_step00(ff& f0, const CoefRing& R, int t, int l2)
+{
+    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][ring_slot(t)].rho, R.fb[1][ring_slot(2 * l2 - t)].rho), f0));
 }
 
-// (0 0 0) family: f(j+1) = -(a(j) / a(j+1)) f(j-1), taken at the odd steps
-// (the family vanishes at odd points).  rho = sqrt(X / Y) = X' / sqrt(X' Y) 2^16
-// with X' = X 2^-32 (exact): X and Y reach 2^64 at the largest lmax, and the
-// scaling keeps X' Y within the FP32 range.
+// sqrt(X / Y) for the last forward points (X, Y up to 2^64: the scaling keeps X Y in range)
 __device__ __forceinline__ ff rho00(ff X, ff Y)
 {
     const ff Xs = ff{X.h * 0x1p-32f, X.l * 0x1p-32f};
     const ff r = ff_mul(Xs, ff_rsqrt(ff_mul_raw(Xs, Y)));
     return ff{r.h * 0x1p16f, r.l * 0x1p16f};
 }
-// forward odd step t: X = P(jmin + t) = t(2d+t)(2l1+1-t)(2l2+t+1), Y = P(jmin + t + 1)
-__device__ __forceinline__ void fwd_step00(ff& f0, int t, int d, int l1, int l2)
+
+// The ring values of block q (first = true: all 78 of each table; otherwise the 16
+// that block q needs beyond block q - 1), for warp row l1 = r0 + 2w and lanes
+// l2 = c0 + 2i.
+__device__ __forceinline__ void build_rings(CoefRing& R, int q, bool first, int w, int l1, int c0, int lane)
 {
-    const ff X = ff_mul_raw(two_prod((float)t, (float)(2 * d + t)), two_prod((float)(2 * l1 + 1 - t), (float)(2 * l2 + t + 1)));
-    const ff Y = ff_mul_raw(two_prod((float)(t + 1), (float)(2 * d + t + 1)), two_prod((float)(2 * l1 - t), (float)(2 * l2 + t + 2)));
-    f0 = ff_neg(ff_mul_raw(rho00(X, Y), f0));
-}
-// backward odd step t (point j = l1 + l2 - t): X = P(j + 1), Y = P(j)
-__device__ __forceinline__ void bwd_step00(ff& f0, int t, int l1, int l2)
-{
-    const ff X = ff_mul_raw(two_prod((float)(2 * l1 - t + 1), (float)(2 * l2 - t + 1)),
-                            two_prod((float)t, (float)(2 * l1 + 2 * l2 + 2 - t)));
-    const ff Y = ff_mul_raw(two_prod((float)(2 * l1 - t), (float)(2 * l2 - t)), two_prod((float)(1 + t), (float)(2 * l1 + 2 * l2 + 1 - t)));
-    f0 = ff_neg(ff_mul_raw(rho00(X, Y), f0));
+    const int tau0 = q * kK;
+    const int tlo = tau0 - 68 + 2 * w;                 // t: [tlo, tlo + 77]
+    const int vlo = 2 * c0 + 2 * w + tau0 - 6;         // v: [vlo, vlo + 77]
+    const int ulo = 2 * c0 - 2 * w + 130 - tau0 - 77;  // u: [ulo, ulo + 77]
+    if (first) {
+        for (int e = lane; e < 78; e += 32) {
+            ring_g(R, tlo + e, l1);
+            ring_f(R, vlo + e, l1);
+            ring_fb(R, ulo + e, l1);
+        }
+    } else if (lane < 16) {
+        ring_g(R, tlo + 62 + lane, l1);  // the top 16 of t
+        ring_fb(R, ulo + lane, l1);      // the bottom 16 of u
+    } else {
+        ring_f(R, vlo + 62 + lane - 16, l1);  // the top 16 of v
+    }
 }
 
 __device__ __forceinline__ float sq(const ff& f)
@@ -232,7 +293,9 @@ template <bool F00>
 __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 {
     __shared__ Smem sm;
+    extern __shared__ __align__(16) unsigned char dyn[];  // the warps' coefficient rings
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    CoefRing& R = reinterpret_cast<CoefRing*>(dyn)[warp];
     const int2 tile = p.tiles[blockIdx.x];
     const int r0 = tile.x, c0 = tile.y;
     const int l1 = r0 + 2 * warp, l2 = c0 + 2 * lane;
@@ -252,11 +315,13 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
     build_B(p, sm, 0, r0, c0, tid);
+    build_rings(R, 0, true, warp, l1, c0, lane);
+    __syncwarp();
 
     // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
     Sweep22 F, B;
-    F.f = ff_make(1.0f); F.fo = ff_make(0.0f); F.a = ff_make(0.0f); F.w = 4.0f * (float)(2 * d + 1);
-    B.f = ff_make(1.0f); B.fo = ff_make(0.0f); B.a = ff_make(0.0f); B.w = 4.0f * (float)(2 * (l1 + l2) + 1);
+    F.f = ff_make(1.0f); F.fo = ff_make(0.0f); F.w = 4.0f * (float)(2 * d + 1);
+    B.f = ff_make(1.0f); B.fo = ff_make(0.0f); B.w = 4.0f * (float)(2 * (l1 + l2) + 1);
     ff tot[2][kMmaCols];
 #pragma unroll
     for (int s = 0; s < 2; ++s)
@@ -316,14 +381,14 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                         xf[e] = e == 0 && runs ? sq(F.f) : 0.0f;
                         xb[e] = e == 0 && runs ? sq(B.f) : 0.0f;
                         if (e == 1) {
-                            fwd_step00(F.f, tf, d, l1, l2);
-                            bwd_step00(B.f, tb, l1, l2);
+                            fwd_step00(F.f, R, tf, l2);
+                            bwd_step00(B.f, R, tb, l2);
                         }
                     } else {
                         xf[e] = runs ? sq(F.f) : 0.0f;
                         xb[e] = runs ? sq(B.f) : 0.0f;
-                        fwd_step(F, tf, d, l1, l2);
-                        bwd_step(B, tb, l1, l2);
+                        fwd_step(F, R, e, tf, l2);
+                        bwd_step(B, R, e, tb, l2);
                     }
                 }
             } else {
@@ -336,19 +401,19 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 if (tf >= 0 && tf < T) {
                     if (F00) {
                         if (e == 0) xf[e] = sq(F.f);
-                        else fwd_step00(F.f, tf, d, l1, l2);
+                        else fwd_step00(F.f, R, tf, l2);
                     } else {
                         xf[e] = sq(F.f);
-                        fwd_step(F, tf, d, l1, l2);
+                        fwd_step(F, R, e, tf, l2);
                     }
                 }
                 if (tb >= 0 && tb < T) {
                     if (F00) {
                         if (e == 0) xb[e] = sq(B.f);
-                        else bwd_step00(B.f, tb, l1, l2);
+                        else bwd_step00(B.f, R, tb, l2);
                     } else {
                         xb[e] = sq(B.f);
-                        bwd_step(B, tb, l1, l2);
+                        bwd_step(B, R, e, tb, l2);
                     }
                 }
             }
@@ -365,7 +430,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         }
         // ---- block boundary ----
         if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
-        if (q + 1 < nk) build_B(p, sm, q + 1, r0, c0, tid);
+        if (q + 1 < nk) {
+            build_B(p, sm, q + 1, r0, c0, tid);
+            build_rings(R, q + 1, false, warp, l1, c0, lane);
+        }
         umma::wait_st();
         umma::fence_smem_async();
         umma::fence_before_sync();
@@ -421,12 +489,15 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         } else {
             gm0 = ff_to_double(F.f);
             x = gm0 * gm0;
-            // one more forward step for f(jm + 1): P(jm + 1) = (T+1)(2d+T+1)(2l1-T)(2l2+T+2)
+            // one more forward step for f(jm + 1): P(jm) = T(2d+T)(2l1+1-T)(2l2+T+1),
+            // P(jm + 1) = (T+1)(2d+T+1)(2l1-T)(2l2+T+2)
+            const ff P0 = ff_mul_raw(two_prod((float)T, (float)(2 * d + T)),
+                                     two_prod((float)(2 * l1 + 1 - T), (float)(2 * l2 + T + 1)));
             const ff P1 = ff_mul_raw(two_prod((float)(T + 1), (float)(2 * d + T + 1)),
                                      two_prod((float)(2 * l1 - T), (float)(2 * l2 + T + 2)));
             const ff r = ff_rsqrt(P1);
             const double gm1 =
-                ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mulf_raw(F.f, F.w), r), ff_mul_raw(ff_mul_raw(F.a, r), F.fo))));
+                ff_to_double(ff_neg(ff_add(ff_mul_raw(ff_mulf_raw(F.f, F.w), r), ff_mul_raw(rho00(P0, P1), F.fo))));
             const double hm0 = ff_to_double(B.f), hm1 = ff_to_double(B.fo);
             lam = (gm0 * hm0 + gm1 * hm1) / (hm0 * hm0 + hm1 * hm1);
         }
@@ -461,10 +532,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     if (warp == 0) umma::tmem_free(tbase, kTmemCols);
 }
 
-// Shared memory requested per block beyond the static part: caps residency at
-// four blocks per SM, so the four blocks' tensor memory (4 x 128 columns) fits
-// the SM's 512 columns and no allocation has to wait.
+// Dynamic shared memory per block: the four warps' coefficient rings, padded so
+// that residency is capped at four blocks per SM and the four blocks' tensor
+// memory (4 x 128 columns) fits the SM's 512 columns: no allocation has to wait.
 constexpr int kOccupancySmem = 40 * 1024;
+static_assert(4 * sizeof(CoefRing) <= kOccupancySmem, "the rings fit the block's dynamic shared memory");
 
 }  // namespace
 
