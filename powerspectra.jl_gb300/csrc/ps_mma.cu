@@ -289,7 +289,8 @@ __device__ __forceinline__ void fold(ff& T, float d)
     T.l = __fadd_rn(T.l, err);
 }
 
-template <bool F00>
+// NC: columns folded into the totals (8 or 16; at least nslot + 1)
+template <bool F00, int NC>
 __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 {
     __shared__ Smem sm;
@@ -322,11 +323,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     Sweep22 F, B;
     F.f = ff_make(1.0f); F.fo = ff_make(0.0f); F.w = 4.0f * (float)(2 * d + 1);
     B.f = ff_make(1.0f); B.fo = ff_make(0.0f); B.w = 4.0f * (float)(2 * (l1 + l2) + 1);
-    ff tot[2][kMmaCols];
+    ff tot[2][NC];
 #pragma unroll
     for (int s = 0; s < 2; ++s)
 #pragma unroll
-        for (int n = 0; n < kMmaCols; ++n) tot[s][n] = ff_make(0.0f);
+        for (int n = 0; n < NC; ++n) tot[s][n] = ff_make(0.0f);
     bool ok = true;
 
     auto flush = [&](int q) {
@@ -340,24 +341,24 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             // the totals move to block q's scale where its exponent grew (the same for every
             // thread: a uniform branch, taken only when some window's scale changed)
             const float4* rs = reinterpret_cast<const float4*>(&sm.rescale[q % 3][s][0]);
-            float resc[kMmaCols];
+            float resc[NC];
 #pragma unroll
-            for (int v = 0; v < kMmaCols / 4; ++v) {
+            for (int v = 0; v < NC / 4; ++v) {
                 const float4 r4 = rs[v];
                 resc[4 * v] = r4.x; resc[4 * v + 1] = r4.y; resc[4 * v + 2] = r4.z; resc[4 * v + 3] = r4.w;
             }
             bool any = false;
 #pragma unroll
-            for (int n = 0; n < kMmaCols; ++n) any |= resc[n] != 1.0f;
+            for (int n = 0; n < NC; ++n) any |= resc[n] != 1.0f;
             if (any) {
 #pragma unroll
-                for (int n = 0; n < kMmaCols; ++n) {
+                for (int n = 0; n < NC; ++n) {
                     tot[s][n].h *= resc[n];
                     tot[s][n].l *= resc[n];
                 }
             }
 #pragma unroll
-            for (int n = 0; n < kMmaCols; ++n)
+            for (int n = 0; n < NC; ++n)
                 if (n < ncols) fold(tot[s][n], dv[n]);
         }
     };
@@ -366,7 +367,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int bofs = 2 * warp + 2 * lane - kRamp;   // tB = tau + bofs
     for (int q = 0; q < nk; ++q) {
         const int buf = q & 1;
-#pragma unroll 1
+#pragma unroll 2
         for (int s2 = 0; s2 < kK; s2 += 2) {
             float xf[2], xb[2];
             const int tau0 = q * kK + s2;
@@ -459,9 +460,9 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll
     for (int k = 0; k < kMmaMaxSlots; ++k) Xi[k] = 0.0;
     if (runs) {
-        double FW[kMmaMaxSlots + 1], BW[kMmaMaxSlots + 1];
+        double FW[NC], BW[NC];
 #pragma unroll
-        for (int n = 0; n <= kMmaMaxSlots; ++n) {
+        for (int n = 0; n < NC; ++n) {
             FW[n] = BW[n] = 0.0;
             if (n < ncols) {
                 FW[n] = ldexp((double)tot[0][n].h + (double)tot[0][n].l, sm.ref[0][n]);
@@ -504,7 +505,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         const double FN = FW[p.nslot] + (2.0 * jm + 1.0) * x;
         const double BN = BW[p.nslot];
 #pragma unroll
-        for (int k = 0; k < kMmaMaxSlots; ++k) {
+        for (int k = 0; k < NC - 1; ++k) {
             if (k < p.nslot) {
                 const int par = p.parity[k];
                 if (par == PAR_ALL || (par == PAR_EVEN) == evenT) FW[k] = fma(x, __ldg(p.wW[k] + jm), FW[k]);
@@ -513,7 +514,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         const double lam2 = lam * lam;
         const double inv = kInv4Pi / fma(lam2, BN, FN);
 #pragma unroll
-        for (int k = 0; k < kMmaMaxSlots; ++k)
+        for (int k = 0; k < NC - 1; ++k)
             if (k < p.nslot) Xi[k] = fma(lam2, BW[k], FW[k]) * inv;
     }
     if (writes) {
@@ -563,10 +564,14 @@ cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s)
 {
     if (p.ntiles <= 0) return cudaSuccess;
     static_assert(kOccupancySmem <= 48 * 1024, "within the default dynamic shared memory limit");
-    if (fam00)
-        k_coupling_mma<true><<<(unsigned)p.ntiles, 128, kOccupancySmem, s>>>(p);
-    else
-        k_coupling_mma<false><<<(unsigned)p.ntiles, 128, kOccupancySmem, s>>>(p);
+    const unsigned grid = (unsigned)p.ntiles;
+    if (p.nslot + 1 <= 8) {
+        if (fam00) k_coupling_mma<true, 8><<<grid, 128, kOccupancySmem, s>>>(p);
+        else k_coupling_mma<false, 8><<<grid, 128, kOccupancySmem, s>>>(p);
+    } else {
+        if (fam00) k_coupling_mma<true, 16><<<grid, 128, kOccupancySmem, s>>>(p);
+        else k_coupling_mma<false, 16><<<grid, 128, kOccupancySmem, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
