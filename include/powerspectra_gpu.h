@@ -132,11 +132,12 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
-/* In chosen mode, the TT slots of a set with at least 5 of them, and its ++
- * and -- slots when there are at least 5 of those, are computed by the
- * tensor-core kernels: one generation of the (0 0 0) or (2 -2 0) family for
- * up to 15 windows, contracted by BF16 tcgen05 MMAs in a three-part split with
- * FP32 accumulators and float-float totals (same 1e-6 bar).  Their waits on
+/* In chosen mode, the TT slots of a set when there are more than 8 of them,
+ * and its ++ and -- slots when there are more than 8 of those (more than one
+ * CUDA-core group holds), are computed by the tensor-core kernels: one
+ * generation of the (0 0 0) or (2 -2 0) family for up to 15 windows,
+ * contracted by BF16 tcgen05 MMAs in a three-part split with FP32
+ * accumulators and float-float totals (same 1e-6 bar).  Their waits on
  * the tensor core are bounded: a wait that gives up is reported as
  * PS_ERR_TIMEOUT by the next ps_synchronize or host-pointer call. */
 /* The same with host spectra and host matrices: returns when every M is

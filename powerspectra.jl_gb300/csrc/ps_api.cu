@@ -411,8 +411,11 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 struct Slot {
     int k, s;
 };
-// Fewest slots of one kind (TT, or ++ and --) for which a chosen-mode set takes a tensor-core kernel.
-constexpr int kMmaMinSlots = 5;
+// Fewest slots of one kind (TT, or ++ and --) for which a chosen-mode set takes a tensor-core kernel:
+// more than one CUDA-core group holds (ps::kMaxWin), so that one family generation replaces two or more.
+// Measured on the lmax 8191 set: 13 ++/-- slots take 567 ms in one tensor-core launch against 920 ms
+// in two CUDA-core groups, while 7 TT slots take 332 ms there against 290 ms in one CUDA-core group.
+constexpr int kMmaMinSlots = ps::kMaxWin + 1;
 template <typename Used>
 static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {
@@ -830,7 +833,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
         base.wlen = wlen;
         // chosen mode: the TT slots (00 family) and the ++ / -- slots (22 family) of a set, each
         // kind with at least kMmaMinSlots slots, go to the tensor-core kernels, up to kMmaMaxSlots
-        // windows per launch
+        // windows per launch; the rest go to the CUDA-core kernels in groups of up to 8
         std::vector<Slot> mma00, mma22;
         if (mode == PS_MODE_CHOSEN && c->tensor_cores)
             for (int k = 0; k < K; ++k)

@@ -1,5 +1,5 @@
 """The tensor-core coupling kernels (k_coupling_mma): the TT slots and the ++ /
--- slots of a chosen-mode set, each kind with at least 5 slots; one (0 0 0) or
+-- slots of a chosen-mode set, each kind with more than 8 slots; one (0 0 0) or
 (2 -2 0) family generation for up to 15 windows, the window contraction as BF16
 tcgen05 MMAs (three-part split, fresh FP32 accumulator per 16 steps,
 float-float totals).
@@ -58,8 +58,8 @@ def _run_set(ctx, Ws, slots, lmin, lmax, pad=3, tensor_cores=True, mode="chosen"
                                         (5, 0, "2L1"), (1, 0, "2L1"), (0, 0, "L1"), (33, 2, "2L1")])
 def test_mma_vs_oracle_small(ctx, L, lmin, nWk):
     nW = {"2L1": 2 * L + 1, "L1": L + 1, "short": max(L // 2, 1)}[nWk]
-    Ws = [_W(nW, seed=10 + k, fsky=0.4 + 0.08 * k) for k in range(6)]
-    slots = [(0, 2), (0, 3), (1, 2), (2, 3), (3, 2), (3, 3)] + [(k, 0) for k in range(1, 6)]
+    Ws = [_W(nW, seed=10 + k, fsky=0.4 + 0.04 * k) for k in range(10)]
+    slots = [(k, s) for k in range(5) for s in (2, 3)] + [(k, 0) for k in range(1, 10)]
     got = _run_set(ctx, Ws, slots, lmin, L)
     for (k, s), G in got.items():
         assert np.all(np.isfinite(G)), (k, s)
@@ -81,8 +81,8 @@ def test_mma_fifteen_windows_and_a_second_launch(ctx):
 def test_mma_negative_windows(ctx):
     """Windows with negative entries: the sums cancel; measured against the sum of |terms|."""
     L = 150
-    Ws = [_W(2 * L + 1, seed=60 + k) * np.where(np.arange(2 * L + 1) % (5 + k) == 0, -1.0, 1.0) for k in range(5)]
-    slots = [(0, 2), (0, 3), (1, 2), (1, 3), (2, 2)] + [(k, 0) for k in range(5)]
+    Ws = [_W(2 * L + 1, seed=60 + k) * np.where(np.arange(2 * L + 1) % (5 + k) == 0, -1.0, 1.0) for k in range(9)]
+    slots = [(k, s) for k in range(5) for s in (2, 3)] + [(k, 0) for k in range(9)]
     got = _run_set(ctx, Ws, slots, 0, L)
     for (k, s), G in got.items():
         R = o.inner_mcm(s, Ws[k], 0, L)
@@ -95,12 +95,12 @@ def test_mma_wide_dynamic_range(ctx):
     l = np.arange(2 * L + 1, dtype=np.float64)
     base = 1e-3 * (l + 1) ** -2 * np.exp(-l * (l + 1) / (2 * 150.0 ** 2))
     Ws = []
-    for k in range(5):
+    for k in range(9):
         W = base * (1.0 + 0.1 * k)
-        W[0] += 4 * np.pi * (0.3 + 0.1 * k)
+        W[0] += 4 * np.pi * (0.3 + 0.05 * k)
         Ws.append(W)
     assert Ws[0][-1] < 1e-90
-    slots = [(0, 2), (0, 3), (1, 2), (1, 3), (2, 2), (2, 3)] + [(k, 0) for k in range(5)]
+    slots = [(k, s) for k in range(5) for s in (2, 3)] + [(k, 0) for k in range(9)]
     got = _run_set(ctx, Ws, slots, 0, L)
     ref = _run_set(ctx, Ws, slots, 0, L, mode="plain")
     for sl in slots:
@@ -119,7 +119,10 @@ def test_mma_matches_plain_fp64_full_size(ctx):
 
 
 def test_mma_agrees_with_cuda_core_path(ctx):
-    """The same set with the tensor-core kernels switched off: both within 2e-6 of each other."""
+    """The same set with the tensor-core kernels switched off: both within 2e-6 of each other,
+    and the routing itself: the 10 ++/-- slots (more than 8) take the tensor-core kernel, so their
+    results differ from the CUDA-core kernel's in the last bits; the 5 TT slots (8 or fewer) take
+    the CUDA-core kernel either way and agree bit for bit."""
     L = 700
     Ws = [_W(2 * L + 1, seed=80 + k, fsky=0.5 + 0.05 * k) for k in range(5)]
     slots = [(k, s) for k in range(5) for s in (0, 2, 3)]
@@ -127,17 +130,21 @@ def test_mma_agrees_with_cuda_core_path(ctx):
     b = _run_set(ctx, Ws, slots, 2, L, tensor_cores=False)
     for sl in slots:
         assert max_err_scaled(a[sl], b[sl], np.abs(b[sl])) < 2 * TOL, sl
+        if sl[1] == 0:
+            assert np.array_equal(a[sl], b[sl]), sl
+        else:
+            assert not np.array_equal(a[sl], b[sl]), sl
 
 
 def test_mma_lmax_8191_sampled_rows(ctx):
-    """lmax 8191, nW 16383: 13 ++/-- and 5 TT slots, sampled rows and columns against the oracle."""
+    """lmax 8191, nW 16383: 13 ++/-- and 9 TT slots, sampled rows and columns against the oracle."""
     from powerspectra_gpu import synthetic as syn
     big = syn.large_set(K=13)
     L, Ws = big["lmax"], big["W"]
-    slots = [(k, 2 if k % 2 == 0 else 3) for k in range(13)] + [(k, 0) for k in range(5)]
+    slots = [(k, 2 if k % 2 == 0 else 3) for k in range(13)] + [(k, 0) for k in range(9)]
     got = _run_set(ctx, Ws, slots, 0, L, pad=0)
     rows = [0, 1, 2, 701, 4094, 8000, 8191]
-    for (k, s) in [(0, 2), (1, 3), (12, 2), (0, 0), (4, 0)]:
+    for (k, s) in [(0, 2), (1, 3), (12, 2), (0, 0), (8, 0)]:
         R = o.inner_mcm(s, Ws[k], 0, L, rows=rows)
         G = got[k, s]
         for r in rows:
@@ -148,8 +155,8 @@ def test_mma_lmax_8191_sampled_rows(ctx):
 def test_mma_host_entry_point(ctx):
     """ps_mcm_set (host spectra, page-locked and pageable outputs) through the tensor-core kernels."""
     L = 300
-    Ws = [_W(2 * L + 1, seed=90 + k) for k in range(5)]
-    slots = {(0, 2), (0, 3), (1, 2), (1, 3), (2, 2), (2, 3), (0, 0), (1, 0), (2, 0), (3, 0), (4, 0)}
+    Ws = [_W(2 * L + 1, seed=90 + k) for k in range(9)]
+    slots = {(k, s) for k in range(5) for s in (2, 3)} | {(k, 0) for k in range(9)}
     n = L + 1
     outs = {}
     for i, sl in enumerate(sorted(slots)):
