@@ -542,7 +542,7 @@ def _finish(ctx, wl, args, mode, kernel_ms, peak64, peak32, world, elapsed, valu
     return 0
 
 
-SET_CONFIGS = ("batched_64", "large_set", "cov_2508")
+SET_CONFIGS = ("batched_64", "batched_small_256", "large_set", "cov_2508")
 
 
 def _set_problems(name, lmax=0):
@@ -550,14 +550,16 @@ def _set_problems(name, lmax=0):
 
     batched_64: 64 problems, lmax drawn from {511, ..., 6143}, K in 1..16 seeded mask
       spectra each, spin 0 (M00 per spectrum) or spin 2 (M++ and M-- per spectrum).
+    batched_small_256: 256 small problems, lmax drawn from {64, ..., 1023}, K in 1..4, spin 0
+      or 2: the persistent queue against one launch per window group and per-problem calls.
     large_set: the large_8191 workload (lmax 8191, nW 16383, K = 20 spectra; spectrum k gives
       TT (k % 3 == 0), EE = M++ (k % 3 == 1) or BB = M-- (k % 3 == 2): 20 matrices of 8192^2,
       10.7 GB) as one ps_mcm_set_device call per spin case, against the persistent batch graph.
     """
     from powerspectra_gpu import synthetic as syn
-    if name == "batched_64":
+    if name in ("batched_64", "batched_small_256"):
         out = []
-        for pr in syn.batched_problems():
+        for pr in (syn.batched_problems() if name == "batched_64" else syn.small_batch()):
             out.append({"lmin": 0, "lmax": pr["lmax"], "cases": 0x1 if pr["spin"] == 0 else 0xC,
                         "nW": pr["lmax"] + 1, "W": pr["W"]})
         return out
@@ -651,7 +653,27 @@ def run_set(args):
                              "ldm": n, "W": [d.data_ptr() for d in dW], "M": pc, "Mp": pp})
         elements = sum(int(c.shape[0]) ** 2 for c, _ in mats)
         tune = ctx.batch_autotune(prob_dev[:min(len(prob_dev), 8)]) if args.config == "batched_64" else None
-        ctx.batch_prepare(prob_dev)
+        if args.config == "batched_small_256":
+            # the persistent kernel (4-slot groups, full occupancy) against the launch form
+            # (one launch per window group) on the same problems, each replayed from a CUDA graph
+            forms = {}
+            for name, bps in (("persistent", 0), ("launch_form", -1)):
+                ctx.batch_prepare(prob_dev, group_slots=4, blocks_per_sm=bps)
+                for _ in range(max(args.warmup, 3)):
+                    ctx.batch_graph_launch()
+                forms[name] = {"ms_per_step": ev_time(ctx.batch_graph_launch, args.steps) * 1e3}
+                forms[name]["rows"] = [c[[0, c.shape[0] // 2, c.shape[0] - 1]].clone() for c, _ in mats]
+            dd = 0.0
+            for a, b in zip(forms["persistent"]["rows"], forms["launch_form"]["rows"]):
+                den = torch.where(b == 0, torch.ones_like(b), b.abs())
+                dd = max(dd, float(((a - b).abs() / den).max().item()))
+            line["batch_forms"] = {k: {"ms_per_step": v["ms_per_step"]} for k, v in forms.items()}
+            line["batch_forms"]["persistent_over_launch_form"] = (forms["launch_form"]["ms_per_step"]
+                                                                  / forms["persistent"]["ms_per_step"])
+            line["batch_forms"]["max_rel_diff"] = dd
+            ctx.batch_prepare(prob_dev, group_slots=4, blocks_per_sm=0)
+        else:
+            ctx.batch_prepare(prob_dev)
 
         def plain():
             for pr in prob_dev:

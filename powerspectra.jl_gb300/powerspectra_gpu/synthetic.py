@@ -110,6 +110,11 @@ def batched_problems(n=64, seed=4, lmax_choices=(511, 1023, 2047, 3071, 4095, 61
     return probs
 
 
+def small_batch(n=256, seed=7, lmax_choices=(64, 96, 128, 192, 256, 384, 512, 768, 1023), kmax=4):
+    """Many small uneven problems (where a launch per window group is mostly ramp and tail)."""
+    return batched_problems(n=n, seed=seed, lmax_choices=lmax_choices, kmax=kmax)
+
+
 # ---- configuration 5: large coupling set, lmax 8191 --------------------------------------------
 def large_set(lmax=8191, K=20, seed=5):
     nW = 2 * lmax + 1
