@@ -17,7 +17,8 @@
                       (test/data/theory.csv: cltt, clte, clee, clbb; noise.csv:
                       nltt, nlee; l = 0..767), read from the reference checkout.
 
-Run from the repository root:  python tests/golden/make_golden.py [--ref PATH]
+Run from the repository root:  python tests/golden/make_golden.py --ref PATH
+(PATH: a checkout of PowerSpectra.jl; it is needed for every fixture but oracle_small.npz).
 """
 import argparse
 import json
@@ -132,9 +133,11 @@ def make_oracle_small():
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="a checkout of PowerSpectra.jl (its test/ folder is read)")
     ap.add_argument("--only", default="all")
     a = ap.parse_args()
+    if a.only != "oracle" and not a.ref:
+        ap.error("--ref PATH (a PowerSpectra.jl checkout) is required for the fixtures read from its tests")
     if a.only in ("all", "namaster"):
         make_namaster(a.ref)
     if a.only in ("all", "decouple"):
