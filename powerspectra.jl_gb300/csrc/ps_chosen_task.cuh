@@ -56,6 +56,56 @@ __device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 belo
     return d < -126 ? 0.0f : __int_as_float((d + 127) << 23);
 }
 
+// A running sum of FP32 chunk partials c 2^e (e: the slice exponent of the
+// chunk, the same for every lane of the warp).  ChunkSum<false> adds them into
+// FP64 (a conversion and a DFMA per add); ChunkSum<true> keeps the sum on the
+// FP32 pipe as a float-float value relative to a running power of two R: when
+// a chunk's exponent exceeds R the value is rescaled by 2^(R - e) (exact) and R
+// moves up, then c 2^(e - R) is added with Knuth's two-sum.  On GB300 the FP64
+// pipe is a small fraction of the FP32 one, and kernels that flush many
+// windows per chunk were bound by it.
+template <bool FF>
+struct ChunkSum;
+template <>
+struct ChunkSum<false> {
+    double v;
+    __device__ __forceinline__ void zero() { v = 0.0; }
+    __device__ __forceinline__ void add(float c, int e) { v = fma((double)c, pow2d(e), v); }
+    __device__ __forceinline__ double get() const { return v; }
+};
+template <>
+struct ChunkSum<true> {
+    float h, l;
+    int R;
+    __device__ __forceinline__ void zero()
+    {
+        h = l = 0.0f;
+        R = kZeroExp;
+    }
+    __device__ __forceinline__ void add(float c, int e)
+    {
+        if (e > R) {  // warp-uniform: e is the slice exponent
+            const float sc = pow2f_or_zero(R - e);
+            h *= sc;
+            l *= sc;
+            R = e;
+        }
+        const float v = __fmul_rn(c, pow2f_or_zero(e - R));
+        const float s = __fadd_rn(h, v);
+        const float bb = __fsub_rn(s, h);
+        const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+        h = s;
+        l = __fadd_rn(l, err);
+    }
+    __device__ __forceinline__ double get() const { return ldexp((double)h + (double)l, R); }
+};
+// The 8-slot kernels of the (0 0 0) family alone (up to 16 window sums per chunk
+// against a cheap two-term recurrence) keep their sums on the FP32 pipe; the
+// others keep FP64, where the FP64 pipe is not the limit and the running
+// exponents would push their registers past 128 into spills.
+template <int NWIN, bool N22>
+constexpr bool chunk_sums_ff() { return NWIN >= 8 && !N22; }
+
 // Window slices move in two stages.  fetch_slice issues asynchronous copies
 // (cp.async, 8 bytes per lane and slot) of the raw (mantissa, exponent) slots
 // [base, base + kSlots) into shared memory; they land while the previous chunk
@@ -410,10 +460,17 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
     F.w = (float)(ws * (2 * jmin + 1));
     B.f2 = ff_make(1.0f); B.f2o = ff_make(0.0f); B.f0 = ff_make(1.0f);
     B.w = (float)(ws * (2 * jmax + 1));
-    double FW[NWIN], BW[NWIN];
+    constexpr bool FFS = chunk_sums_ff<NWIN, N22>();
+    ChunkSum<FFS> SFW[NWIN], SBW[NWIN], SFN0, SFN2, SBN0, SBN2;
 #pragma unroll
-    for (int k = 0; k < NWIN; ++k) FW[k] = BW[k] = 0.0;
-    double FN0 = 0.0, FN2 = 0.0, BN0 = 0.0, BN2 = 0.0;
+    for (int k = 0; k < NWIN; ++k) {
+        SFW[k].zero();
+        SBW[k].zero();
+    }
+    SFN0.zero();
+    SFN2.zero();
+    SBN0.zero();
+    SBN2.zero();
 
     int2* rF = raw;                  // raw forward slices, [NWIN][kSlots]
     int2* rB = raw + NWIN * kSlots;  // raw backward slices
@@ -478,25 +535,29 @@ __device__ __forceinline__ bool chosen_xi(const CouplingParams& p, const int l1,
             tab_fwd<N00, N22, false, WS4>(F, tb, s, lane);
             tab_bwd<N00, N22, false, WS4>(B, tb, s, lane);
         }
-        // ---- FP64 flush of the chunk sums ----
+        // ---- flush of the chunk sums (the norm sums carry the weight factor ws = 2^(WS4 ? 2 : 0)) ----
 #pragma unroll
         for (int k = 0; k < NWIN; ++k) {
-            FW[k] = fma((double)cF[k], pow2d(eF[k]), FW[k]);
-            BW[k] = fma((double)cB[k], pow2d(eB[k]), BW[k]);
+            SFW[k].add(cF[k], eF[k]);
+            SBW[k].add(cB[k], eB[k]);
         }
-        if (WS4) {
-            FN0 = fma((double)n0F, 0.25, FN0);
-            FN2 = fma((double)n2F, 0.25, FN2);
-            BN0 = fma((double)n0B, 0.25, BN0);
-            BN2 = fma((double)n2B, 0.25, BN2);
-        } else {
-            FN0 += (double)n0F;
-            FN2 += (double)n2F;
-            BN0 += (double)n0B;
-            BN2 += (double)n2B;
+        if (N00) {
+            SFN0.add(n0F, WS4 ? -2 : 0);
+            SBN0.add(n0B, WS4 ? -2 : 0);
+        }
+        if (N22) {
+            SFN2.add(n2F, WS4 ? -2 : 0);
+            SBN2.add(n2B, WS4 ? -2 : 0);
         }
         __syncwarp();
     }
+    double FW[NWIN], BW[NWIN];
+#pragma unroll
+    for (int k = 0; k < NWIN; ++k) {
+        FW[k] = SFW[k].get();
+        BW[k] = SBW[k].get();
+    }
+    double FN0 = SFN0.get(), FN2 = SFN2.get(), BN0 = SBN0.get(), BN2 = SBN2.get();
 
     // last forward point t = T (j = jm), in FP64; its parity is that of T
     const int jm = jmin + T;

@@ -219,27 +219,40 @@ __device__ __forceinline__ void step22(Sweep22& S, ff rho, ff r, float dw)
     S.f = ff_neg(ff_add_raw(x, y));
     S.w += dw;
 }
-// forward step t of lane l2 (parity p of t): g[t] and f[2 l2 + t]
-__device__ __forceinline__ void fwd_step(Sweep22& S, const CoefRing& R, int p, int t, int l2)
+// Ring slots of one pair of steps (tau even, then odd) of a lane: t, v = 2 l2 + t of the
+// forward step and t of the backward step are even at the even step, so both steps use the
+// same slot of each; u = 2 l2 - t of the backward step is even at the even step and one less at
+// the odd one.
+struct PairSlots {
+    int g, f, gb, fb0, fb1;
+};
+__device__ __forceinline__ PairSlots pair_slots(int tf_even, int tb_even, int l2)
 {
-    const ffpair g = R.g[p][ring_slot(t)], f = R.f[p][ring_slot(2 * l2 + t)];
+    const int u0 = 2 * l2 - tb_even;
+    return PairSlots{ring_slot(tf_even), ring_slot(2 * l2 + tf_even), ring_slot(tb_even), ring_slot(u0),
+                     ring_slot(u0 - 1)};
+}
+// forward step of parity p: g[t] and f[2 l2 + t]
+__device__ __forceinline__ void fwd_step(Sweep22& S, const CoefRing& R, int p, const PairSlots& q)
+{
+    const ffpair g = R.g[p][q.g], f = R.f[p][q.f];
     step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), 8.0f);
 }
-// backward step t: g[t] and fb[2 l2 - t]
-__device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, int t, int l2)
+// backward step of parity p: g[t] and fb[2 l2 - t]
+__device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, const PairSlots& q)
 {
-    const ffpair g = R.g[p][ring_slot(t)], f = R.fb[p][ring_slot(2 * l2 - t)];
+    const ffpair g = R.g[p][q.gb], f = R.fb[p][p ? q.fb1 : q.fb0];
     step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), -8.0f);
 }
-// (0 0 0) family at an odd step t: f(j+1) = -rho f(j-1), rho = a(j)/a(j+1) (forward) or
+// (0 0 0) family at the odd step: f(j+1) = -rho f(j-1), rho = a(j)/a(j+1) (forward) or
 // a(j+1)/a(j) (backward), the same ring entries as the (2 -2 0) step
-__device__ __forceinline__ void fwd_step00(ff& f0, const CoefRing& R, int t, int l2)
+__device__ __forceinline__ void fwd_step00(ff& f0, const CoefRing& R, const PairSlots& q)
 {
-    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][ring_slot(t)].rho, R.f[1][ring_slot(2 * l2 + t)].rho), f0));
+    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][q.g].rho, R.f[1][q.f].rho), f0));
 }
-__device__ __forceinline__ void bwd_step00(ff& f0, const CoefRing& R, int t, int l2)
+__device__ __forceinline__ void bwd_step00(ff& f0, const CoefRing& R, const PairSlots& q)
 {
-    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][ring_slot(t)].rho, R.fb[1][ring_slot(2 * l2 - t)].rho), f0));
+    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][q.gb].rho, R.fb[1][q.fb1].rho), f0));
 }
 
 // sqrt(X / Y) for the last forward points (X, Y up to 2^64: the scaling keeps X Y in range)
@@ -371,25 +384,25 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         for (int s2 = 0; s2 < kK; s2 += 2) {
             float xf[2], xb[2];
             const int tau0 = q * kK + s2;
+            const PairSlots ps2 = pair_slots(tau0 + fofs, tau0 + bofs, l2);
             if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
                 // steady state: every lane that runs is inside both sweeps, so both steps run
                 // unconditionally (their two dependency chains interleave); lanes that do not
                 // run compute values that are masked out of x and never written
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
-                    const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
                     if (F00) {
                         xf[e] = e == 0 && runs ? sq(F.f) : 0.0f;
                         xb[e] = e == 0 && runs ? sq(B.f) : 0.0f;
                         if (e == 1) {
-                            fwd_step00(F.f, R, tf, l2);
-                            bwd_step00(B.f, R, tb, l2);
+                            fwd_step00(F.f, R, ps2);
+                            bwd_step00(B.f, R, ps2);
                         }
                     } else {
                         xf[e] = runs ? sq(F.f) : 0.0f;
                         xb[e] = runs ? sq(B.f) : 0.0f;
-                        fwd_step(F, R, e, tf, l2);
-                        bwd_step(B, R, e, tb, l2);
+                        fwd_step(F, R, e, ps2);
+                        bwd_step(B, R, e, ps2);
                     }
                 }
             } else {
@@ -402,19 +415,19 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 if (tf >= 0 && tf < T) {
                     if (F00) {
                         if (e == 0) xf[e] = sq(F.f);
-                        else fwd_step00(F.f, R, tf, l2);
+                        else fwd_step00(F.f, R, ps2);
                     } else {
                         xf[e] = sq(F.f);
-                        fwd_step(F, R, e, tf, l2);
+                        fwd_step(F, R, e, ps2);
                     }
                 }
                 if (tb >= 0 && tb < T) {
                     if (F00) {
                         if (e == 0) xb[e] = sq(B.f);
-                        else bwd_step00(B.f, R, tb, l2);
+                        else bwd_step00(B.f, R, ps2);
                     } else {
                         xb[e] = sq(B.f);
-                        bwd_step(B, R, e, tb, l2);
+                        bwd_step(B, R, e, ps2);
                     }
                 }
             }
