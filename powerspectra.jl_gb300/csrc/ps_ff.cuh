@@ -25,6 +25,14 @@ __device__ __forceinline__ ff fast_two_sum(float a, float b)
     return ff{s, e};
 }
 
+// a + b = s + e exactly, for any a and b (Knuth)
+__device__ __forceinline__ ff two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
 __device__ __forceinline__ ff two_prod(float a, float b)
 {
     float p = __fmul_rn(a, b);

@@ -29,8 +29,8 @@
 // 24 bits) and D is formed from six products (all but the three smallest),
 // ordered so that the hi x hi product is added last: the tensor core rounds
 // its FP32 accumulation toward zero, so each 16-step D starts from zero and
-// takes one such rounding at full scale.  Each D is added into float-float
-// totals on the CUDA cores.  B is scaled per 16-step block by a running power
+// takes one such rounding at full scale.  Each D is added to float-float
+// totals on the CUDA cores (into the low word; renormalised every fourth block).  B is scaled per 16-step block by a running power
 // of two (block floating point; windows span 1e-45), the same role the slice
 // exponents play in the chosen kernel.  The last forward point, the match of
 // the two sweeps, the normalisation and the outputs are FP64.
@@ -78,6 +78,7 @@ __device__ __forceinline__ uint32_t a_col(int buf, int sweep, int plane)
 struct __align__(128) Smem {
     unsigned char B[2][2][kPlanes][kBPlane];  // [buffer][sweep][part]: K-major BF16, core matrices 8 x 16 B
     float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
+    int grew[3][4];                           // per warp of build_B: some column's scale grew (slot q % 3)
     int ref[2][kMmaCols];                     // running exponent of B's scale per sweep and column
     uint64_t mbar;
     uint32_t tmem;
@@ -143,6 +144,9 @@ __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int
         sm.ref[s][n] = rnew;
         sm.rescale[q % 3][s][n] = rold == rnew ? 1.0f : pow2f_or_zero(rold - rnew);
     }
+    // warps 0, 1 build sweep 0 and warps 2, 3 sweep 1: the flush reads two flags, not 16 factors
+    const unsigned grew = __ballot_sync(0xffffffffu, qd == 0 && rold != rnew);
+    if (lane == 0) sm.grew[q % 3][tid >> 5] = grew != 0u;
     float v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) v[u] = m[u] * pow2f_or_zero(e[u] - rnew);
@@ -263,26 +267,57 @@ __device__ __forceinline__ ff rho00(ff X, ff Y)
     return ff{r.h * 0x1p16f, r.l * 0x1p16f};
 }
 
-// The ring values of block q (first = true: all 78 of each table; otherwise the 16
-// that block q needs beyond block q - 1), for warp row l1 = r0 + 2w and lanes
-// l2 = c0 + 2i.
-__device__ __forceinline__ void build_rings(CoefRing& R, int q, bool first, int w, int l1, int c0, int lane)
+// The ring values of block q, for warp row l1 = r0 + 2w and lanes l2 = c0 + 2i:
+// t in [tlo, tlo + 77], v in [vlo, vlo + 77], u in [ulo, ulo + 77].
+__device__ __forceinline__ int ring_tlo(int q, int w) { return q * kK - 68 + 2 * w; }
+__device__ __forceinline__ int ring_vlo(int q, int w, int c0) { return 2 * c0 + 2 * w + q * kK - 6; }
+__device__ __forceinline__ int ring_ulo(int q, int w, int c0) { return 2 * c0 - 2 * w + 53 - q * kK; }
+
+// All 78 values of each table (the first block).
+__device__ __forceinline__ void build_rings_first(CoefRing& R, int w, int l1, int c0, int lane)
 {
-    const int tau0 = q * kK;
-    const int tlo = tau0 - 68 + 2 * w;                 // t: [tlo, tlo + 77]
-    const int vlo = 2 * c0 + 2 * w + tau0 - 6;         // v: [vlo, vlo + 77]
-    const int ulo = 2 * c0 - 2 * w + 130 - tau0 - 77;  // u: [ulo, ulo + 77]
-    if (first) {
-        for (int e = lane; e < 78; e += 32) {
-            ring_g(R, tlo + e, l1);
-            ring_f(R, vlo + e, l1);
-            ring_fb(R, ulo + e, l1);
-        }
-    } else if (lane < 16) {
-        ring_g(R, tlo + 62 + lane, l1);  // the top 16 of t
-        ring_fb(R, ulo + lane, l1);      // the bottom 16 of u
-    } else {
-        ring_f(R, vlo + 62 + lane - 16, l1);  // the top 16 of v
+    const int tlo = ring_tlo(0, w), vlo = ring_vlo(0, w, c0), ulo = ring_ulo(0, w, c0);
+    for (int e = lane; e < 78; e += 32) {
+        ring_g(R, tlo + e, l1);
+        ring_f(R, vlo + e, l1);
+        ring_fb(R, ulo + e, l1);
+    }
+}
+
+// The 16 values per table that block q needs beyond block q - 1: the top 16 of t and v, the
+// bottom 16 of u.  With s(x) = 1/sqrt(P(x)) for the table's products P,
+//   g, f entry x  = (sqrt(P(x) / P(x+1)), 1/sqrt(P(x+1))) = (P(x) s(x) s(x+1), s(x+1)),
+//   fb entry x    = (sqrt(P(x+1) / P(x)), 1/sqrt(P(x)))   = (P(x+1) s(x+1) s(x), s(x)),
+// so a new entry takes one float-float 1/sqrt; the neighbouring s comes from the next lane or,
+// at the edge of the 16, from the entry of block q - 1 that holds it as its r.  P(x) is 0 only
+// at the first step of a sweep, where the entry's rho is 0.  Pass 1: lanes 0-15 take g, lanes
+// 16-31 f (no divergence); pass 2: lanes 0-15 take fb.
+__device__ __forceinline__ void build_rings_next(CoefRing& R, int q, int w, int l1, int c0, int lane)
+{
+    const int e = lane & 15;
+    {
+        const bool isf = lane >= 16;
+        const int x = isf ? ring_vlo(q, w, c0) + 62 + e : ring_tlo(q, w) + 62 + e;
+        // g: P(x) = x (2 l1 + 1 - x), P(x + 1) = (x + 1)(2 l1 - x)
+        // f: P(x) = (x - 2 l1)(x + 1), P(x + 1) = (x + 1 - 2 l1)(x + 2)
+        const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
+        const ff s1 = ff_rsqrt(two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
+        ff s0{__shfl_up_sync(0xffffffffu, s1.h, 1, 16), __shfl_up_sync(0xffffffffu, s1.l, 1, 16)};
+        ffpair(*tab)[kRing] = isf ? R.f : R.g;
+        if (e == 0) s0 = tab[(x - 1) & 1][ring_slot(x - 1)].r;
+        const ff P0 = two_prod(a0, b0);
+        const ff rho = P0.h > 0.0f ? ff_mul(ff_mul_raw(P0, s0), s1) : ff_make(0.0f);
+        tab[x & 1][ring_slot(x)] = ffpair{rho, s1};
+    }
+    if (lane < 16) {
+        const int x = ring_ulo(q, w, c0) + e;  // Fb(x) = x (2 l1 + 1 + x)
+        const float a0 = (float)x, b0 = (float)(2 * l1 + 1 + x);
+        const ff s0 = ff_rsqrt(two_prod(a0, b0));
+        ff s1{__shfl_down_sync(0x0000ffffu, s0.h, 1, 16), __shfl_down_sync(0x0000ffffu, s0.l, 1, 16)};
+        if (e == 15) s1 = R.fb[(x + 1) & 1][ring_slot(x + 1)].r;
+        const ff P1 = two_prod(a0 + 1.0f, b0 + 1.0f);
+        const ff rho = P1.h > 0.0f ? ff_mul(ff_mul_raw(P1, s1), s0) : ff_make(0.0f);
+        R.fb[x & 1][ring_slot(x)] = ffpair{rho, s0};
     }
 }
 
@@ -292,14 +327,16 @@ __device__ __forceinline__ float sq(const ff& f)
     return __fmul_rn(g, g);
 }
 
-// totals += D (Knuth two-sum on the high words)
-__device__ __forceinline__ void fold(ff& T, float d)
+// The totals take each block's D into their low word (one FP32 add), and the columns
+// n = R (mod 4) are renormalised by a two-sum at blocks q = R (mod 4).  So a low word sums at
+// most four blocks between renormalisations: at most four roundings of 2^-24 relative to those
+// blocks' sum, against one rounding of the tensor core's truncating accumulation per block.
+template <int R, int NC>
+__device__ __forceinline__ void renorm(ff (&t)[NC], int ncols)
 {
-    const float s = __fadd_rn(T.h, d);
-    const float bb = __fsub_rn(s, T.h);
-    const float err = __fadd_rn(__fsub_rn(T.h, __fsub_rn(s, bb)), __fsub_rn(d, bb));
-    T.h = s;
-    T.l = __fadd_rn(T.l, err);
+#pragma unroll
+    for (int n = R; n < NC; n += 4)
+        if (n < ncols) t[n] = two_sum(t[n].h, t[n].l);
 }
 
 // NC: columns folded into the totals (8 or 16; at least nslot + 1)
@@ -329,7 +366,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
     build_B(p, sm, 0, r0, c0, tid);
-    build_rings(R, 0, true, warp, l1, c0, lane);
+    build_rings_first(R, warp, l1, c0, lane);
     __syncwarp();
 
     // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
@@ -353,26 +390,28 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             umma::ld_x16(tlane + (uint32_t)(s * kMmaCols), dv);
             // the totals move to block q's scale where its exponent grew (the same for every
             // thread: a uniform branch, taken only when some window's scale changed)
-            const float4* rs = reinterpret_cast<const float4*>(&sm.rescale[q % 3][s][0]);
-            float resc[NC];
+            if (sm.grew[q % 3][2 * s] | sm.grew[q % 3][2 * s + 1]) {
+                const float4* rs = reinterpret_cast<const float4*>(&sm.rescale[q % 3][s][0]);
 #pragma unroll
-            for (int v = 0; v < NC / 4; ++v) {
-                const float4 r4 = rs[v];
-                resc[4 * v] = r4.x; resc[4 * v + 1] = r4.y; resc[4 * v + 2] = r4.z; resc[4 * v + 3] = r4.w;
-            }
-            bool any = false;
+                for (int v = 0; v < NC / 4; ++v) {
+                    const float4 r4 = rs[v];
+                    const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
 #pragma unroll
-            for (int n = 0; n < NC; ++n) any |= resc[n] != 1.0f;
-            if (any) {
-#pragma unroll
-                for (int n = 0; n < NC; ++n) {
-                    tot[s][n].h *= resc[n];
-                    tot[s][n].l *= resc[n];
+                    for (int j = 0; j < 4; ++j) {
+                        tot[s][4 * v + j].h *= rv[j];
+                        tot[s][4 * v + j].l *= rv[j];
+                    }
                 }
             }
 #pragma unroll
             for (int n = 0; n < NC; ++n)
-                if (n < ncols) fold(tot[s][n], dv[n]);
+                if (n < ncols) tot[s][n].l = __fadd_rn(tot[s][n].l, dv[n]);
+            switch (q & 3) {
+                case 0: renorm<0>(tot[s], ncols); break;
+                case 1: renorm<1>(tot[s], ncols); break;
+                case 2: renorm<2>(tot[s], ncols); break;
+                default: renorm<3>(tot[s], ncols); break;
+            }
         }
     };
 
@@ -446,7 +485,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
         if (q + 1 < nk) {
             build_B(p, sm, q + 1, r0, c0, tid);
-            build_rings(R, q + 1, false, warp, l1, c0, lane);
+            build_rings_next(R, q + 1, warp, l1, c0, lane);
         }
         umma::wait_st();
         umma::fence_smem_async();
