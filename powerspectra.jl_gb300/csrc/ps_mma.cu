@@ -79,6 +79,7 @@ struct __align__(128) Smem {
     unsigned char B[2][2][kPlanes][kBPlane];  // [buffer][sweep][part]: K-major BF16, core matrices 8 x 16 B
     float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
     int grew[3][4];                           // per warp of build_B: some column's scale grew (slot q % 3)
+    int2 stage[2][2][kMmaCols][kK];           // [q & 1][sweep][column][step]: block q's window values, fetched ahead
     int ref[2][kMmaCols];                     // running exponent of B's scale per sweep and column
     uint64_t mbar;
     uint32_t tmem;
@@ -108,30 +109,54 @@ __device__ __forceinline__ void split3(float a, float b, uint32_t (&w)[kPlanes])
     w[2] = bf2_bits(l);
 }
 
-// B of block q into buffer q & 1 (all 128 threads: thread = sweep x column x 4 steps).
-__device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int r0, int c0, int tid)
+// Whether B's element (sweep s, column n, time step tau) is a window value, and its l3.
+__device__ __forceinline__ bool b_window(const MmaParams& p, int s, int n, int tau, int r0, int c0, int& l3)
+{
+    l3 = s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+    if (l3 < 0 || l3 >= p.wlen || n >= p.nslot) return false;
+    const int par = p.parity[n];
+    return par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0);
+}
+
+// Block q covers the time steps tb .. tb + 15.
+// Start the copies of block q's window values that this thread's part of build_B needs (4
+// steps of one sweep and column, 8 bytes each) into stage[q & 1]; a block ahead, so their
+// latency is hidden behind a block of steps.
+__device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
+{
+    const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        int l3;
+        if (b_window(p, s, n, tb + 4 * qd + u, r0, c0, l3))
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(umma::smem_addr(&sm.stage[q & 1][s][n][4 * qd + u])),
+                         "l"(p.bf[n] + l3)
+                         : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// B of block q into buffer q & 1 (all 128 threads: thread = sweep x column x 4 steps), from
+// the values this thread fetched.
+__device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     float m[4];
     int e[4];
     int emax = kZeroExp;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-        const int tau = q * kK + 4 * qd + u;
-        const int l3 = s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+        const int tau = tb + 4 * qd + u;
+        int l3;
         m[u] = 0.0f;
         e[u] = kZeroExp;
-        if (l3 >= 0 && l3 < p.wlen) {
-            if (n < p.nslot) {
-                const int par = p.parity[n];
-                if (par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0)) {
-                    const int2 v = __ldg(p.bf[n] + l3);
-                    m[u] = __int_as_float(v.x);
-                    e[u] = v.y;
-                }
-            } else if (n == p.nslot) {  // the normalisation column: 2 l3 + 1
-                m[u] = frexpf((float)(2 * l3 + 1), &e[u]);
-            }
+        if (b_window(p, s, n, tau, r0, c0, l3)) {
+            const int2 v = sm.stage[q & 1][s][n][4 * qd + u];
+            m[u] = __int_as_float(v.x);
+            e[u] = v.y;
+        } else if (n == p.nslot && l3 >= 0 && l3 < p.wlen) {  // the normalisation column: 2 l3 + 1
+            m[u] = frexpf((float)(2 * l3 + 1), &e[u]);
         }
         emax = max(emax, e[u]);
     }
@@ -267,16 +292,16 @@ __device__ __forceinline__ ff rho00(ff X, ff Y)
     return ff{r.h * 0x1p16f, r.l * 0x1p16f};
 }
 
-// The ring values of block q, for warp row l1 = r0 + 2w and lanes l2 = c0 + 2i:
-// t in [tlo, tlo + 77], v in [vlo, vlo + 77], u in [ulo, ulo + 77].
-__device__ __forceinline__ int ring_tlo(int q, int w) { return q * kK - 68 + 2 * w; }
-__device__ __forceinline__ int ring_vlo(int q, int w, int c0) { return 2 * c0 + 2 * w + q * kK - 6; }
-__device__ __forceinline__ int ring_ulo(int q, int w, int c0) { return 2 * c0 - 2 * w + 53 - q * kK; }
+// The ring values of the block starting at time step tb, for warp row l1 = r0 + 2w and lanes
+// l2 = c0 + 2i: t in [tlo, tlo + 77], v in [vlo, vlo + 77], u in [ulo, ulo + 77].
+__device__ __forceinline__ int ring_tlo(int tb, int w) { return tb - 68 + 2 * w; }
+__device__ __forceinline__ int ring_vlo(int tb, int w, int c0) { return 2 * c0 + 2 * w + tb - 6; }
+__device__ __forceinline__ int ring_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 53 - tb; }
 
 // All 78 values of each table (the first block).
-__device__ __forceinline__ void build_rings_first(CoefRing& R, int w, int l1, int c0, int lane)
+__device__ __forceinline__ void build_rings_first(CoefRing& R, int tb, int w, int l1, int c0, int lane)
 {
-    const int tlo = ring_tlo(0, w), vlo = ring_vlo(0, w, c0), ulo = ring_ulo(0, w, c0);
+    const int tlo = ring_tlo(tb, w), vlo = ring_vlo(tb, w, c0), ulo = ring_ulo(tb, w, c0);
     for (int e = lane; e < 78; e += 32) {
         ring_g(R, tlo + e, l1);
         ring_f(R, vlo + e, l1);
@@ -292,12 +317,12 @@ __device__ __forceinline__ void build_rings_first(CoefRing& R, int w, int l1, in
 // at the edge of the 16, from the entry of block q - 1 that holds it as its r.  P(x) is 0 only
 // at the first step of a sweep, where the entry's rho is 0.  Pass 1: lanes 0-15 take g, lanes
 // 16-31 f (no divergence); pass 2: lanes 0-15 take fb.
-__device__ __forceinline__ void build_rings_next(CoefRing& R, int q, int w, int l1, int c0, int lane)
+__device__ __forceinline__ void build_rings_next(CoefRing& R, int tb, int w, int l1, int c0, int lane)
 {
     const int e = lane & 15;
     {
         const bool isf = lane >= 16;
-        const int x = isf ? ring_vlo(q, w, c0) + 62 + e : ring_tlo(q, w) + 62 + e;
+        const int x = isf ? ring_vlo(tb, w, c0) + 62 + e : ring_tlo(tb, w) + 62 + e;
         // g: P(x) = x (2 l1 + 1 - x), P(x + 1) = (x + 1)(2 l1 - x)
         // f: P(x) = (x - 2 l1)(x + 1), P(x + 1) = (x + 1 - 2 l1)(x + 2)
         const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
@@ -310,7 +335,7 @@ __device__ __forceinline__ void build_rings_next(CoefRing& R, int q, int w, int 
         tab[x & 1][ring_slot(x)] = ffpair{rho, s1};
     }
     if (lane < 16) {
-        const int x = ring_ulo(q, w, c0) + e;  // Fb(x) = x (2 l1 + 1 + x)
+        const int x = ring_ulo(tb, w, c0) + e;  // Fb(x) = x (2 l1 + 1 + x)
         const float a0 = (float)x, b0 = (float)(2 * l1 + 1 + x);
         const ff s0 = ff_rsqrt(two_prod(a0, b0));
         ff s1{__shfl_down_sync(0x0000ffffu, s0.h, 1, 16), __shfl_down_sync(0x0000ffffu, s0.l, 1, 16)};
@@ -354,6 +379,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const bool runs = writes && (F00 || l1 >= 2);  // the (2 -2 0) family vanishes for l1 < 2
     const int T = runs ? l1 : 0;
     const int d = l2 - l1;
+    // block q covers the time steps q kK .. q kK + 15; the sweeps run for tau in [0, r0 + kRamp)
     const int nk = (r0 + kRamp + kK - 1) / kK;  // 16-step blocks of the skewed sweeps (block-uniform)
     const int ncols = p.nslot + 1;
 
@@ -365,8 +391,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     umma::fence_after_sync();
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
-    build_B(p, sm, 0, r0, c0, tid);
-    build_rings_first(R, warp, l1, c0, lane);
+    fetch_B(p, sm, 0, 0, r0, c0, tid);
+    if (nk > 1) fetch_B(p, sm, 1, kK, r0, c0, tid);
+    build_B(p, sm, 0, 0, r0, c0, tid);
+    build_rings_first(R, 0, warp, l1, c0, lane);
     __syncwarp();
 
     // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
@@ -484,8 +512,8 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         // ---- block boundary ----
         if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
         if (q + 1 < nk) {
-            build_B(p, sm, q + 1, r0, c0, tid);
-            build_rings_next(R, q + 1, warp, l1, c0, lane);
+            build_B(p, sm, q + 1, (q + 1) * kK, r0, c0, tid);
+            build_rings_next(R, (q + 1) * kK, warp, l1, c0, lane);
         }
         umma::wait_st();
         umma::fence_smem_async();
@@ -503,6 +531,8 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 }
             umma::mma_commit(&sm.mbar);
         }
+        // stage[q & 1] was last read by build_B(q), before the barrier above
+        if (q + 2 < nk) fetch_B(p, sm, q + 2, (q + 2) * kK, r0, c0, tid);
     }
     flush(nk - 1);
     if (!ok) atomicExch(p.status, 1u);
@@ -585,11 +615,15 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     if (warp == 0) umma::tmem_free(tbase, kTmemCols);
 }
 
-// Dynamic shared memory per block: the four warps' coefficient rings, padded so
-// that residency is capped at four blocks per SM and the four blocks' tensor
-// memory (4 x 128 columns) fits the SM's 512 columns: no allocation has to wait.
-constexpr int kOccupancySmem = 40 * 1024;
+// Shared memory per block: the static Smem plus the four warps' coefficient rings
+// (dynamic), padded to the 48 KB a block may take without opting in.  That caps
+// residency at four blocks per SM, so the four blocks' tensor memory (4 x 128
+// columns) fits the SM's 512 columns: no allocation has to wait.
+constexpr int kBlockSmem = 48 * 1024;
+constexpr int kOccupancySmem = kBlockSmem - (int)sizeof(Smem);
 static_assert(4 * sizeof(CoefRing) <= kOccupancySmem, "the rings fit the block's dynamic shared memory");
+static_assert(5 * (kBlockSmem + 1024) > 228 * 1024 && 4 * (kBlockSmem + 1024) <= 228 * 1024,
+              "four blocks per SM (1 KB reserved per block)");
 
 }  // namespace
 
@@ -615,7 +649,7 @@ void mma_tile_list(int lmin, int lmax, std::vector<int2>& t)
 cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s)
 {
     if (p.ntiles <= 0) return cudaSuccess;
-    static_assert(kOccupancySmem <= 48 * 1024, "within the default dynamic shared memory limit");
+    static_assert(sizeof(Smem) + kOccupancySmem <= 48 * 1024, "within the default shared memory limit");
     const unsigned grid = (unsigned)p.ntiles;
     if (p.nslot + 1 <= 8) {
         if (fam00) k_coupling_mma<true, 8><<<grid, 128, kOccupancySmem, s>>>(p);
