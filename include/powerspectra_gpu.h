@@ -132,7 +132,7 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
-/* In chosen mode, the TT slots of a set when there are more than 8 of them,
+/* In chosen mode, the TT slots of a set when there are 5 or more of them,
  * and its ++ and -- slots when there are more than 8 of those (more than one
  * CUDA-core group holds), are computed by the tensor-core kernels: one
  * generation of the (0 0 0) or (2 -2 0) family for up to 15 windows,

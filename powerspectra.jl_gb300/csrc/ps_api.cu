@@ -411,11 +411,17 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 struct Slot {
     int k, s;
 };
-// Fewest slots of one kind (TT, or ++ and --) for which a chosen-mode set takes a tensor-core kernel:
-// more than one CUDA-core group holds (ps::kMaxWin), so that one family generation replaces two or more.
-// Measured on the lmax 8191 set: 13 ++/-- slots take 567 ms in one tensor-core launch against 920 ms
-// in two CUDA-core groups, while 7 TT slots take 332 ms there against 290 ms in one CUDA-core group.
-constexpr int kMmaMinSlots = ps::kMaxWin + 1;
+// Fewest slots of one kind for which a chosen-mode set takes a tensor-core kernel.
+// ++ and --: more than one CUDA-core group holds (ps::kMaxWin), so that one family generation
+// replaces two or more; on the lmax 8191 set 13 such slots take 487 ms in one tensor-core launch
+// against 944 ms in two CUDA-core groups, while up to 8 of them fit one CUDA-core group, which is
+// as fast or faster (at lmax 4095: 62 ms for 8 slots and 36 ms for 2, against 63-65 ms).
+// TT: the tensor-core kernel steps the (0 0 0) family two points at a time and costs about the
+// same for 1 to 15 windows (24 ms at lmax 4095), against 10.5, 16.7 and 19.4 ms for 1, 2 and 4
+// slots in the 4-slot CUDA-core kernel and 33-35 ms for 7-8 slots in the 8-slot one; at lmax 8191
+// 7 TT slots take 180 ms against 257 ms.  So TT sets of 5 or more slots take it.
+constexpr int kMmaMin22 = ps::kMaxWin + 1;
+constexpr int kMmaMin00 = 5;
 template <typename Used>
 static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {
@@ -832,7 +838,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
         }
         base.wlen = wlen;
         // chosen mode: the TT slots (00 family) and the ++ / -- slots (22 family) of a set, each
-        // kind with at least kMmaMinSlots slots, go to the tensor-core kernels, up to kMmaMaxSlots
+        // kind with at least kMmaMin00 / kMmaMin22 slots, go to the tensor-core kernels, up to kMmaMaxSlots
         // windows per launch; the rest go to the CUDA-core kernels in groups of up to 8
         std::vector<Slot> mma00, mma22;
         if (mode == PS_MODE_CHOSEN && c->tensor_cores)
@@ -840,8 +846,8 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                 for (int s = 0; s < 4; ++s)
                     if ((cases & (1u << s)) && dM[4 * k + s] && s != PS_SPIN_02)
                         (s == PS_SPIN_00 ? mma00 : mma22).push_back(Slot{k, s});
-        if ((int)mma00.size() < kMmaMinSlots) mma00.clear();
-        if ((int)mma22.size() < kMmaMinSlots) mma22.clear();
+        if ((int)mma00.size() < kMmaMin00) mma00.clear();
+        if ((int)mma22.size() < kMmaMin22) mma22.clear();
         const int gs = ps::kMaxWin;  // one generation of the families serves up to 8 slots
         const auto groups = group_slots(cases, K, gs, [&](int k, int s) {
             if (!dM[4 * k + s]) return false;

@@ -25,14 +25,22 @@
 // and gives the normalisation sum.  Each lane runs at most 68 idle steps at
 // the ramps (lanes start and finish at different tau).
 //
+// The (0 0 0) family vanishes where l1 + l2 + l3 is odd, so its sweeps step two
+// points per time step: lane (w, i) takes forward step nF = tau - i + w - 3
+// (l3 = l2 - l1 + 2 nF) and backward step nB = tau + w + i - 34
+// (l3 = l1 + l2 - 2 nB); every pair is at forward l3 = c0 - r0 - 6 + 2 tau and
+// backward l3 = r0 + c0 + 68 - 2 tau, and a block of 16 time steps covers 32
+// points, half the time steps of the one-point skew.
+//
 // Precision.  x and B are split into three BF16 parts (hi + mid + lo carries
 // 24 bits) and D is formed from six products (all but the three smallest),
 // ordered so that the hi x hi product is added last: the tensor core rounds
 // its FP32 accumulation toward zero, so each 16-step D starts from zero and
 // takes one such rounding at full scale.  Each D is added to float-float
-// totals on the CUDA cores (into the low word; renormalised every fourth block).  B is scaled per 16-step block by a running power
-// of two (block floating point; windows span 1e-45), the same role the slice
-// exponents play in the chosen kernel.  The last forward point, the match of
+// totals on the CUDA cores (into the low word; renormalised every fourth
+// block).  B is scaled per 16-step block by a running power of two (block
+// floating point; windows span 1e-45), the same role the slice exponents play
+// in the chosen kernel.  The last forward point, the match of
 // the two sweeps, the normalisation and the outputs are FP64.
 //
 // Pipeline per 16-step block q: the lanes write x (three planes, two steps per
@@ -40,7 +48,8 @@
 // 12 MMAs of q (6 per sweep) and commits them to an mbarrier; the lanes go on
 // with block q + 1 into the other A buffer, and at its end wait (bounded) for
 // q's MMAs, read D and fold it into the totals.  B tiles are built in shared
-// memory one block ahead.  A wait that gives up sets *p.status.
+// memory one block ahead, from window values fetched (cp.async) a block before
+// that.  A wait that gives up sets *p.status.
 #include "ps_internal.cuh"
 #include "ps_epilogue.cuh"
 #include "ps_ff.cuh"
@@ -48,6 +57,7 @@
 
 #include <cuda_bf16.h>
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 namespace ps {
@@ -109,12 +119,25 @@ __device__ __forceinline__ void split3(float a, float b, uint32_t (&w)[kPlanes])
     w[2] = bf2_bits(l);
 }
 
-// Whether B's element (sweep s, column n, time step tau) is a window value, and its l3.
+// The l3 of time step tau: the (2 -2 0) sweeps move one l3 per step; the (0 0 0) sweeps two,
+// from one non-zero point of the family to the next (forward l3 = l2 - l1 + 2 nF, nF = tau - i
+// + w - 3; backward l3 = l1 + l2 - 2 nB, nB = tau + w + i - 34).
+template <bool F00>
+__device__ __forceinline__ int l3_of(int s, int tau, int r0, int c0)
+{
+    if (F00) return s ? r0 + c0 + 68 - 2 * tau : c0 - r0 - 6 + 2 * tau;
+    return s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+}
+
+// Whether B's element (sweep s, column n, time step tau) is a window value, and its l3.  The
+// (0 0 0) sweeps visit only points where l1 + l2 + l3 is even.
+template <bool F00>
 __device__ __forceinline__ bool b_window(const MmaParams& p, int s, int n, int tau, int r0, int c0, int& l3)
 {
-    l3 = s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+    l3 = l3_of<F00>(s, tau, r0, c0);
     if (l3 < 0 || l3 >= p.wlen || n >= p.nslot) return false;
     const int par = p.parity[n];
+    if (F00) return par != PAR_ODD;
     return par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0);
 }
 
@@ -122,13 +145,14 @@ __device__ __forceinline__ bool b_window(const MmaParams& p, int s, int n, int t
 // Start the copies of block q's window values that this thread's part of build_B needs (4
 // steps of one sweep and column, 8 bytes each) into stage[q & 1]; a block ahead, so their
 // latency is hidden behind a block of steps.
+template <bool F00>
 __device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         int l3;
-        if (b_window(p, s, n, tb + 4 * qd + u, r0, c0, l3))
+        if (b_window<F00>(p, s, n, tb + 4 * qd + u, r0, c0, l3))
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(umma::smem_addr(&sm.stage[q & 1][s][n][4 * qd + u])),
                          "l"(p.bf[n] + l3)
                          : "memory");
@@ -138,6 +162,7 @@ __device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int q, int
 
 // B of block q into buffer q & 1 (all 128 threads: thread = sweep x column x 4 steps), from
 // the values this thread fetched.
+template <bool F00>
 __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
@@ -151,7 +176,7 @@ __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int
         int l3;
         m[u] = 0.0f;
         e[u] = kZeroExp;
-        if (b_window(p, s, n, tau, r0, c0, l3)) {
+        if (b_window<F00>(p, s, n, tau, r0, c0, l3)) {
             const int2 v = sm.stage[q & 1][s][n][4 * qd + u];
             m[u] = __int_as_float(v.x);
             e[u] = v.y;
@@ -273,15 +298,65 @@ __device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, c
     const ffpair g = R.g[p][q.gb], f = R.fb[p][p ? q.fb1 : q.fb0];
     step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), -8.0f);
 }
-// (0 0 0) family at the odd step: f(j+1) = -rho f(j-1), rho = a(j)/a(j+1) (forward) or
-// a(j+1)/a(j) (backward), the same ring entries as the (2 -2 0) step
-__device__ __forceinline__ void fwd_step00(ff& f0, const CoefRing& R, const PairSlots& q)
+
+// ---- the (0 0 0) sweeps --------------------------------------------------------
+// The (0 0 0) family vanishes where l1 + l2 + l3 is odd, so its sweeps step two points at a
+// time: f(j + 2) = -rho f(j) with rho the product of the odd-t entries of the (2 -2 0) step
+// (forward g[t] f[2 l2 + t], backward g[t] fb[2 l2 - t], t = 2n + 1 at step n), whose rho alone
+// is needed.  Each warp keeps them as rings of 64 odd values; a 16-step block reads 47
+// consecutive ones of each table, and the next block needs 16 more.
+struct __align__(16) Ring00 {
+    ff g[kRing], f[kRing], fb[kRing];  // slot (x >> 1) & 63 of odd x
+};
+// sqrt(X / Y) of two exact integer products, 0 where X is
+__device__ __forceinline__ ff rho_entry(ff X, ff Y)
 {
-    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][q.g].rho, R.f[1][q.f].rho), f0));
+    return X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
 }
-__device__ __forceinline__ void bwd_step00(ff& f0, const CoefRing& R, const PairSlots& q)
+// the odd values of block tb (its first time step): t in [tlo, tlo + 92], v in [vlo, vlo + 92],
+// u in [ulo, ulo + 92]
+__device__ __forceinline__ int ring00_tlo(int tb, int w) { return 2 * tb + 2 * w - 67; }
+__device__ __forceinline__ int ring00_vlo(int tb, int w, int c0) { return 2 * c0 + 2 * w + 2 * tb - 5; }
+__device__ __forceinline__ int ring00_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 37 - 2 * tb; }
+// One entry of g (isf false) or f (isf true) at odd x: P(x) = a0 b0, P(x + 1) = (a0 + 1)(b0 -+ 1)
+__device__ __forceinline__ void ring00_gf(Ring00& R, int x, bool isf, int l1)
 {
-    f0 = ff_neg(ff_mul_raw(ff_mul_raw(R.g[1][q.gb].rho, R.fb[1][q.fb1].rho), f0));
+    const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
+    const ff rho = rho_entry(two_prod(a0, b0), two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
+    (isf ? R.f : R.g)[ring_slot(x)] = rho;
+}
+// One entry of fb at odd u: sqrt(Fb(u + 1) / Fb(u)), Fb(u) = u (2 l1 + 1 + u)
+__device__ __forceinline__ void ring00_fb(Ring00& R, int u, int l1)
+{
+    const float a0 = (float)u, b0 = (float)(2 * l1 + 1 + u);
+    R.fb[ring_slot(u)] = rho_entry(two_prod(a0 + 1.0f, b0 + 1.0f), two_prod(a0, b0));
+}
+__device__ __forceinline__ void build_rings00_first(Ring00& R, int tb, int w, int l1, int c0, int lane)
+{
+    const int tlo = ring00_tlo(tb, w), vlo = ring00_vlo(tb, w, c0), ulo = ring00_ulo(tb, w, c0);
+    for (int e = lane; e < 47; e += 32) {
+        ring00_gf(R, tlo + 2 * e, false, l1);
+        ring00_gf(R, vlo + 2 * e, true, l1);
+        ring00_fb(R, ulo + 2 * e, l1);
+    }
+}
+// The 16 values per table that block tb needs beyond the block before: the top 16 of t and v
+// (lanes 0-15 and 16-31, no divergence), then the bottom 16 of u (lanes 0-15).
+__device__ __forceinline__ void build_rings00_next(Ring00& R, int tb, int w, int l1, int c0, int lane)
+{
+    const int e = lane & 15;
+    const bool isf = lane >= 16;
+    ring00_gf(R, (isf ? ring00_vlo(tb, w, c0) : ring00_tlo(tb, w)) + 62 + 2 * e, isf, l1);
+    if (lane < 16) ring00_fb(R, ring00_ulo(tb, w, c0) + 2 * e, l1);
+}
+// forward step n: t = 2n + 1, v = 2 l2 + t; backward step n: t = 2n + 1, u = 2 l2 - t
+__device__ __forceinline__ void fwd_step00c(ff& f, const Ring00& R, int n, int l2)
+{
+    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[n & (kRing - 1)], R.f[(l2 + n) & (kRing - 1)]), f));
+}
+__device__ __forceinline__ void bwd_step00c(ff& f, const Ring00& R, int n, int l2)
+{
+    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[n & (kRing - 1)], R.fb[(l2 - n - 1) & (kRing - 1)]), f));
 }
 
 // sqrt(X / Y) for the last forward points (X, Y up to 2^64: the scaling keeps X Y in range)
@@ -364,6 +439,9 @@ __device__ __forceinline__ void renorm(ff (&t)[NC], int ncols)
         if (n < ncols) t[n] = two_sum(t[n].h, t[n].l);
 }
 
+template <bool F00>
+using RingT = typename std::conditional<F00, Ring00, CoefRing>::type;
+
 // NC: columns folded into the totals (8 or 16; at least nslot + 1)
 template <bool F00, int NC>
 __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
@@ -371,7 +449,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     __shared__ Smem sm;
     extern __shared__ __align__(16) unsigned char dyn[];  // the warps' coefficient rings
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    CoefRing& R = reinterpret_cast<CoefRing*>(dyn)[warp];
+    RingT<F00>& R = reinterpret_cast<RingT<F00>*>(dyn)[warp];
     const int2 tile = p.tiles[blockIdx.x];
     const int r0 = tile.x, c0 = tile.y;
     const int l1 = r0 + 2 * warp, l2 = c0 + 2 * lane;
@@ -380,7 +458,9 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int T = runs ? l1 : 0;
     const int d = l2 - l1;
     // block q covers the time steps q kK .. q kK + 15; the sweeps run for tau in [0, r0 + kRamp)
-    const int nk = (r0 + kRamp + kK - 1) / kK;  // 16-step blocks of the skewed sweeps (block-uniform)
+    // ((2 -2 0)) or [0, floor((r0 + 1) / 2) + 34) ((0 0 0), two points per step)
+    const int ntau = F00 ? ((r0 + 1) >> 1) + 34 : r0 + kRamp;
+    const int nk = (ntau + kK - 1) / kK;  // 16-step blocks of the skewed sweeps (block-uniform)
     const int ncols = p.nslot + 1;
 
     if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
@@ -391,10 +471,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     umma::fence_after_sync();
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
-    fetch_B(p, sm, 0, 0, r0, c0, tid);
-    if (nk > 1) fetch_B(p, sm, 1, kK, r0, c0, tid);
-    build_B(p, sm, 0, 0, r0, c0, tid);
-    build_rings_first(R, 0, warp, l1, c0, lane);
+    fetch_B<F00>(p, sm, 0, 0, r0, c0, tid);
+    if (nk > 1) fetch_B<F00>(p, sm, 1, kK, r0, c0, tid);
+    build_B<F00>(p, sm, 0, 0, r0, c0, tid);
+    if constexpr (F00) build_rings00_first(R, 0, warp, l1, c0, lane);
+    else build_rings_first(R, 0, warp, l1, c0, lane);
     __syncwarp();
 
     // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
@@ -443,14 +524,46 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         }
     };
 
-    const int fofs = -kLead - 2 * lane + 2 * warp;  // tF = tau + fofs
-    const int bofs = 2 * warp + 2 * lane - kRamp;   // tB = tau + bofs
+    // (2 -2 0): forward step tF = tau + fofs, backward tB = tau + bofs (one point each);
+    // (0 0 0): forward step nF = tau + fofs, backward nB = tau + bofs (two points each)
+    const int fofs = F00 ? warp - lane - 3 : -kLead - 2 * lane + 2 * warp;
+    const int bofs = F00 ? warp + lane - 34 : 2 * warp + 2 * lane - kRamp;
+    // (0 0 0): both sweeps take (T + 1) / 2 points; the forward one steps after each (ending at
+    // l2 or l2 + 1), the backward one after all but the last when T is odd (ending there too).
+    // From tau = 34 to floor((r0 + 1) / 2) + 1 every lane that runs is inside both sweeps.
+    const int nx00 = (T + 1) / 2, ns00 = T / 2, steady00 = ((r0 + 1) >> 1) + 1;
     for (int q = 0; q < nk; ++q) {
         const int buf = q & 1;
 #pragma unroll 2
         for (int s2 = 0; s2 < kK; s2 += 2) {
             float xf[2], xb[2];
             const int tau0 = q * kK + s2;
+            if constexpr (F00) {
+                if (tau0 >= 34 && tau0 + 1 <= steady00) {
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        xf[e] = runs ? sq(F.f) : 0.0f;
+                        xb[e] = runs ? sq(B.f) : 0.0f;
+                        fwd_step00c(F.f, R, tau0 + e + fofs, l2);
+                        bwd_step00c(B.f, R, tau0 + e + bofs, l2);
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int nf = tau0 + e + fofs, nb = tau0 + e + bofs;
+                        xf[e] = 0.0f;
+                        xb[e] = 0.0f;
+                        if (nf >= 0 && nf < nx00) {
+                            xf[e] = sq(F.f);
+                            fwd_step00c(F.f, R, nf, l2);
+                        }
+                        if (nb >= 0 && nb < nx00) {
+                            xb[e] = sq(B.f);
+                            if (nb < ns00) bwd_step00c(B.f, R, nb, l2);
+                        }
+                    }
+                }
+            } else {
             const PairSlots ps2 = pair_slots(tau0 + fofs, tau0 + bofs, l2);
             if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
                 // steady state: every lane that runs is inside both sweeps, so both steps run
@@ -458,19 +571,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 // run compute values that are masked out of x and never written
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
-                    if (F00) {
-                        xf[e] = e == 0 && runs ? sq(F.f) : 0.0f;
-                        xb[e] = e == 0 && runs ? sq(B.f) : 0.0f;
-                        if (e == 1) {
-                            fwd_step00(F.f, R, ps2);
-                            bwd_step00(B.f, R, ps2);
-                        }
-                    } else {
-                        xf[e] = runs ? sq(F.f) : 0.0f;
-                        xb[e] = runs ? sq(B.f) : 0.0f;
-                        fwd_step(F, R, e, ps2);
-                        bwd_step(B, R, e, ps2);
-                    }
+                    xf[e] = runs ? sq(F.f) : 0.0f;
+                    xb[e] = runs ? sq(B.f) : 0.0f;
+                    fwd_step(F, R, e, ps2);
+                    bwd_step(B, R, e, ps2);
                 }
             } else {
 #pragma unroll
@@ -480,23 +584,14 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 xf[e] = 0.0f;
                 xb[e] = 0.0f;
                 if (tf >= 0 && tf < T) {
-                    if (F00) {
-                        if (e == 0) xf[e] = sq(F.f);
-                        else fwd_step00(F.f, R, ps2);
-                    } else {
-                        xf[e] = sq(F.f);
-                        fwd_step(F, R, e, ps2);
-                    }
+                    xf[e] = sq(F.f);
+                    fwd_step(F, R, e, ps2);
                 }
                 if (tb >= 0 && tb < T) {
-                    if (F00) {
-                        if (e == 0) xb[e] = sq(B.f);
-                        else bwd_step00(B.f, R, ps2);
-                    } else {
-                        xb[e] = sq(B.f);
-                        bwd_step(B, R, e, ps2);
-                    }
+                    xb[e] = sq(B.f);
+                    bwd_step(B, R, e, ps2);
                 }
+            }
             }
             }
             uint32_t wf[kPlanes], wb[kPlanes];
@@ -512,8 +607,9 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         // ---- block boundary ----
         if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
         if (q + 1 < nk) {
-            build_B(p, sm, q + 1, (q + 1) * kK, r0, c0, tid);
-            build_rings_next(R, (q + 1) * kK, warp, l1, c0, lane);
+            build_B<F00>(p, sm, q + 1, (q + 1) * kK, r0, c0, tid);
+            if constexpr (F00) build_rings00_next(R, (q + 1) * kK, warp, l1, c0, lane);
+            else build_rings_next(R, (q + 1) * kK, warp, l1, c0, lane);
         }
         umma::wait_st();
         umma::fence_smem_async();
@@ -532,7 +628,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             umma::mma_commit(&sm.mbar);
         }
         // stage[q & 1] was last read by build_B(q), before the barrier above
-        if (q + 2 < nk) fetch_B(p, sm, q + 2, (q + 2) * kK, r0, c0, tid);
+        if (q + 2 < nk) fetch_B<F00>(p, sm, q + 2, (q + 2) * kK, r0, c0, tid);
     }
     flush(nk - 1);
     if (!ok) atomicExch(p.status, 1u);
@@ -556,18 +652,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         double gm0, lam;
         double x = 0.0;
         if (F00) {
-            // the 00 family is non-zero at points of the parity of jmin: jm when T is even, jm + 1
-            // otherwise; both sweeps end there and are matched at that one point
+            // both sweeps end at jm when T is even (a point neither summed) and at jm + 1
+            // otherwise (summed by the backward sweep; jm is a zero of the family) and are
+            // matched there
             gm0 = ff_to_double(F.f);
-            if (evenT) {
-                x = gm0 * gm0;
-            } else {
-                const ff X = ff_mul_raw(two_prod((float)T, (float)(2 * d + T)),
-                                        two_prod((float)(2 * l1 + 1 - T), (float)(2 * l2 + T + 1)));
-                const ff Y = ff_mul_raw(two_prod((float)(T + 1), (float)(2 * d + T + 1)),
-                                        two_prod((float)(2 * l1 - T), (float)(2 * l2 + T + 2)));
-                gm0 = ff_to_double(ff_neg(ff_mul(rho00(X, Y), F.f)));
-            }
+            if (evenT) x = gm0 * gm0;
             lam = gm0 / ff_to_double(B.f);
         } else {
             gm0 = ff_to_double(F.f);

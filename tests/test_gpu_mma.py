@@ -1,6 +1,7 @@
-"""The tensor-core coupling kernels (k_coupling_mma): the TT slots and the ++ /
--- slots of a chosen-mode set, each kind with more than 8 slots; one (0 0 0) or
-(2 -2 0) family generation for up to 15 windows, the window contraction as BF16
+"""The tensor-core coupling kernels (k_coupling_mma): the TT slots of a
+chosen-mode set when there are 5 or more, and its ++ / -- slots when there are
+more than 8; one (0 0 0) or (2 -2 0) family generation for up to 15 windows
+(the (0 0 0) sweeps two points per time step), the window contraction as BF16
 tcgen05 MMAs (three-part split, fresh FP32 accumulator per 16 steps,
 float-float totals).
 
@@ -120,9 +121,8 @@ def test_mma_matches_plain_fp64_full_size(ctx):
 
 def test_mma_agrees_with_cuda_core_path(ctx):
     """The same set with the tensor-core kernels switched off: both within 2e-6 of each other,
-    and the routing itself: the 10 ++/-- slots (more than 8) take the tensor-core kernel, so their
-    results differ from the CUDA-core kernel's in the last bits (the 5 TT slots take CUDA-core
-    kernels either way)."""
+    and the routing itself: the 10 ++/-- slots (more than 8) and the 5 TT slots take the
+    tensor-core kernels, so their results differ from the CUDA-core kernels' in the last bits."""
     L = 700
     Ws = [_W(2 * L + 1, seed=80 + k, fsky=0.5 + 0.05 * k) for k in range(5)]
     slots = [(k, s) for k in range(5) for s in (0, 2, 3)]
@@ -130,8 +130,22 @@ def test_mma_agrees_with_cuda_core_path(ctx):
     b = _run_set(ctx, Ws, slots, 2, L, tensor_cores=False)
     for sl in slots:
         assert max_err_scaled(a[sl], b[sl], np.abs(b[sl])) < 2 * TOL, sl
-        if sl[1] != 0:
-            assert not np.array_equal(a[sl], b[sl]), sl
+        assert not np.array_equal(a[sl], b[sl]), sl
+
+
+@pytest.mark.parametrize("K,routed", [(4, False), (5, True)])
+def test_mma_tt_routing_threshold(ctx, K, routed):
+    """TT sets: 4 slots stay on the CUDA cores (the same bits with the tensor cores switched off),
+    5 take the tensor-core kernel (odd lmin and lmax, lmin > 0)."""
+    L = 333
+    Ws = [_W(2 * L + 1, seed=120 + k, fsky=0.45 + 0.05 * k) for k in range(K)]
+    slots = [(k, 0) for k in range(K)]
+    a = _run_set(ctx, Ws, slots, 5, L)
+    b = _run_set(ctx, Ws, slots, 5, L, tensor_cores=False)
+    for (k, s) in slots:
+        R = o.inner_mcm(s, Ws[k], 5, L)
+        assert max_err_scaled(a[k, s], R, cond_scale(s, Ws[k], 5, L)) < TOL, (k, s)
+        assert np.array_equal(a[k, s], b[k, s]) != routed, (k, s)
 
 
 def test_mma_lmax_8191_sampled_rows(ctx):
