@@ -232,14 +232,35 @@ struct Sweep22 {
 // i is t of the forward sweep of lane 31 - i).  A 16-step block reads 78
 // consecutive values of each table (39 per parity); the next block needs 16 new
 // ones per table, built at the block boundary.
+//
+// A block's 8 step pairs read 8 consecutive slots of each table (increasing for g
+// and f, decreasing for fb) from a start computed once per block.  So each table
+// keeps kGuard slots a second time past its end (g, f: slot s < kGuard also at
+// kRing + s) or before its start (fb: slot s at kGuard + s, and slot s >= kRing -
+// kGuard also at s - (kRing - kGuard)), and a run of kGuard slots from any start is
+// contiguous: no wrap-around arithmetic per step.
 constexpr int kRing = 64;
+constexpr int kGuard = 8;
 struct ffpair {
     ff rho, r;
 };
 struct __align__(16) CoefRing {
-    ffpair g[2][kRing], f[2][kRing], fb[2][kRing];
+    ffpair g[2][kRing + kGuard], f[2][kRing + kGuard], fb[2][kGuard + kRing];
 };
 __device__ __forceinline__ int ring_slot(int x) { return (x >> 1) & (kRing - 1); }
+// store slot s of a table read upwards / downwards in runs of G slots
+template <int G, typename T>
+__device__ __forceinline__ void put_up(T* t, int s, const T& v)
+{
+    t[s] = v;
+    if (s < G) t[kRing + s] = v;
+}
+template <int G, typename T>
+__device__ __forceinline__ void put_down(T* t, int s, const T& v)
+{
+    t[G + s] = v;
+    if (s >= kRing - G) t[s - (kRing - G)] = v;
+}
 
 // (sqrt(X / Y), 1 / sqrt(Y)) of two exact integer products; rho is 0 where X is
 __device__ __forceinline__ ffpair ratio_entry(ff X, ff Y)
@@ -250,18 +271,20 @@ __device__ __forceinline__ ffpair ratio_entry(ff X, ff Y)
 }
 __device__ __forceinline__ void ring_g(CoefRing& R, int t, int l1)
 {
-    R.g[t & 1][ring_slot(t)] = ratio_entry(two_prod((float)t, (float)(2 * l1 + 1 - t)),
-                                           two_prod((float)(t + 1), (float)(2 * l1 - t)));
+    put_up<kGuard>(R.g[t & 1], ring_slot(t),
+                   ratio_entry(two_prod((float)t, (float)(2 * l1 + 1 - t)), two_prod((float)(t + 1), (float)(2 * l1 - t))));
 }
 __device__ __forceinline__ void ring_f(CoefRing& R, int v, int l1)
 {
-    R.f[v & 1][ring_slot(v)] = ratio_entry(two_prod((float)(v - 2 * l1), (float)(v + 1)),
-                                           two_prod((float)(v + 1 - 2 * l1), (float)(v + 2)));
+    put_up<kGuard>(R.f[v & 1], ring_slot(v),
+                   ratio_entry(two_prod((float)(v - 2 * l1), (float)(v + 1)),
+                               two_prod((float)(v + 1 - 2 * l1), (float)(v + 2))));
 }
 __device__ __forceinline__ void ring_fb(CoefRing& R, int u, int l1)
 {
-    R.fb[u & 1][ring_slot(u)] = ratio_entry(two_prod((float)(u + 1), (float)(2 * l1 + 2 + u)),
-                                            two_prod((float)u, (float)(2 * l1 + 1 + u)));
+    put_down<kGuard>(R.fb[u & 1], ring_slot(u),
+                     ratio_entry(two_prod((float)(u + 1), (float)(2 * l1 + 2 + u)),
+                                 two_prod((float)u, (float)(2 * l1 + 1 + u))));
 }
 
 // one step of the (2 -2 0) family: f(next) = -(w f r + rho f(prev))
@@ -273,29 +296,29 @@ __device__ __forceinline__ void step22(Sweep22& S, ff rho, ff r, float dw)
     S.f = ff_neg(ff_add_raw(x, y));
     S.w += dw;
 }
-// Ring slots of one pair of steps (tau even, then odd) of a lane: t, v = 2 l2 + t of the
-// forward step and t of the backward step are even at the even step, so both steps use the
+// Table indices of a lane's first step pair in a block (tau even, then odd): t, v = 2 l2 + t of
+// the forward step and t of the backward step are even at the even step, so both steps use the
 // same slot of each; u = 2 l2 - t of the backward step is even at the even step and one less at
-// the odd one.
-struct PairSlots {
+// the odd one.  Pair k of the block reads g and f at + k and fb at - k.
+struct RingIdx {
     int g, f, gb, fb0, fb1;
 };
-__device__ __forceinline__ PairSlots pair_slots(int tf_even, int tb_even, int l2)
+__device__ __forceinline__ RingIdx ring_idx(int tf_even, int tb_even, int l2)
 {
     const int u0 = 2 * l2 - tb_even;
-    return PairSlots{ring_slot(tf_even), ring_slot(2 * l2 + tf_even), ring_slot(tb_even), ring_slot(u0),
-                     ring_slot(u0 - 1)};
+    return RingIdx{ring_slot(tf_even), ring_slot(2 * l2 + tf_even), ring_slot(tb_even), kGuard + ring_slot(u0),
+                   kGuard + ring_slot(u0 - 1)};
 }
-// forward step of parity p: g[t] and f[2 l2 + t]
-__device__ __forceinline__ void fwd_step(Sweep22& S, const CoefRing& R, int p, const PairSlots& q)
+// forward step of parity p in pair k: g[t] and f[2 l2 + t]
+__device__ __forceinline__ void fwd_step(Sweep22& S, const CoefRing& R, int p, const RingIdx& q, int k)
 {
-    const ffpair g = R.g[p][q.g], f = R.f[p][q.f];
+    const ffpair g = R.g[p][q.g + k], f = R.f[p][q.f + k];
     step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), 8.0f);
 }
-// backward step of parity p: g[t] and fb[2 l2 - t]
-__device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, const PairSlots& q)
+// backward step of parity p in pair k: g[t] and fb[2 l2 - t]
+__device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, const RingIdx& q, int k)
 {
-    const ffpair g = R.g[p][q.gb], f = R.fb[p][p ? q.fb1 : q.fb0];
+    const ffpair g = R.g[p][q.gb + k], f = R.fb[p][(p ? q.fb1 : q.fb0) - k];
     step22(S, ff_mul_raw(g.rho, f.rho), ff_mul_raw(g.r, f.r), -8.0f);
 }
 
@@ -305,8 +328,9 @@ __device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, c
 // (forward g[t] f[2 l2 + t], backward g[t] fb[2 l2 - t], t = 2n + 1 at step n), whose rho alone
 // is needed.  Each warp keeps them as rings of 64 odd values; a 16-step block reads 47
 // consecutive ones of each table, and the next block needs 16 more.
+constexpr int kGuard00 = 16;  // a block's 16 steps read 16 consecutive slots of each table
 struct __align__(16) Ring00 {
-    ff g[kRing], f[kRing], fb[kRing];  // slot (x >> 1) & 63 of odd x
+    ff g[kRing + kGuard00], f[kRing + kGuard00], fb[kGuard00 + kRing];  // slot (x >> 1) & 63 of odd x
 };
 // sqrt(X / Y) of two exact integer products, 0 where X is
 __device__ __forceinline__ ff rho_entry(ff X, ff Y)
@@ -323,13 +347,13 @@ __device__ __forceinline__ void ring00_gf(Ring00& R, int x, bool isf, int l1)
 {
     const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
     const ff rho = rho_entry(two_prod(a0, b0), two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
-    (isf ? R.f : R.g)[ring_slot(x)] = rho;
+    put_up<kGuard00>(isf ? R.f : R.g, ring_slot(x), rho);
 }
 // One entry of fb at odd u: sqrt(Fb(u + 1) / Fb(u)), Fb(u) = u (2 l1 + 1 + u)
 __device__ __forceinline__ void ring00_fb(Ring00& R, int u, int l1)
 {
     const float a0 = (float)u, b0 = (float)(2 * l1 + 1 + u);
-    R.fb[ring_slot(u)] = rho_entry(two_prod(a0 + 1.0f, b0 + 1.0f), two_prod(a0, b0));
+    put_down<kGuard00>(R.fb, ring_slot(u), rho_entry(two_prod(a0 + 1.0f, b0 + 1.0f), two_prod(a0, b0)));
 }
 __device__ __forceinline__ void build_rings00_first(Ring00& R, int tb, int w, int l1, int c0, int lane)
 {
@@ -349,14 +373,24 @@ __device__ __forceinline__ void build_rings00_next(Ring00& R, int tb, int w, int
     ring00_gf(R, (isf ? ring00_vlo(tb, w, c0) : ring00_tlo(tb, w)) + 62 + 2 * e, isf, l1);
     if (lane < 16) ring00_fb(R, ring00_ulo(tb, w, c0) + 2 * e, l1);
 }
-// forward step n: t = 2n + 1, v = 2 l2 + t; backward step n: t = 2n + 1, u = 2 l2 - t
-__device__ __forceinline__ void fwd_step00c(ff& f, const Ring00& R, int n, int l2)
+// Table indices of a lane's first step in a block: forward step n reads g at t = 2n + 1 (slot
+// n) and f at v = 2 l2 + t (slot l2 + n); backward step n reads g at t (slot n) and fb at
+// u = 2 l2 - t (slot l2 - n - 1).  Step j of the block reads g and f at + j and fb at - j.
+struct RingIdx00 {
+    int g, f, gb, fb;
+};
+__device__ __forceinline__ RingIdx00 ring00_idx(int nf, int nb, int l2)
 {
-    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[n & (kRing - 1)], R.f[(l2 + n) & (kRing - 1)]), f));
+    return RingIdx00{nf & (kRing - 1), (l2 + nf) & (kRing - 1), nb & (kRing - 1),
+                     kGuard00 + ((l2 - nb - 1) & (kRing - 1))};
 }
-__device__ __forceinline__ void bwd_step00c(ff& f, const Ring00& R, int n, int l2)
+__device__ __forceinline__ void fwd_step00c(ff& f, const Ring00& R, const RingIdx00& q, int j)
 {
-    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[n & (kRing - 1)], R.fb[(l2 - n - 1) & (kRing - 1)]), f));
+    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[q.g + j], R.f[q.f + j]), f));
+}
+__device__ __forceinline__ void bwd_step00c(ff& f, const Ring00& R, const RingIdx00& q, int j)
+{
+    f = ff_neg(ff_mul_raw(ff_mul_raw(R.g[q.gb + j], R.fb[q.fb - j]), f));
 }
 
 // sqrt(X / Y) for the last forward points (X, Y up to 2^64: the scaling keeps X Y in range)
@@ -403,21 +437,21 @@ __device__ __forceinline__ void build_rings_next(CoefRing& R, int tb, int w, int
         const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
         const ff s1 = ff_rsqrt(two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
         ff s0{__shfl_up_sync(0xffffffffu, s1.h, 1, 16), __shfl_up_sync(0xffffffffu, s1.l, 1, 16)};
-        ffpair(*tab)[kRing] = isf ? R.f : R.g;
+        ffpair(*tab)[kRing + kGuard] = isf ? R.f : R.g;
         if (e == 0) s0 = tab[(x - 1) & 1][ring_slot(x - 1)].r;
         const ff P0 = two_prod(a0, b0);
         const ff rho = P0.h > 0.0f ? ff_mul(ff_mul_raw(P0, s0), s1) : ff_make(0.0f);
-        tab[x & 1][ring_slot(x)] = ffpair{rho, s1};
+        put_up<kGuard>(tab[x & 1], ring_slot(x), ffpair{rho, s1});
     }
     if (lane < 16) {
         const int x = ring_ulo(tb, w, c0) + e;  // Fb(x) = x (2 l1 + 1 + x)
         const float a0 = (float)x, b0 = (float)(2 * l1 + 1 + x);
         const ff s0 = ff_rsqrt(two_prod(a0, b0));
         ff s1{__shfl_down_sync(0x0000ffffu, s0.h, 1, 16), __shfl_down_sync(0x0000ffffu, s0.l, 1, 16)};
-        if (e == 15) s1 = R.fb[(x + 1) & 1][ring_slot(x + 1)].r;
+        if (e == 15) s1 = R.fb[(x + 1) & 1][kGuard + ring_slot(x + 1)].r;
         const ff P1 = two_prod(a0 + 1.0f, b0 + 1.0f);
         const ff rho = P1.h > 0.0f ? ff_mul(ff_mul_raw(P1, s1), s0) : ff_make(0.0f);
-        R.fb[x & 1][ring_slot(x)] = ffpair{rho, s0};
+        put_down<kGuard>(R.fb[x & 1], ring_slot(x), ffpair{rho, s0});
     }
 }
 
@@ -534,18 +568,27 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int nx00 = (T + 1) / 2, ns00 = T / 2, steady00 = ((r0 + 1) >> 1) + 1;
     for (int q = 0; q < nk; ++q) {
         const int buf = q & 1;
+        // the ring indices of the block's first time step (first step pair)
+        RingIdx00 ix00;
+        RingIdx ix22;
+        if constexpr (F00) ix00 = ring00_idx(q * kK + fofs, q * kK + bofs, l2);
+        else ix22 = ring_idx(q * kK + fofs, q * kK + bofs, l2);
 #pragma unroll 2
         for (int s2 = 0; s2 < kK; s2 += 2) {
             float xf[2], xb[2];
             const int tau0 = q * kK + s2;
+            // steady state: every lane that runs is inside both sweeps, so both steps run
+            // unconditionally (their dependency chains interleave).  Lanes that do not run
+            // compute values that may not be finite: they reach only their own rows of the
+            // MMAs (row m of D is row m of A times B) and their own totals, never written.
             if constexpr (F00) {
                 if (tau0 >= 34 && tau0 + 1 <= steady00) {
 #pragma unroll
                     for (int e = 0; e < 2; ++e) {
-                        xf[e] = runs ? sq(F.f) : 0.0f;
-                        xb[e] = runs ? sq(B.f) : 0.0f;
-                        fwd_step00c(F.f, R, tau0 + e + fofs, l2);
-                        bwd_step00c(B.f, R, tau0 + e + bofs, l2);
+                        xf[e] = sq(F.f);
+                        xb[e] = sq(B.f);
+                        fwd_step00c(F.f, R, ix00, s2 + e);
+                        bwd_step00c(B.f, R, ix00, s2 + e);
                     }
                 } else {
 #pragma unroll
@@ -555,44 +598,40 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                         xb[e] = 0.0f;
                         if (nf >= 0 && nf < nx00) {
                             xf[e] = sq(F.f);
-                            fwd_step00c(F.f, R, nf, l2);
+                            fwd_step00c(F.f, R, ix00, s2 + e);
                         }
                         if (nb >= 0 && nb < nx00) {
                             xb[e] = sq(B.f);
-                            if (nb < ns00) bwd_step00c(B.f, R, nb, l2);
+                            if (nb < ns00) bwd_step00c(B.f, R, ix00, s2 + e);
                         }
                     }
                 }
             } else {
-            const PairSlots ps2 = pair_slots(tau0 + fofs, tau0 + bofs, l2);
-            if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
-                // steady state: every lane that runs is inside both sweeps, so both steps run
-                // unconditionally (their two dependency chains interleave); lanes that do not
-                // run compute values that are masked out of x and never written
+                const int k = s2 >> 1;  // the step pair of the block
+                if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
 #pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    xf[e] = runs ? sq(F.f) : 0.0f;
-                    xb[e] = runs ? sq(B.f) : 0.0f;
-                    fwd_step(F, R, e, ps2);
-                    bwd_step(B, R, e, ps2);
-                }
-            } else {
+                    for (int e = 0; e < 2; ++e) {
+                        xf[e] = sq(F.f);
+                        xb[e] = sq(B.f);
+                        fwd_step(F, R, e, ix22, k);
+                        bwd_step(B, R, e, ix22, k);
+                    }
+                } else {
 #pragma unroll
-            for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
-                const int tau = q * kK + s2 + e;
-                const int tf = tau + fofs, tb = tau + bofs;
-                xf[e] = 0.0f;
-                xb[e] = 0.0f;
-                if (tf >= 0 && tf < T) {
-                    xf[e] = sq(F.f);
-                    fwd_step(F, R, e, ps2);
+                    for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
+                        const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
+                        xf[e] = 0.0f;
+                        xb[e] = 0.0f;
+                        if (tf >= 0 && tf < T) {
+                            xf[e] = sq(F.f);
+                            fwd_step(F, R, e, ix22, k);
+                        }
+                        if (tb >= 0 && tb < T) {
+                            xb[e] = sq(B.f);
+                            bwd_step(B, R, e, ix22, k);
+                        }
+                    }
                 }
-                if (tb >= 0 && tb < T) {
-                    xb[e] = sq(B.f);
-                    bwd_step(B, R, e, ps2);
-                }
-            }
-            }
             }
             uint32_t wf[kPlanes], wb[kPlanes];
             split3(xf[0], xf[1], wf);
