@@ -227,8 +227,11 @@ typedef struct ps_problem {
  * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
  * ps_batch_autotune() found, else defaults.  blocks_per_sm = -1 selects the
  * launch form instead: one chosen-kernel launch per window group.
- * run() enqueues the window preparation, then the queue reset and ONE
- * persistent kernel (or the per-group launches).  graph_launch() captures run()
+ * A problem's TT slots when there are 5 or more, and its ++/-- slots when
+ * there are more than 8, go to tensor-core launches instead, as in
+ * ps_mcm_set_device (unless ps_set_tensor_cores(ctx, 0)).
+ * run() enqueues the window preparation, the tensor-core launches, then the
+ * queue reset and ONE persistent kernel (or the per-group launches).  graph_launch() captures run()
  * into a CUDA graph on first use and replays it afterwards.  The problems'
  * pointers must stay valid while the batch is in use. */
 int ps_batch_prepare(ps_ctx *ctx, const ps_problem *probs, int nprob, int group_slots, int blocks_per_sm);

@@ -77,6 +77,12 @@ struct ps_ctx {
         bool launches = false;
         std::vector<ps::CouplingParams> host_groups;
         int2* d_tasks = nullptr;
+        // tensor-core launches (the problems' TT slots when there are kMmaMin00 or more, their
+        // ++/-- slots when there are kMmaMin22 or more), enqueued before the CUDA-core part,
+        // with the block lists of every distinct (lmin, lmax) in d_mtiles
+        std::vector<ps::MmaParams> host_mma;
+        std::vector<char> host_mma00;
+        int2* d_mtiles = nullptr;
     } batch;
     int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
     // tensor-core kernels: their block list for the current (lmin, lmax) and the status of their bounded waits
@@ -226,6 +232,27 @@ static int ensure_mtiles(ps_ctx* c, int lmin, int lmax)
     c->nmtiles = (int)t.size();
     c->mtile_lmin = lmin;
     c->mtile_lmax = lmax;
+    return PS_OK;
+}
+
+// The status word of the tensor-core kernels' bounded waits, cleared on the stream unless a
+// launch whose status is unchecked is pending.
+static int alloc_status(ps_ctx* c)
+{
+    if (c->d_status) return PS_OK;
+    cudaError_t e = cudaMalloc((void**)&c->d_status, sizeof(unsigned));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c->d_status = nullptr;
+        return set_err(c, PS_ERR_OOM, "cudaMalloc of the status word failed: %s", cudaGetErrorString(e));
+    }
+    return PS_OK;
+}
+static int arm_status(ps_ctx* c, cudaStream_t s)
+{
+    if (int st = alloc_status(c)) return st;
+    if (!c->status_pending) PS_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(unsigned), s));
+    c->status_pending = true;
     return PS_OK;
 }
 
@@ -382,6 +409,7 @@ static void batch_release(ps_ctx* c)
     cudaFree(b.d_win);
     cudaFree(b.d_bf);
     cudaFree(b.d_tasks);
+    cudaFree(b.d_mtiles);
     b = ps_ctx::Batch();
 }
 
@@ -857,16 +885,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
         PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
         if (!mma00.empty() || !mma22.empty()) {
             if ((st = ensure_mtiles(c, lmin, lmax))) return st;
-            if (!c->d_status) {
-                cudaError_t e = cudaMalloc((void**)&c->d_status, sizeof(unsigned));
-                if (e != cudaSuccess) {
-                    cudaGetLastError();
-                    c->d_status = nullptr;
-                    return set_err(c, PS_ERR_OOM, "cudaMalloc of the status word failed: %s", cudaGetErrorString(e));
-                }
-            }
-            if (!c->status_pending) PS_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(unsigned), c->stream));
-            c->status_pending = true;
+            if ((st = arm_status(c, c->stream))) return st;
         }
         for (const std::vector<Slot>* list : {&mma00, &mma22}) {
             for (size_t i0 = 0; i0 < list->size(); i0 += ps::kMmaMaxSlots) {
@@ -988,6 +1007,9 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     std::vector<ps::CouplingParams> groups;
     std::vector<int4> items;
     std::vector<float> cost;
+    std::vector<int2> mtiles, one_mt;
+    std::vector<std::pair<long long, int2>> mtile_of;  // (lmin, lmax) key -> (offset in mtiles, count)
+    std::vector<size_t> mma_tile_off;                   // per tensor-core launch
     for (int i = 0; i < nprob; ++i) {
         const ps_problem& P = probs[i];
         int wlen = 2 * P.lmax + 2;
@@ -1004,7 +1026,56 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
             descs[k].wW = w.wW;
             descs[k].bf = w.bf;
         }
-        for (const auto& grp : batch_group_slots(P.cases, P.K, gs)) {
+        // the problem's TT slots and its ++/-- slots, each kind on its own, go to the
+        // tensor-core kernels when there are enough of them (as in ps_mcm_set_device)
+        unsigned cases_cc = P.cases;
+        std::vector<Slot> m00, m22;
+        if (c->tensor_cores) {
+            for (int k = 0; k < P.K; ++k)
+                for (int s = 0; s < 4; ++s)
+                    if ((P.cases & (1u << s)) && s != PS_SPIN_02) (s == PS_SPIN_00 ? m00 : m22).push_back(Slot{k, s});
+            if ((int)m00.size() >= kMmaMin00) cases_cc &= ~(1u << PS_SPIN_00);
+            else m00.clear();
+            if ((int)m22.size() >= kMmaMin22) cases_cc &= ~((1u << PS_SPIN_PP) | (1u << PS_SPIN_MM));
+            else m22.clear();
+        }
+        if (!m00.empty() || !m22.empty()) {
+            const long long key = ((long long)P.lmin << 32) | (unsigned)P.lmax;
+            int2 oc = make_int2(-1, 0);
+            for (const auto& t : mtile_of)
+                if (t.first == key) oc = t.second;
+            if (oc.x < 0) {
+                ps::mma_tile_list(P.lmin, P.lmax, one_mt);
+                oc = make_int2((int)mtiles.size(), (int)one_mt.size());
+                mtiles.insert(mtiles.end(), one_mt.begin(), one_mt.end());
+                mtile_of.push_back({key, oc});
+            }
+            for (const std::vector<Slot>* list : {&m00, &m22}) {
+                for (size_t i0 = 0; i0 < list->size(); i0 += ps::kMmaMaxSlots) {
+                    ps::MmaParams mp;
+                    memset(&mp, 0, sizeof(mp));
+                    mp.lmin = P.lmin;
+                    mp.lmax = P.lmax;
+                    mp.nslot = (int)std::min(list->size() - i0, (size_t)ps::kMmaMaxSlots);
+                    for (int q = 0; q < mp.nslot; ++q) {
+                        const Slot sl = (*list)[i0 + q];
+                        mp.bf[q] = descs[sl.k].bf;
+                        mp.wW[q] = descs[sl.k].wW;
+                        mp.parity[q] = sl.s == PS_SPIN_00 ? ps::PAR_ALL : (sl.s == PS_SPIN_PP ? ps::PAR_EVEN : ps::PAR_ODD);
+                        mp.out[q] = P.M[4 * sl.k + sl.s];
+                    }
+                    mp.ldo = P.ldm;
+                    mp.wlen = wlen;
+                    mp.epilogue = ps::EPI_MCM;
+                    mp.ntiles = oc.y;
+                    b.host_mma.push_back(mp);
+                    b.host_mma00.push_back(list == &m00);
+                    mma_tile_off.push_back((size_t)oc.x);
+                }
+            }
+        }
+        if (!cases_cc) continue;
+        for (const auto& grp : batch_group_slots(cases_cc, P.K, gs)) {
             ps::CouplingParams g;
             memset(&g, 0, sizeof(g));
             g.lmin = P.lmin;
@@ -1064,9 +1135,18 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
         task_of.push_back({key, {off, (int)(tasks.size() - off)}});
     }
     if ((st = dev_upload(c, &b.d_groups, groups)) || (st = dev_upload(c, &b.d_items, sorted)) ||
-        (st = dev_upload(c, &b.d_preps, preps)) || (st = dev_upload(c, &b.d_tasks, tasks))) {
+        (st = dev_upload(c, &b.d_preps, preps)) || (st = dev_upload(c, &b.d_tasks, tasks)) ||
+        (st = dev_upload(c, &b.d_mtiles, mtiles))) {
         batch_release(c);
         return st;
+    }
+    if (!b.host_mma.empty() && (st = alloc_status(c))) {
+        batch_release(c);
+        return st;
+    }
+    for (size_t m = 0; m < b.host_mma.size(); ++m) {
+        b.host_mma[m].tiles = b.d_mtiles + mma_tile_off[m];
+        b.host_mma[m].status = c->d_status;
     }
     b.host_groups = groups;
     for (auto& g : b.host_groups) {
@@ -1093,26 +1173,34 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
     return PS_OK;
 }
 
+// The batch's kernels on stream s: window preparation, the tensor-core launches, then the
+// CUDA-core part (the persistent kernel, or one launch per group).  The status word of the
+// tensor-core launches is cleared by the caller, outside any graph.
 static int batch_enqueue(ps_ctx* c, cudaStream_t s)
 {
     ps_ctx::Batch& b = c->batch;
     PS_CUDA(c, ps::launch_prep_windows(b.d_preps, b.npreps, b.max_wlen, s));
-    if (b.launches) {  // one chosen-kernel launch per window group, all on the stream
-        PS_CUDA(c, cudaEventRecord(c->ev0, s));
-        for (const auto& g : b.host_groups) PS_CUDA(c, ps::launch_chosen(g, s));
-        PS_CUDA(c, cudaEventRecord(c->ev1, s));
-        return PS_OK;
-    }
-    PS_CUDA(c, cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s));
-    ps::BatchParams bp;
-    bp.groups = b.d_groups;
-    bp.items = b.d_items;
-    bp.nitems = b.nitems;
-    bp.counter = b.d_counter;
+    if (!b.launches && b.nitems > 0) PS_CUDA(c, cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), s));
     PS_CUDA(c, cudaEventRecord(c->ev0, s));
-    PS_CUDA(c, ps::launch_batch_chosen(bp, b.blocks, b.group_slots, s));
+    for (size_t m = 0; m < b.host_mma.size(); ++m) PS_CUDA(c, ps::launch_mma(b.host_mma[m], b.host_mma00[m] != 0, s));
+    if (b.launches) {  // one chosen-kernel launch per window group, all on the stream
+        for (const auto& g : b.host_groups) PS_CUDA(c, ps::launch_chosen(g, s));
+    } else if (b.nitems > 0) {
+        ps::BatchParams bp;
+        bp.groups = b.d_groups;
+        bp.items = b.d_items;
+        bp.nitems = b.nitems;
+        bp.counter = b.d_counter;
+        PS_CUDA(c, ps::launch_batch_chosen(bp, b.blocks, b.group_slots, s));
+    }
     PS_CUDA(c, cudaEventRecord(c->ev1, s));
     return PS_OK;
+}
+
+// kernels one run of the batch launches (window preparation included)
+static size_t batch_kernel_count(const ps_ctx::Batch& b)
+{
+    return 1 + b.host_mma.size() + (b.launches ? b.host_groups.size() : (b.nitems > 0 ? 1 : 0));
 }
 
 int ps_batch_run(ps_ctx* c)
@@ -1120,9 +1208,10 @@ int ps_batch_run(ps_ctx* c)
     if (!c) return PS_ERR_ARG;
     if (!c->batch.ready) return set_err(c, PS_ERR_ARG, "ps_batch_prepare has not been called");
     PS_CUDA(c, cudaSetDevice(c->device));
-    int st = batch_enqueue(c, c->stream);
-    if (st) return st;
-    c->launches += c->batch.launches ? 1 + c->batch.host_groups.size() : 2;
+    int st;
+    if (!c->batch.host_mma.empty() && (st = arm_status(c, c->stream))) return st;
+    if ((st = batch_enqueue(c, c->stream))) return st;
+    c->launches += batch_kernel_count(c->batch);
     c->timed = true;
     return PS_OK;
 }
@@ -1152,8 +1241,12 @@ int ps_batch_graph_launch(ps_ctx* c)
             return set_err(c, PS_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
         }
     }
+    if (!b.host_mma.empty()) {
+        int st = arm_status(c, c->stream);
+        if (st) return st;
+    }
     PS_CUDA(c, cudaGraphLaunch(b.exec, c->stream));
-    c->launches += b.launches ? 1 + b.host_groups.size() : 2;
+    c->launches += batch_kernel_count(b);
     c->timed = true;
     return PS_OK;
 }

@@ -150,6 +150,65 @@ def test_mcm_set_host(ctx, cases):
         assert max_err_scaled(m, ref, cond_scale(s, Ws[k], lmin, L)) < 1e-6, (k, s)
 
 
+def _routed_problems():
+    """Problems whose TT slots (5 or more) or ++/-- slots (more than 8) take the tensor-core
+    kernels, next to ones that stay on the CUDA cores."""
+    specs = [(97, 0, 0x1, 6), (130, 3, 0xC, 5), (64, 0, 0xF, 5), (77, 2, 0x1, 4), (50, 0, 0x3, 5)]
+    probs, refs = [], []
+    for i, (L, lmin, cases, K) in enumerate(specs):
+        n = L - lmin + 1
+        Ws = [_W(2 * L + 1, seed=700 + 10 * i + k) for k in range(K)]
+        dW = [_dev(w) for w in Ws]
+        dM = [torch.full((n, n), float("nan"), dtype=torch.float64, device="cuda") if cases & (1 << s) else None
+              for k in range(K) for s in range(4)]
+        probs.append({"lmin": lmin, "lmax": L, "cases": cases, "nW": 2 * L + 1, "ldm": n,
+                      "W": [d.data_ptr() for d in dW], "M": [m.data_ptr() if m is not None else 0 for m in dM],
+                      "_keep": (dW, dM)})
+        refs.append((Ws, lmin, L, cases, dM))
+    return probs, refs
+
+
+@pytest.mark.parametrize("bps,graph", [(0, False), (-1, False), (0, True), (-1, True)])
+def test_batch_tensor_core_routing(ctx, bps, graph):
+    """The batch routes each problem's TT slots (5 or more) and ++/-- slots (more than 8) to the
+    tensor-core kernels, like ps_mcm_set_device: every output against the oracle (NaN sentinels),
+    in the persistent and the launch form, directly and from a CUDA graph; with the tensor cores
+    switched off the routed slots change in their last bits, and problem 3 (4 TT slots, grouped
+    the same either way) not at all.  The TE slots of problems 2 and 4 stay on the CUDA cores but
+    in other groups (a TE-only body instead of a mixed one), so only their tolerance is checked."""
+    probs, refs = _routed_problems()
+    routed = {(0, 0), (1, 2), (1, 3), (2, 0), (2, 2), (2, 3), (4, 0)}  # (problem, spin case)
+    same_groups = {(3, 0)}
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        outs = {}
+        for tc in (True, False):
+            ctx.set_tensor_cores(tc)
+            for _, _, _, _, dM in refs:
+                for m in dM:
+                    if m is not None:
+                        m.fill_(float("nan"))
+            ctx.batch_prepare(probs, group_slots=4, blocks_per_sm=bps)
+            for _ in range(2 if graph else 1):
+                ctx.batch_graph_launch() if graph else ctx.batch_run()
+            torch.cuda.synchronize()
+            ctx.synchronize()  # reports a tensor-core wait that gave up
+            _check(refs)
+            outs[tc] = [[m.cpu().numpy() if m is not None else None for m in dM] for _, _, _, _, dM in refs]
+        for i, (Ws, _, _, cases, _) in enumerate(refs):
+            for k in range(len(Ws)):
+                for s in range(4):
+                    if cases & (1 << s):
+                        same = np.array_equal(outs[True][i][4 * k + s], outs[False][i][4 * k + s])
+                        if (i, s) in routed:
+                            assert not same, (i, k, s)
+                        elif (i, s) in same_groups:
+                            assert same, (i, k, s)
+    finally:
+        ctx.set_tensor_cores(True)
+        ctx.set_stream(0)
+
+
 def test_batch_launch_form_in_a_graph(ctx):
     """blocks_per_sm = -1: one launch per window group, captured into a CUDA graph and replayed."""
     probs, refs = _batch_problems(seed=5)
