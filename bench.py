@@ -610,7 +610,7 @@ def run_set(args):
         ws, spectra, noise = syn.covariance_inputs(L)
         blocks = syn.COV_BLOCKS
         n = L + 1
-        jobs, outs_c, outs_p = [], [], []
+        jobs, outs_c, outs_p, outs_b = [], [], [], []
         windows = set()
         for (a, b) in blocks:
             kind, S, R, Ws = pg.covariance.gather(a, b, ws, spectra, noise)
@@ -618,16 +618,23 @@ def run_set(args):
             jobs.append((kind, [dev(x) for x in S], [dev(x) for x in R], [dev(x) for x in Ws]))
             outs_c.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
             outs_p.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
+            outs_b.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
 
-        def run(mode, outs):
+        def run_set(mode, outs):  # one ps_coupledcov_set_device call for the six blocks
+            ctx.coupledcov_set_device([(kind, [x.data_ptr() for x in S], [x.data_ptr() for x in R],
+                                        [x.data_ptr() for x in Ws], C.data_ptr())
+                                       for (kind, S, R, Ws), C in zip(jobs, outs)], n, 0, L, n, mode=mode)
+
+        def run_blocks(mode, outs):  # one ps_coupledcov_device call per block
             for (kind, S, R, Ws), C in zip(jobs, outs):
                 ctx.coupledcov_device(kind, [x.data_ptr() for x in S], [x.data_ptr() for x in R],
                                       [x.data_ptr() for x in Ws], n, 0, L, C.data_ptr(), n, mode=mode)
         elements = len(jobs) * n * n
         line["config"].update({"lmax": L, "blocks": ["%s%s" % bl for bl in blocks],
-                               "windows": sum(len(j[3]) for j in jobs), "distinct_windows": len(windows)})
-        chosen = lambda: run("chosen", outs_c)
-        plain = lambda: run("plain", outs_p)
+                               "windows": sum(len(j[3]) for j in jobs), "distinct_windows": len(windows),
+                               "call": "ps_coupledcov_set_device"})
+        chosen = lambda: run_set("chosen", outs_c)
+        plain = lambda: run_set("plain", outs_p)
         mats = list(zip(outs_c, outs_p))
     else:
         probs = _set_problems(args.config, args.lmax)
@@ -702,7 +709,18 @@ def run_set(args):
     for _ in range(max(args.warmup, 3)):
         chosen()
     t_c = ev_time(chosen, args.steps)
-    if args.config != "cov_2508":
+    if args.config == "cov_2508":
+        # the same blocks as six separate ps_coupledcov_device calls (fused kernels only)
+        blk = lambda: run_blocks("chosen", outs_b)
+        blk()
+        t_b = ev_time(blk, 2)
+        d = 0.0
+        for c, q in zip(outs_c, outs_b):
+            den = torch.where(q == 0, torch.ones_like(q), q.abs())
+            d = max(d, float(((c - q).abs() / den).max().item()))
+        line["per_block_calls"] = {"ms_per_step": t_b * 1e3, "steps": 2, "set_over_per_block": t_b / t_c,
+                                   "max_rel_diff_vs_timed_path": d}
+    else:
         d = 0.0
         for (c, _), r in zip(mats, seq_rows):
             b = c[[0, c.shape[0] // 2, c.shape[0] - 1]]

@@ -121,6 +121,19 @@ int ps_coupledcov(ps_ctx *ctx, int kind, const double *const *S, const double *c
                   int64_t nW, int lmin, int lmax, int mode, double *C, int64_t ldc);
 int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const double *const *dR,
                          const double *const *dW, int64_t nW, int lmin, int lmax, int mode, double *dC, int64_t ldc);
+/* Several covariance blocks of one (l1, l2) grid (device pointers, enqueued
+ * on the context stream): block b is ps_coupledcov_device(kinds[b], dS[b],
+ * dR[b], dW[b], ..., dC[b]).  The reference computes one block per
+ * loop_cov*! call; here, in chosen mode, the blocks whose windows all use
+ * the squared (0 0 0) family (TTTT, TTTE, TTEE) have their windows' Xi
+ * computed together by the tensor-core kernel when there are 5 or more such
+ * windows (one family generation per pair for up to 15 windows), and each
+ * such block is formed from them by the same per-element formula; the other
+ * blocks run the fused covariance kernel.  dR[b] may be NULL for kinds
+ * without noise ratios (TTEE). */
+int ps_coupledcov_set_device(ps_ctx *ctx, int nblk, const int *kinds, const double *const *const *dS,
+                             const double *const *const *dR, const double *const *const *dW, int64_t nW, int lmin,
+                             int lmax, int mode, double *const *dC, int64_t ldc);
 
 /* Many mask spectra on one (l1, l2) grid: for window k and every spin case s
  * selected in `cases`, dM[4*k + s] receives the matrix (entries of unselected

@@ -59,6 +59,13 @@ struct ps_ctx {
     size_t part_cap = 0;
     double* d_qp = nullptr;  // chosen QuickPol scratch: W as floats and its exponent
     size_t qp_cap = 0;
+    // covariance sets: the windows of the tensor-core launches (padded, split) and their Xi
+    double* d_cwin = nullptr;
+    size_t cwin_cap = 0;
+    int2* d_cbf = nullptr;
+    size_t cbf_cap = 0;
+    double* d_xi = nullptr;
+    size_t xi_cap = 0;
     double* h_pack = nullptr;  // pinned host staging for packed coefficient sets
     size_t pack_cap = 0;
     // batched workload state (ps_batch_*)
@@ -559,6 +566,9 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_win);
     cudaFree(c->d_raw);
     cudaFree(c->d_spec);
+    cudaFree(c->d_cwin);
+    cudaFree(c->d_cbf);
+    cudaFree(c->d_xi);
     cudaFree(c->d_out);
     cudaFree(c->d_probe);
     cudaFree(c->d_bf);
@@ -752,7 +762,8 @@ int ps_xi(ps_ctx* c, int product, int parity, const double* const* W, int K, int
 }
 
 static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* const* R, const double* const* W,
-                    int64_t nW, int lmin, int lmax, int mode, double* C, int64_t ldc, bool host)
+                    int64_t nW, int lmin, int lmax, int mode, double* C, int64_t ldc, bool host, bool first = true,
+                    bool last = true)
 {
     int st = check_grid(c, lmin, lmax, nW, ldc);
     if (st) return st;
@@ -803,7 +814,7 @@ static int cov_impl(ps_ctx* c, int kind, const double* const* S, const double* c
         p.out[0] = C;
         p.ldo = ldc;
     }
-    if ((st = run_coupling(c, p, mode))) return st;
+    if ((st = run_coupling(c, p, mode, first, last))) return st;
     if (host) {
         if (!mapped)
             PS_CUDA(c, cudaMemcpy2DAsync(C, (size_t)ldc * sizeof(double), p.out[0], (size_t)n * sizeof(double),
@@ -823,6 +834,122 @@ int ps_coupledcov_device(ps_ctx* c, int kind, const double* const* dS, const dou
                          const double* const* dW, int64_t nW, int lmin, int lmax, int mode, double* dC, int64_t ldc)
 {
     return cov_impl(c, kind, dS, dR, dW, nW, lmin, lmax, mode, dC, ldc, false);
+}
+
+int ps_coupledcov_set_device(ps_ctx* c, int nblk, const int* kinds, const double* const* const* dS,
+                             const double* const* const* dR, const double* const* const* dW, int64_t nW, int lmin,
+                             int lmax, int mode, double* const* dC, int64_t ldc)
+{
+    int st = check_grid(c, lmin, lmax, nW, ldc);
+    if (st) return st;
+    if ((st = check_mode(c, mode))) return st;
+    if (nblk < 1 || !kinds || !dS || !dW || !dC)
+        return set_err(c, PS_ERR_ARG, "nblk >= 1 and the kinds, S, W and C arrays are required");
+    for (int b = 0; b < nblk; ++b) {
+        const int K = ps::cov_nwindows(kinds[b]), NR = ps::cov_nratios(kinds[b]);
+        if (K < 0) return set_err(c, PS_ERR_ARG, "block %d: %d is not a covariance kind", b, kinds[b]);
+        if (!dS[b] || !dW[b] || !dC[b] || (NR > 0 && (!dR || !dR[b])))
+            return set_err(c, PS_ERR_ARG, "block %d: S, R, W and C must not be NULL", b);
+        for (int i = 0; i < 4; ++i)
+            if (!dS[b][i]) return set_err(c, PS_ERR_ARG, "block %d: spectrum S[%d] is NULL", b, i);
+        for (int i = 0; i < NR; ++i)
+            if (!dR[b][i]) return set_err(c, PS_ERR_ARG, "block %d: noise ratio R[%d] is NULL", b, i);
+        for (int k = 0; k < K; ++k)
+            if (!dW[b][k]) return set_err(c, PS_ERR_ARG, "block %d: window %d is NULL", b, k);
+    }
+    PS_CUDA(c, cudaSetDevice(c->device));
+    // Chosen mode: the blocks whose windows all use the squared (0 0 0) family (TTTT, TTTE, TTEE)
+    // have their windows' Xi computed together by the (0 0 0) tensor-core kernel, up to
+    // kMmaMaxSlots windows per launch, when there are kMmaMin00 or more such windows; each such
+    // block is then formed from its Xi.  The other blocks run the fused covariance kernel.
+    std::vector<int> tcb;
+    int nx = 0;
+    if (mode == PS_MODE_CHOSEN && c->tensor_cores) {
+        for (int b = 0; b < nblk; ++b) {
+            const int K = ps::cov_nwindows(kinds[b]);
+            bool all00 = true;
+            for (int k = 0; k < K; ++k) {
+                int prod, par;
+                ps::cov_window_spec(kinds[b], k, &prod, &par);
+                all00 = all00 && prod == ps::PROD_00_00;
+            }
+            if (all00) {
+                tcb.push_back(b);
+                nx += K;
+            }
+        }
+        if (nx < kMmaMin00) {
+            tcb.clear();
+            nx = 0;
+        }
+    }
+    PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    if (!tcb.empty()) {
+        const long long n = lmax - lmin + 1;
+        const int wlen = 2 * lmax + 2;
+        const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+        if ((st = ensure(c, &c->d_cwin, &c->cwin_cap, (size_t)nx * wlen)) ||
+            (st = ensure_int2(c, &c->d_cbf, &c->cbf_cap, (size_t)nx * wlen)) ||
+            (st = ensure(c, &c->d_xi, &c->xi_cap, (size_t)nx * n * n)) || (st = ensure_mtiles(c, lmin, lmax)) ||
+            (st = arm_status(c, c->stream)))
+            return st;
+        int j = 0;
+        for (int b : tcb)
+            for (int k = 0; k < ps::cov_nwindows(kinds[b]); ++k, ++j) {
+                PS_CUDA(c, ps::launch_pad_windows(c->d_cwin + (size_t)j * wlen, dW[b][k], nuse, wlen, c->stream));
+                PS_CUDA(c, ps::launch_split_windows(c->d_cbf + (size_t)j * wlen, c->d_cwin + (size_t)j * wlen, wlen,
+                                                    c->stream));
+                c->launches += 2;
+            }
+        for (int i0 = 0; i0 < nx; i0 += ps::kMmaMaxSlots) {
+            ps::MmaParams mp;
+            memset(&mp, 0, sizeof(mp));
+            mp.lmin = lmin;
+            mp.lmax = lmax;
+            mp.nslot = std::min(nx - i0, ps::kMmaMaxSlots);
+            for (int q = 0; q < mp.nslot; ++q) {
+                mp.bf[q] = c->d_cbf + (size_t)(i0 + q) * wlen;
+                mp.wW[q] = c->d_cwin + (size_t)(i0 + q) * wlen;
+                mp.parity[q] = ps::PAR_ALL;
+                mp.out[q] = c->d_xi + (size_t)(i0 + q) * n * n;
+            }
+            mp.ldo = n;
+            mp.wlen = wlen;
+            mp.epilogue = ps::EPI_XI;
+            mp.tiles = c->d_mtiles;
+            mp.ntiles = c->nmtiles;
+            mp.status = c->d_status;
+            PS_CUDA(c, ps::launch_mma(mp, true, c->stream));
+            c->launches++;
+        }
+        j = 0;
+        for (int b : tcb) {
+            ps::CovCombineParams cp;
+            memset(&cp, 0, sizeof(cp));
+            cp.kind = kinds[b];
+            cp.lmin = lmin;
+            cp.n = (int)n;
+            cp.nx = ps::cov_nwindows(kinds[b]);
+            for (int i = 0; i < 4; ++i) cp.S[i] = dS[b][i];
+            for (int i = 0; i < ps::cov_nratios(kinds[b]); ++i) cp.R[i] = dR[b][i];
+            for (int k = 0; k < cp.nx; ++k) cp.X[k] = c->d_xi + (size_t)(j + k) * n * n;
+            j += cp.nx;
+            cp.ldx = n;
+            cp.C = dC[b];
+            cp.ldc = ldc;
+            PS_CUDA(c, ps::launch_cov_combine(cp, c->stream));
+            c->launches++;
+        }
+    }
+    for (int b = 0; b < nblk; ++b) {
+        if (std::find(tcb.begin(), tcb.end(), b) != tcb.end()) continue;
+        if ((st = cov_impl(c, kinds[b], dS[b], ps::cov_nratios(kinds[b]) > 0 ? dR[b] : nullptr, dW[b], nW, lmin, lmax,
+                           mode, dC[b], ldc, false, false, false)))
+            return st;
+    }
+    PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+    c->timed = true;
+    return PS_OK;
 }
 
 int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K, int64_t nW, int lmin, int lmax,

@@ -135,6 +135,19 @@ struct MmaParams {
 // fam00: the (0 0 0) family (every slot PAR_ALL); otherwise the (2 -2 0) family
 cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s);
 
+// A covariance block from its Xi matrices (ps_cov_combine.cu): C[l1, l2] =
+// cov_combine(kind, S, R, {X_k[l1, l2]}, l1, l2) over the whole n x n block.
+struct CovCombineParams {
+    int kind, lmin, n, nx;     // nx: the block's windows (cov_nwindows(kind))
+    const double* S[4];
+    const double* R[4];
+    const double* X[kMaxWin];  // the block's windows' Xi, n x n, leading dimension ldx
+    long long ldx;
+    double* C;
+    long long ldc;
+};
+cudaError_t launch_cov_combine(const CovCombineParams& p, cudaStream_t s);
+
 // Host-side covariance table (ps_api.cu).
 int cov_nwindows(int kind);
 int cov_nratios(int kind);

@@ -25,7 +25,7 @@ MODES = {"plain": PS_MODE_PLAIN_FP64, "fp64": PS_MODE_PLAIN_FP64, "chosen": PS_M
 
 # every symbol declared in include/powerspectra_gpu.h
 EXPORTS = ("ps_create", "ps_destroy", "ps_last_error", "ps_set_stream", "ps_synchronize", "ps_mcm", "ps_mcm_multi",
-           "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_mcm_set_device",
+           "ps_mcm_multi_device", "ps_xi", "ps_coupledcov", "ps_coupledcov_device", "ps_coupledcov_set_device", "ps_mcm_set_device",
            "ps_batch_prepare", "ps_batch_run", "ps_batch_graph_launch", "ps_batch_autotune", "ps_last_kernel_ms",
            "ps_launch_count", "ps_probe_fma_peak", "ps_mcm_multi_device_noalloc", "ps_decouple_covmat", "ps_solve",
            "ps_quickpol_xi", "ps_decouple_covmat_device", "ps_window_W", "ps_window_W_device",
@@ -101,6 +101,9 @@ def load(path=None):
         lib.ps_coupledcov.restype = ci
         lib.ps_coupledcov_device.argtypes = [vp, ci, _DPP, _DPP, _DPP, i64, ci, ci, ci, _DP, i64]
         lib.ps_coupledcov_device.restype = ci
+        lib.ps_coupledcov_set_device.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(_DPP),
+                                                 ctypes.POINTER(_DPP), ctypes.POINTER(_DPP), i64, ci, ci, ci, _DPP, i64]
+        lib.ps_coupledcov_set_device.restype = ci
         lib.ps_mcm_set_device.argtypes = [vp, ctypes.c_uint, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
         lib.ps_mcm_set_device.restype = ci
         lib.ps_mcm_set.argtypes = [vp, ctypes.c_uint, _DPP, ci, i64, ci, ci, ci, _DPP, i64]
@@ -346,6 +349,20 @@ class Context:
         self.check(self.lib.ps_coupledcov_device(self.handle, k, dptr_array([int(x) for x in dS]),
                                                  dptr_array([int(x) for x in dR]), dptr_array([int(x) for x in dW]),
                                                  int(nW), lmin, lmax, mode_code(mode), dptr(int(dC)), int(ldc)))
+
+    def coupledcov_set_device(self, blocks, nW, lmin, lmax, ldc, mode="chosen"):
+        """Several covariance blocks of one grid: `blocks` is a list of (kind, dS, dR, dW, dC) with
+        device addresses as ints (dR may be empty for TTEE)."""
+        nb = len(blocks)
+        kinds = (ctypes.c_int * nb)(*[COV_KINDS[b[0]] if isinstance(b[0], str) else int(b[0]) for b in blocks])
+        keep = [(dptr_array([int(x) for x in b[1]]), dptr_array([int(x) for x in b[2]]),
+                 dptr_array([int(x) for x in b[3]])) for b in blocks]
+        S = (_DPP * nb)(*[ctypes.cast(k[0], _DPP) for k in keep])
+        R = (_DPP * nb)(*[ctypes.cast(k[1], _DPP) if len(b[2]) else None for k, b in zip(keep, blocks)])
+        W = (_DPP * nb)(*[ctypes.cast(k[2], _DPP) for k in keep])
+        C = dptr_array([int(b[4]) for b in blocks])
+        self.check(self.lib.ps_coupledcov_set_device(self.handle, nb, kinds, S, R, W, int(nW), lmin, lmax,
+                                                     mode_code(mode), C, int(ldc)))
 
     def mcm_set(self, cases, Ws, lmin, lmax, mode="chosen", outs=None, slots=None):
         """mcm for a set of host spectra on one grid: returns {(k, s): matrix} for window k and each spin
