@@ -124,13 +124,16 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
 /* Several covariance blocks of one (l1, l2) grid (device pointers, enqueued
  * on the context stream): block b is ps_coupledcov_device(kinds[b], dS[b],
  * dR[b], dW[b], ..., dC[b]).  The reference computes one block per
- * loop_cov*! call; here, in chosen mode, the blocks whose windows all use
- * the squared (0 0 0) family (TTTT, TTTE, TTEE) have their windows' Xi
- * computed together by the tensor-core kernel when there are 5 or more such
- * windows (one family generation per pair for up to 15 windows), and each
- * such block is formed from them by the same per-element formula; the other
- * blocks run the fused covariance kernel.  dR[b] may be NULL for kinds
- * without noise ratios (TTEE). */
+ * loop_cov*! call.  Here, in chosen mode, the Xi of all the blocks' windows
+ * are computed grouped across the blocks by family product and parity, so
+ * one family generation serves each group: the squared (0 0 0) windows by the
+ * tensor-core kernel when there are 5 or more (up to 15 per launch), the
+ * squared (2 -2 0) ones by the tensor-core kernel when there are more than 8,
+ * the others by the CUDA-core kernel in groups of up to 8.  Each block is then
+ * formed from its windows' Xi by the same per-element formula as the fused
+ * kernel.  Plain FP64, or ps_set_tensor_cores(ctx, 0), runs the fused kernel
+ * block by block.  Scratch: one n x n FP64 matrix per window (n = lmax - lmin
+ * + 1).  dR[b] may be NULL for kinds without noise ratios (TTEE). */
 int ps_coupledcov_set_device(ps_ctx *ctx, int nblk, const int *kinds, const double *const *const *dS,
                              const double *const *const *dR, const double *const *const *dW, int64_t nW, int lmin,
                              int lmax, int mode, double *const *dC, int64_t ldc);

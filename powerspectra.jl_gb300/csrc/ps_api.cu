@@ -858,94 +858,116 @@ int ps_coupledcov_set_device(ps_ctx* c, int nblk, const int* kinds, const double
             if (!dW[b][k]) return set_err(c, PS_ERR_ARG, "block %d: window %d is NULL", b, k);
     }
     PS_CUDA(c, cudaSetDevice(c->device));
-    // Chosen mode: the blocks whose windows all use the squared (0 0 0) family (TTTT, TTTE, TTEE)
-    // have their windows' Xi computed together by the (0 0 0) tensor-core kernel, up to
-    // kMmaMaxSlots windows per launch, when there are kMmaMin00 or more such windows; each such
-    // block is then formed from its Xi.  The other blocks run the fused covariance kernel.
-    std::vector<int> tcb;
-    int nx = 0;
-    if (mode == PS_MODE_CHOSEN && c->tensor_cores) {
-        for (int b = 0; b < nblk; ++b) {
-            const int K = ps::cov_nwindows(kinds[b]);
-            bool all00 = true;
-            for (int k = 0; k < K; ++k) {
-                int prod, par;
-                ps::cov_window_spec(kinds[b], k, &prod, &par);
-                all00 = all00 && prod == ps::PROD_00_00;
-            }
-            if (all00) {
-                tcb.push_back(b);
-                nx += K;
-            }
-        }
-        if (nx < kMmaMin00) {
-            tcb.clear();
-            nx = 0;
-        }
-    }
     PS_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-    if (!tcb.empty()) {
-        const long long n = lmax - lmin + 1;
-        const int wlen = 2 * lmax + 2;
-        const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
-        if ((st = ensure(c, &c->d_cwin, &c->cwin_cap, (size_t)nx * wlen)) ||
-            (st = ensure_int2(c, &c->d_cbf, &c->cbf_cap, (size_t)nx * wlen)) ||
-            (st = ensure(c, &c->d_xi, &c->xi_cap, (size_t)nx * n * n)) || (st = ensure_mtiles(c, lmin, lmax)) ||
-            (st = arm_status(c, c->stream)))
-            return st;
-        int j = 0;
-        for (int b : tcb)
-            for (int k = 0; k < ps::cov_nwindows(kinds[b]); ++k, ++j) {
-                PS_CUDA(c, ps::launch_pad_windows(c->d_cwin + (size_t)j * wlen, dW[b][k], nuse, wlen, c->stream));
-                PS_CUDA(c, ps::launch_split_windows(c->d_cbf + (size_t)j * wlen, c->d_cwin + (size_t)j * wlen, wlen,
-                                                    c->stream));
-                c->launches += 2;
-            }
-        for (int i0 = 0; i0 < nx; i0 += ps::kMmaMaxSlots) {
-            ps::MmaParams mp;
-            memset(&mp, 0, sizeof(mp));
-            mp.lmin = lmin;
-            mp.lmax = lmax;
-            mp.nslot = std::min(nx - i0, ps::kMmaMaxSlots);
-            for (int q = 0; q < mp.nslot; ++q) {
-                mp.bf[q] = c->d_cbf + (size_t)(i0 + q) * wlen;
-                mp.wW[q] = c->d_cwin + (size_t)(i0 + q) * wlen;
-                mp.parity[q] = ps::PAR_ALL;
-                mp.out[q] = c->d_xi + (size_t)(i0 + q) * n * n;
-            }
-            mp.ldo = n;
-            mp.wlen = wlen;
-            mp.epilogue = ps::EPI_XI;
-            mp.tiles = c->d_mtiles;
-            mp.ntiles = c->nmtiles;
-            mp.status = c->d_status;
-            PS_CUDA(c, ps::launch_mma(mp, true, c->stream));
-            c->launches++;
+    if (mode != PS_MODE_CHOSEN || !c->tensor_cores) {  // the fused kernel, block by block
+        for (int b = 0; b < nblk; ++b)
+            if ((st = cov_impl(c, kinds[b], dS[b], ps::cov_nratios(kinds[b]) > 0 ? dR[b] : nullptr, dW[b], nW, lmin,
+                               lmax, mode, dC[b], ldc, false, false, false)))
+                return st;
+        PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+        c->timed = true;
+        return PS_OK;
+    }
+    // Chosen mode with the tensor cores: the Xi of every window of every block, grouped across
+    // the blocks by family product and parity, so that one family generation serves each group:
+    // the squared (0 0 0) windows by the (0 0 0) tensor-core kernel when there are kMmaMin00 or
+    // more, the squared (2 -2 0) ones by the (2 -2 0) tensor-core kernel when there are kMmaMin22
+    // or more, and the others by the CUDA-core kernel in groups of up to kMaxWin.  Then each block
+    // is formed from its windows' Xi.
+    struct XWin {
+        int b, k, prod, par;
+    };
+    std::vector<XWin> xw;
+    for (int b = 0; b < nblk; ++b)
+        for (int k = 0; k < ps::cov_nwindows(kinds[b]); ++k) {
+            XWin x{b, k, 0, 0};
+            ps::cov_window_spec(kinds[b], k, &x.prod, &x.par);
+            xw.push_back(x);
         }
-        j = 0;
-        for (int b : tcb) {
-            ps::CovCombineParams cp;
-            memset(&cp, 0, sizeof(cp));
-            cp.kind = kinds[b];
-            cp.lmin = lmin;
-            cp.n = (int)n;
-            cp.nx = ps::cov_nwindows(kinds[b]);
-            for (int i = 0; i < 4; ++i) cp.S[i] = dS[b][i];
-            for (int i = 0; i < ps::cov_nratios(kinds[b]); ++i) cp.R[i] = dR[b][i];
-            for (int k = 0; k < cp.nx; ++k) cp.X[k] = c->d_xi + (size_t)(j + k) * n * n;
-            j += cp.nx;
-            cp.ldx = n;
-            cp.C = dC[b];
-            cp.ldc = ldc;
-            PS_CUDA(c, ps::launch_cov_combine(cp, c->stream));
-            c->launches++;
+    const int nx = (int)xw.size();
+    const long long n = lmax - lmin + 1;
+    const int wlen = 2 * lmax + 2;
+    const long long nuse = nW < (int64_t)(2 * lmax + 1) ? nW : (int64_t)(2 * lmax + 1);
+    if ((st = ensure(c, &c->d_cwin, &c->cwin_cap, (size_t)nx * wlen)) ||
+        (st = ensure_int2(c, &c->d_cbf, &c->cbf_cap, (size_t)nx * wlen)) ||
+        (st = ensure(c, &c->d_xi, &c->xi_cap, (size_t)nx * n * n)))
+        return st;
+    for (int j = 0; j < nx; ++j) {
+        PS_CUDA(c, ps::launch_pad_windows(c->d_cwin + (size_t)j * wlen, dW[xw[j].b][xw[j].k], nuse, wlen, c->stream));
+        PS_CUDA(c, ps::launch_split_windows(c->d_cbf + (size_t)j * wlen, c->d_cwin + (size_t)j * wlen, wlen, c->stream));
+        c->launches += 2;
+    }
+    const int classes[4][2] = {{ps::PROD_00_00, ps::PAR_ALL}, {ps::PROD_22_22, ps::PAR_EVEN},
+                               {ps::PROD_22_22, ps::PAR_ODD}, {ps::PROD_00_22, ps::PAR_EVEN}};
+    for (const auto& cl : classes) {
+        std::vector<int> js;
+        for (int j = 0; j < nx; ++j)
+            if (xw[j].prod == cl[0] && xw[j].par == cl[1]) js.push_back(j);
+        if (js.empty()) continue;
+        const bool mma00 = cl[0] == ps::PROD_00_00 && (int)js.size() >= kMmaMin00;
+        const bool mma22 = cl[0] == ps::PROD_22_22 && (int)js.size() >= kMmaMin22;
+        if (mma00 || mma22) {
+            if ((st = ensure_mtiles(c, lmin, lmax)) || (st = arm_status(c, c->stream))) return st;
+            for (size_t i0 = 0; i0 < js.size(); i0 += ps::kMmaMaxSlots) {
+                ps::MmaParams mp;
+                memset(&mp, 0, sizeof(mp));
+                mp.lmin = lmin;
+                mp.lmax = lmax;
+                mp.nslot = (int)std::min(js.size() - i0, (size_t)ps::kMmaMaxSlots);
+                for (int q = 0; q < mp.nslot; ++q) {
+                    const int j = js[i0 + q];
+                    mp.bf[q] = c->d_cbf + (size_t)j * wlen;
+                    mp.wW[q] = c->d_cwin + (size_t)j * wlen;
+                    mp.parity[q] = cl[1];
+                    mp.out[q] = c->d_xi + (size_t)j * n * n;
+                }
+                mp.ldo = n;
+                mp.wlen = wlen;
+                mp.epilogue = ps::EPI_XI;
+                mp.tiles = c->d_mtiles;
+                mp.ntiles = c->nmtiles;
+                mp.status = c->d_status;
+                PS_CUDA(c, ps::launch_mma(mp, mma00, c->stream));
+                c->launches++;
+            }
+        } else {
+            for (size_t i0 = 0; i0 < js.size(); i0 += ps::kMaxWin) {
+                ps::CouplingParams p;
+                memset(&p, 0, sizeof(p));
+                p.lmin = lmin;
+                p.lmax = lmax;
+                p.epilogue = ps::EPI_XI;
+                p.wlen = wlen;
+                p.nwin = (int)std::min(js.size() - i0, (size_t)ps::kMaxWin);
+                for (int q = 0; q < p.nwin; ++q) {
+                    const int j = js[i0 + q];
+                    p.win[q].product = cl[0];
+                    p.win[q].parity = cl[1];
+                    p.win[q].wW = c->d_cwin + (size_t)j * wlen;
+                    p.win[q].bf = c->d_cbf + (size_t)j * wlen;
+                    p.out[q] = c->d_xi + (size_t)j * n * n;
+                }
+                p.ldo = n;
+                if ((st = run_coupling(c, p, mode, false, false))) return st;
+            }
         }
     }
-    for (int b = 0; b < nblk; ++b) {
-        if (std::find(tcb.begin(), tcb.end(), b) != tcb.end()) continue;
-        if ((st = cov_impl(c, kinds[b], dS[b], ps::cov_nratios(kinds[b]) > 0 ? dR[b] : nullptr, dW[b], nW, lmin, lmax,
-                           mode, dC[b], ldc, false, false, false)))
-            return st;
+    for (int b = 0, j = 0; b < nblk; ++b) {
+        ps::CovCombineParams cp;
+        memset(&cp, 0, sizeof(cp));
+        cp.kind = kinds[b];
+        cp.lmin = lmin;
+        cp.n = (int)n;
+        cp.nx = ps::cov_nwindows(kinds[b]);
+        for (int i = 0; i < 4; ++i) cp.S[i] = dS[b][i];
+        for (int i = 0; i < ps::cov_nratios(kinds[b]); ++i) cp.R[i] = dR[b][i];
+        for (int k = 0; k < cp.nx; ++k) cp.X[k] = c->d_xi + (size_t)(j + k) * n * n;
+        j += cp.nx;
+        cp.ldx = n;
+        cp.C = dC[b];
+        cp.ldc = ldc;
+        PS_CUDA(c, ps::launch_cov_combine(cp, c->stream));
+        c->launches++;
     }
     PS_CUDA(c, cudaEventRecord(c->ev1, c->stream));
     c->timed = true;
