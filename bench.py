@@ -614,7 +614,7 @@ def run_set(args):
         windows = set()
         for (a, b) in blocks:
             kind, S, R, Ws = pg.covariance.gather(a, b, ws, spectra, noise)
-            windows.update(id(w) for w in Ws)
+            windows.update(hash(np.ascontiguousarray(w).tobytes()) for w in Ws)  # distinct spectra by content
             jobs.append((kind, [dev(x) for x in S], [dev(x) for x in R], [dev(x) for x in Ws]))
             outs_c.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
             outs_p.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
