@@ -573,27 +573,25 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         RingIdx ix22;
         if constexpr (F00) ix00 = ring00_idx(q * kK + fofs, q * kK + bofs, l2);
         else ix22 = ring_idx(q * kK + fofs, q * kK + bofs, l2);
-#pragma unroll 2
-        for (int s2 = 0; s2 < kK; s2 += 2) {
+        // One step pair of the block: the steps of both sweeps, then x into tensor memory.  In a
+        // block whose steps all lie in the steady state, every lane that runs is inside both
+        // sweeps, so both steps run unconditionally (their dependency chains interleave).  Lanes
+        // that do not run compute values that may not be finite: they reach only their own rows
+        // of the MMAs (row m of D is row m of A times B) and their own totals, never written.
+        // The other blocks (the first few and the last) check every step.
+        auto pair = [&](int s2, bool steady) {
             float xf[2], xb[2];
             const int tau0 = q * kK + s2;
-            // steady state: every lane that runs is inside both sweeps, so both steps run
-            // unconditionally (their dependency chains interleave).  Lanes that do not run
-            // compute values that may not be finite: they reach only their own rows of the
-            // MMAs (row m of D is row m of A times B) and their own totals, never written.
             if constexpr (F00) {
-                if (tau0 >= 34 && tau0 + 1 <= steady00) {
 #pragma unroll
-                    for (int e = 0; e < 2; ++e) {
+                for (int e = 0; e < 2; ++e) {
+                    const int nf = tau0 + e + fofs, nb = tau0 + e + bofs;
+                    if (steady) {
                         xf[e] = sq(F.f);
                         xb[e] = sq(B.f);
                         fwd_step00c(F.f, R, ix00, s2 + e);
                         bwd_step00c(B.f, R, ix00, s2 + e);
-                    }
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {
-                        const int nf = tau0 + e + fofs, nb = tau0 + e + bofs;
+                    } else {
                         xf[e] = 0.0f;
                         xb[e] = 0.0f;
                         if (nf >= 0 && nf < nx00) {
@@ -608,18 +606,15 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 }
             } else {
                 const int k = s2 >> 1;  // the step pair of the block
-                if (tau0 >= kSteady && tau0 + 1 <= r0 + kLead - 1) {
 #pragma unroll
-                    for (int e = 0; e < 2; ++e) {
+                for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
+                    const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
+                    if (steady) {
                         xf[e] = sq(F.f);
                         xb[e] = sq(B.f);
                         fwd_step(F, R, e, ix22, k);
                         bwd_step(B, R, e, ix22, k);
-                    }
-                } else {
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
-                        const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
+                    } else {
                         xf[e] = 0.0f;
                         xb[e] = 0.0f;
                         if (tf >= 0 && tf < T) {
@@ -642,6 +637,15 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 umma::st_x1(tlane + a_col(buf, 0, pl) + (uint32_t)(s2 >> 1), wf[pl]);
                 umma::st_x1(tlane + a_col(buf, 1, pl) + (uint32_t)(s2 >> 1), wb[pl]);
             }
+        };
+        const int t0 = q * kK, t1 = q * kK + kK - 1;  // the block's first and last time step
+        const bool steady = F00 ? (t0 >= 34 && t1 <= steady00) : (t0 >= kSteady && t1 <= r0 + kLead - 1);
+        if (steady) {
+#pragma unroll 2
+            for (int s2 = 0; s2 < kK; s2 += 2) pair(s2, true);
+        } else {
+#pragma unroll 1
+            for (int s2 = 0; s2 < kK; s2 += 2) pair(s2, false);
         }
         // ---- block boundary ----
         if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
