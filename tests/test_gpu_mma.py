@@ -164,6 +164,38 @@ def test_mma_lmax_8191_sampled_rows(ctx):
             assert max_err_scaled(G[r:, r], R[r:, r], np.abs(R[r:, r])) < TOL, (k, s, r)
 
 
+def test_mma_at_the_largest_lmax(ctx):
+    """lmax 16383 (the largest the library accepts), nW 32767: 5 TT slots and 10 ++/-- slots on the
+    tensor-core kernels; sampled rows and columns against the oracle (sampled on the device)."""
+    from powerspectra_gpu import synthetic as syn
+    L = 16383
+    n = L + 1
+    Ws = [syn.mask_spectrum(2 * L + 1, 0.5 + 0.05 * k, 1500.0 + 100.0 * k, seed=16000 + k) for k in range(5)]
+    slots = [(k, s) for k in range(5) for s in (0, 2, 3)]
+    dW = [torch.tensor(w, device="cuda") for w in Ws]
+    mats = {sl: torch.empty((n, n), dtype=torch.float64, device="cuda") for sl in slots}
+    ptrs = [0] * (4 * len(Ws))
+    for (k, s), m in mats.items():
+        ptrs[4 * k + s] = m.data_ptr()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        ctx.mcm_set_device(0xD, [d.data_ptr() for d in dW], 2 * L + 1, 0, L, ptrs, n, mode="chosen")
+        torch.cuda.synchronize()
+        ctx.synchronize()
+    finally:
+        ctx.set_stream(0)
+    rows = [2, 9000, 16383]
+    for (k, s) in [(0, 0), (4, 0), (1, 2), (3, 3)]:
+        R = o.inner_mcm(s, Ws[k], 0, L, rows=rows)
+        m = mats[k, s]  # column-major storage: m[l2, l1] = M[l1, l2]
+        for r in rows:
+            row, col = m[r:, r].cpu().numpy(), m[r, r:].cpu().numpy()  # M[r, r:] and M[r:, r]
+            assert max_err_scaled(row, R[r, r:], np.abs(R[r, r:])) < TOL, (k, s, r)
+            assert max_err_scaled(col, R[r:, r], np.abs(R[r:, r])) < TOL, (k, s, r)
+    del mats
+    torch.cuda.empty_cache()
+
+
 def test_mma_host_entry_point(ctx):
     """ps_mcm_set (host spectra, page-locked and pageable outputs) through the tensor-core kernels."""
     L = 300
