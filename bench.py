@@ -483,9 +483,11 @@ def _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements):
             ctx.mcm_set(wl["cases_mask"], hW, lmin, lmax, mode=mode, outs=hM, slots=set(slots))
     host_step()  # warm the host path
     barrier()
+    kms = 0.0
     e0 = time.perf_counter()
     for _ in range(args.steps):
         host_step()
+        kms += ctx.last_kernel_ms()  # the call has synchronised: its coupling kernels' CUDA-event time
     barrier()
     e_el = max_over_ranks(time.perf_counter() - e0)
     nuse = min(nW, 2 * lmax + 1)
@@ -493,7 +495,8 @@ def _run_e2e(ctx, wl, args, barrier, max_over_ranks, world, elements):
            "h2d_bytes_per_step": int(len(set(k for k, _ in slots)) * nuse * 8),
            "d2h_bytes_per_step": int(elements * 8),
            "call": "ps_mcm_multi" if wl["kind"] == "multi" else "ps_mcm_set",
-           "how": "pinned host spectra in; pinned host matrices out, written by the kernel in place"}
+           "how": "pinned host spectra in; pinned host matrices out, written by the kernel in place",
+           "kernel_ms_per_step": kms / args.steps}
     del hM
     return e2e
 
