@@ -29,27 +29,29 @@
 // points per time step: lane (w, i) takes forward step nF = tau - i + w - 3
 // (l3 = l2 - l1 + 2 nF) and backward step nB = tau + w + i - 34
 // (l3 = l1 + l2 - 2 nB); every pair is at forward l3 = c0 - r0 - 6 + 2 tau and
-// backward l3 = r0 + c0 + 68 - 2 tau, and a block of 16 time steps covers 32
-// points, half the time steps of the one-point skew.
+// backward l3 = r0 + c0 + 68 - 2 tau: half the time steps of the one-point
+// skew.
 //
 // Precision.  x and B are split into three BF16 parts (hi + mid + lo carries
 // 24 bits) and D is formed from six products (all but the three smallest),
-// ordered so that the hi x hi product is added last: the tensor core rounds
-// its FP32 accumulation toward zero, so each 16-step D starts from zero and
-// takes one such rounding at full scale.  Each D is added to float-float
-// totals on the CUDA cores (into the low word; renormalised every fourth
-// block).  B is scaled per 16-step block by a running power of two (block
-// floating point; windows span 1e-45), the same role the slice exponents play
-// in the chosen kernel.  The last forward point, the match of
-// the two sweeps, the normalisation and the outputs are FP64.
+// ordered so that the hi x hi products are added last: the tensor core rounds
+// its FP32 accumulation toward zero, so each block's D starts from zero and
+// takes one such rounding at full scale per 16 steps (the hi x hi of each of
+// its two MMA halves).  Each D is added to float-float totals on the CUDA
+// cores (into the low word; renormalised every fourth block).  B is scaled per
+// block by a running power of two (block floating point; windows span 1e-45),
+// the same role the slice exponents play in the chosen kernel.  The last
+// forward point, the match of the two sweeps, the normalisation and the
+// outputs are FP64.
 //
-// Pipeline per 16-step block q: the lanes write x (three planes, two steps per
-// 32-bit column) into tensor memory; at the block end one thread issues the
-// 12 MMAs of q (6 per sweep) and commits them to an mbarrier; the lanes go on
-// with block q + 1 into the other A buffer, and at its end wait (bounded) for
-// q's MMAs, read D and fold it into the totals.  B tiles are built in shared
-// memory one block ahead, from window values fetched (cp.async) a block before
-// that.  A wait that gives up sets *p.status.
+// Pipeline per block q of 32 time steps: at its start the lanes build the
+// block's new ring values, wait (bounded) for the MMAs of block q - 1, add its
+// D into the totals, and build B of block q in shared memory from window
+// values fetched (cp.async) during block q - 1; then they write x (three
+// planes, two steps per 32-bit column, two MMA halves) into tensor memory, and
+// at the block end one thread issues the 24 MMAs of q (12 per sweep) and
+// commits them to an mbarrier.  A, B and D are single-buffered: 128 tensor
+// memory columns per block.  A wait that gives up sets *p.status.
 #include "ps_internal.cuh"
 #include "ps_epilogue.cuh"
 #include "ps_ff.cuh"
@@ -64,6 +66,7 @@ namespace ps {
 namespace {
 
 constexpr int kK = 16;            // time steps per MMA (BF16 K)
+constexpr int kBlk = 2 * kK;      // time steps per block: two MMA halves, one D, one barrier
 constexpr int kPlanes = 3;        // hi, mid, lo BF16 parts
 constexpr int kLead = 6;          // forward skew offset: tF = tau - kLead - 2i + 2w
 constexpr int kRamp = 68;         // extra time steps of a block beyond r0 (both sweeps)
@@ -79,17 +82,18 @@ constexpr uint32_t kIdesc = umma::idesc_bf16(128, kMmaCols);
 // (A part, B part)
 __device__ constexpr int kPass[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
 
-// tensor memory columns: D forward [0, 16), D backward [16, 32), then A[buf][sweep][plane], 8 columns each
-__device__ __forceinline__ uint32_t a_col(int buf, int sweep, int plane)
+// tensor memory columns: D forward [0, 16), D backward [16, 32), then A[half][sweep][plane], 8
+// columns each (a block's 32 steps: two MMA halves of 16, two steps per column)
+__device__ __forceinline__ uint32_t a_col(int half, int sweep, int plane)
 {
-    return 2u * kMmaCols + (uint32_t)(((buf * 2 + sweep) * kPlanes + plane) * (kK / 2));
+    return 2u * kMmaCols + (uint32_t)(((half * 2 + sweep) * kPlanes + plane) * (kK / 2));
 }
 
 struct __align__(128) Smem {
-    unsigned char B[2][2][kPlanes][kBPlane];  // [buffer][sweep][part]: K-major BF16, core matrices 8 x 16 B
+    unsigned char B[2][2][kPlanes][kBPlane];  // [half][sweep][part]: K-major BF16, core matrices 8 x 16 B
     float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
     int grew[3][4];                           // per warp of build_B: some column's scale grew (slot q % 3)
-    int2 stage[2][2][kMmaCols][kK];           // [q & 1][sweep][column][step]: block q's window values, fetched ahead
+    int2 stage[2][2][kMmaCols][kK];           // [half][sweep][column][step]: the next block's window values
     int ref[2][kMmaCols];                     // running exponent of B's scale per sweep and column
     uint64_t mbar;
     uint32_t tmem;
@@ -141,50 +145,56 @@ __device__ __forceinline__ bool b_window(const MmaParams& p, int s, int n, int t
     return par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0);
 }
 
-// Block q covers the time steps tb .. tb + 15.
-// Start the copies of block q's window values that this thread's part of build_B needs (4
-// steps of one sweep and column, 8 bytes each) into stage[q & 1]; a block ahead, so their
+// A block covers the time steps tb .. tb + 31 (two halves of 16).
+// Start the copies of a block's window values that this thread's part of build_B needs (4 steps
+// of each half, one sweep and column, 8 bytes each) into the stage, a block ahead, so their
 // latency is hidden behind a block of steps.
 template <bool F00>
-__device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
+__device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        int l3;
-        if (b_window<F00>(p, s, n, tb + 4 * qd + u, r0, c0, l3))
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(umma::smem_addr(&sm.stage[q & 1][s][n][4 * qd + u])),
-                         "l"(p.bf[n] + l3)
-                         : "memory");
-    }
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int l3;
+            if (b_window<F00>(p, s, n, tb + kK * h + 4 * qd + u, r0, c0, l3))
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
+                                 umma::smem_addr(&sm.stage[h][s][n][4 * qd + u])),
+                             "l"(p.bf[n] + l3)
+                             : "memory");
+        }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
-// B of block q into buffer q & 1 (all 128 threads: thread = sweep x column x 4 steps), from
-// the values this thread fetched.
+// B of block q (both halves; all 128 threads: thread = sweep x column x 4 steps of each half),
+// from the values this thread fetched.  One scale per block, sweep and column: the two halves'
+// MMAs add into one D.
 template <bool F00>
 __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    float m[4];
-    int e[4];
+    float m[8];
+    int e[8];
     int emax = kZeroExp;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int tau = tb + 4 * qd + u;
-        int l3;
-        m[u] = 0.0f;
-        e[u] = kZeroExp;
-        if (b_window<F00>(p, s, n, tau, r0, c0, l3)) {
-            const int2 v = sm.stage[q & 1][s][n][4 * qd + u];
-            m[u] = __int_as_float(v.x);
-            e[u] = v.y;
-        } else if (n == p.nslot && l3 >= 0 && l3 < p.wlen) {  // the normalisation column: 2 l3 + 1
-            m[u] = frexpf((float)(2 * l3 + 1), &e[u]);
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = 4 * h + u, tau = tb + kK * h + 4 * qd + u;
+            int l3;
+            m[i] = 0.0f;
+            e[i] = kZeroExp;
+            if (b_window<F00>(p, s, n, tau, r0, c0, l3)) {
+                const int2 v = sm.stage[h][s][n][4 * qd + u];
+                m[i] = __int_as_float(v.x);
+                e[i] = v.y;
+            } else if (n == p.nslot && l3 >= 0 && l3 < p.wlen) {  // the normalisation column: 2 l3 + 1
+                m[i] = frexpf((float)(2 * l3 + 1), &e[i]);
+            }
+            emax = max(emax, e[i]);
         }
-        emax = max(emax, e[u]);
-    }
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
     int rold = qd == 0 ? sm.ref[s][n] : 0;
@@ -197,16 +207,19 @@ __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int
     // warps 0, 1 build sweep 0 and warps 2, 3 sweep 1: the flush reads two flags, not 16 factors
     const unsigned grew = __ballot_sync(0xffffffffu, qd == 0 && rold != rnew);
     if (lane == 0) sm.grew[q % 3][tid >> 5] = grew != 0u;
-    float v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = m[u] * pow2f_or_zero(e[u] - rnew);
-    uint32_t w01[kPlanes], w23[kPlanes];
-    split3(v[0], v[1], w01);
-    split3(v[2], v[3], w23);
     const int off = b_off(n, 4 * qd);
 #pragma unroll
-    for (int pl = 0; pl < kPlanes; ++pl)
-        *reinterpret_cast<uint2*>(&sm.B[q & 1][s][pl][off]) = make_uint2(w01[pl], w23[pl]);
+    for (int h = 0; h < 2; ++h) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = m[4 * h + u] * pow2f_or_zero(e[4 * h + u] - rnew);
+        uint32_t w01[kPlanes], w23[kPlanes];
+        split3(v[0], v[1], w01);
+        split3(v[2], v[3], w23);
+#pragma unroll
+        for (int pl = 0; pl < kPlanes; ++pl)
+            *reinterpret_cast<uint2*>(&sm.B[h][s][pl][off]) = make_uint2(w01[pl], w23[pl]);
+    }
 }
 
 struct Sweep22 {
@@ -229,18 +242,18 @@ struct Sweep22 {
 // parity.  In the skewed frame t, v and u all have the parity of tau, lane i
 // reads entry (index / 2) of consecutive lanes' neighbours (no bank conflicts),
 // and the forward and backward sweeps share g (t of the backward sweep of lane
-// i is t of the forward sweep of lane 31 - i).  A 16-step block reads 78
-// consecutive values of each table (39 per parity); the next block needs 16 new
-// ones per table, built at the block boundary.
+// i is t of the forward sweep of lane 31 - i).  A 32-step block reads 94
+// consecutive values of each table (47 per parity); it needs 32 new ones per
+// table beyond the block before, built at its start (the ring holds 128).
 //
-// A block's 8 step pairs read 8 consecutive slots of each table (increasing for g
+// A block's 16 step pairs read 16 consecutive slots of each table (increasing for g
 // and f, decreasing for fb) from a start computed once per block.  So each table
 // keeps kGuard slots a second time past its end (g, f: slot s < kGuard also at
 // kRing + s) or before its start (fb: slot s at kGuard + s, and slot s >= kRing -
 // kGuard also at s - (kRing - kGuard)), and a run of kGuard slots from any start is
 // contiguous: no wrap-around arithmetic per step.
 constexpr int kRing = 64;
-constexpr int kGuard = 8;
+constexpr int kGuard = kBlk / 2;
 struct ffpair {
     ff rho, r;
 };
@@ -299,7 +312,7 @@ __device__ __forceinline__ void step22(Sweep22& S, ff rho, ff r, float dw)
 // Table indices of a lane's first step pair in a block (tau even, then odd): t, v = 2 l2 + t of
 // the forward step and t of the backward step are even at the even step, so both steps use the
 // same slot of each; u = 2 l2 - t of the backward step is even at the even step and one less at
-// the odd one.  Pair k of the block reads g and f at + k and fb at - k.
+// the odd one.  Pair k of the block (k < 16) reads g and f at + k and fb at - k.
 struct RingIdx {
     int g, f, gb, fb0, fb1;
 };
@@ -326,9 +339,9 @@ __device__ __forceinline__ void bwd_step(Sweep22& S, const CoefRing& R, int p, c
 // The (0 0 0) family vanishes where l1 + l2 + l3 is odd, so its sweeps step two points at a
 // time: f(j + 2) = -rho f(j) with rho the product of the odd-t entries of the (2 -2 0) step
 // (forward g[t] f[2 l2 + t], backward g[t] fb[2 l2 - t], t = 2n + 1 at step n), whose rho alone
-// is needed.  Each warp keeps them as rings of 64 odd values; a 16-step block reads 47
-// consecutive ones of each table, and the next block needs 16 more.
-constexpr int kGuard00 = 16;  // a block's 16 steps read 16 consecutive slots of each table
+// is needed.  Each warp keeps them as rings of 64 odd values; a 32-step block reads 63
+// consecutive ones of each table, 32 of them new, built at its start.
+constexpr int kGuard00 = kBlk;  // a block's 32 steps read 32 consecutive slots of each table
 struct __align__(16) Ring00 {
     ff g[kRing + kGuard00], f[kRing + kGuard00], fb[kGuard00 + kRing];  // slot (x >> 1) & 63 of odd x
 };
@@ -337,11 +350,11 @@ __device__ __forceinline__ ff rho_entry(ff X, ff Y)
 {
     return X.h > 0.0f ? ff_mul(X, ff_rsqrt(ff_mul_raw(X, Y))) : ff_make(0.0f);
 }
-// the odd values of block tb (its first time step): t in [tlo, tlo + 92], v in [vlo, vlo + 92],
-// u in [ulo, ulo + 92]
+// the odd values of the block starting at time step tb: t in [tlo, tlo + 124], v in
+// [vlo, vlo + 124], u in [ulo, ulo + 124]
 __device__ __forceinline__ int ring00_tlo(int tb, int w) { return 2 * tb + 2 * w - 67; }
 __device__ __forceinline__ int ring00_vlo(int tb, int w, int c0) { return 2 * c0 + 2 * w + 2 * tb - 5; }
-__device__ __forceinline__ int ring00_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 37 - 2 * tb; }
+__device__ __forceinline__ int ring00_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 5 - 2 * tb; }
 // One entry of g (isf false) or f (isf true) at odd x: P(x) = a0 b0, P(x + 1) = (a0 + 1)(b0 -+ 1)
 __device__ __forceinline__ void ring00_gf(Ring00& R, int x, bool isf, int l1)
 {
@@ -358,20 +371,19 @@ __device__ __forceinline__ void ring00_fb(Ring00& R, int u, int l1)
 __device__ __forceinline__ void build_rings00_first(Ring00& R, int tb, int w, int l1, int c0, int lane)
 {
     const int tlo = ring00_tlo(tb, w), vlo = ring00_vlo(tb, w, c0), ulo = ring00_ulo(tb, w, c0);
-    for (int e = lane; e < 47; e += 32) {
+    for (int e = lane; e < 63; e += 32) {
         ring00_gf(R, tlo + 2 * e, false, l1);
         ring00_gf(R, vlo + 2 * e, true, l1);
         ring00_fb(R, ulo + 2 * e, l1);
     }
 }
-// The 16 values per table that block tb needs beyond the block before: the top 16 of t and v
-// (lanes 0-15 and 16-31, no divergence), then the bottom 16 of u (lanes 0-15).
+// The 32 values per table that block tb needs beyond the block before: the top 32 of t and v,
+// the bottom 32 of u, one per lane in each of three passes.
 __device__ __forceinline__ void build_rings00_next(Ring00& R, int tb, int w, int l1, int c0, int lane)
 {
-    const int e = lane & 15;
-    const bool isf = lane >= 16;
-    ring00_gf(R, (isf ? ring00_vlo(tb, w, c0) : ring00_tlo(tb, w)) + 62 + 2 * e, isf, l1);
-    if (lane < 16) ring00_fb(R, ring00_ulo(tb, w, c0) + 2 * e, l1);
+    ring00_gf(R, ring00_tlo(tb, w) + 62 + 2 * lane, false, l1);
+    ring00_gf(R, ring00_vlo(tb, w, c0) + 62 + 2 * lane, true, l1);
+    ring00_fb(R, ring00_ulo(tb, w, c0) + 2 * lane, l1);
 }
 // Table indices of a lane's first step in a block: forward step n reads g at t = 2n + 1 (slot
 // n) and f at v = 2 l2 + t (slot l2 + n); backward step n reads g at t (slot n) and fb at
@@ -402,57 +414,55 @@ __device__ __forceinline__ ff rho00(ff X, ff Y)
 }
 
 // The ring values of the block starting at time step tb, for warp row l1 = r0 + 2w and lanes
-// l2 = c0 + 2i: t in [tlo, tlo + 77], v in [vlo, vlo + 77], u in [ulo, ulo + 77].
+// l2 = c0 + 2i: t in [tlo, tlo + 93], v in [vlo, vlo + 93], u in [ulo, ulo + 93].
 __device__ __forceinline__ int ring_tlo(int tb, int w) { return tb - 68 + 2 * w; }
 __device__ __forceinline__ int ring_vlo(int tb, int w, int c0) { return 2 * c0 + 2 * w + tb - 6; }
-__device__ __forceinline__ int ring_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 53 - tb; }
+__device__ __forceinline__ int ring_ulo(int tb, int w, int c0) { return 2 * c0 - 2 * w + 37 - tb; }
 
-// All 78 values of each table (the first block).
+// All 94 values of each table (the first block).
 __device__ __forceinline__ void build_rings_first(CoefRing& R, int tb, int w, int l1, int c0, int lane)
 {
     const int tlo = ring_tlo(tb, w), vlo = ring_vlo(tb, w, c0), ulo = ring_ulo(tb, w, c0);
-    for (int e = lane; e < 78; e += 32) {
+    for (int e = lane; e < 94; e += 32) {
         ring_g(R, tlo + e, l1);
         ring_f(R, vlo + e, l1);
         ring_fb(R, ulo + e, l1);
     }
 }
 
-// The 16 values per table that block q needs beyond block q - 1: the top 16 of t and v, the
-// bottom 16 of u.  With s(x) = 1/sqrt(P(x)) for the table's products P,
+// The 32 values per table that block tb needs beyond the block before: the top 32 of t and v,
+// the bottom 32 of u.  With s(x) = 1/sqrt(P(x)) for the table's products P,
 //   g, f entry x  = (sqrt(P(x) / P(x+1)), 1/sqrt(P(x+1))) = (P(x) s(x) s(x+1), s(x+1)),
 //   fb entry x    = (sqrt(P(x+1) / P(x)), 1/sqrt(P(x)))   = (P(x+1) s(x+1) s(x), s(x)),
 // so a new entry takes one float-float 1/sqrt; the neighbouring s comes from the next lane or,
-// at the edge of the 16, from the entry of block q - 1 that holds it as its r.  P(x) is 0 only
-// at the first step of a sweep, where the entry's rho is 0.  Pass 1: lanes 0-15 take g, lanes
-// 16-31 f (no divergence); pass 2: lanes 0-15 take fb.
+// at the edge of the 32, from the entry of the block before that holds it as its r.  P(x) is 0
+// only at the first step of a sweep, where the entry's rho is 0.  One pass per table, one
+// entry per lane.
+__device__ __forceinline__ void ring_gf_next(CoefRing& R, int x, bool isf, int l1, int lane)
+{
+    // g: P(x) = x (2 l1 + 1 - x), P(x + 1) = (x + 1)(2 l1 - x)
+    // f: P(x) = (x - 2 l1)(x + 1), P(x + 1) = (x + 1 - 2 l1)(x + 2)
+    const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
+    const ff s1 = ff_rsqrt(two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
+    ff s0{__shfl_up_sync(0xffffffffu, s1.h, 1), __shfl_up_sync(0xffffffffu, s1.l, 1)};
+    ffpair(*tab)[kRing + kGuard] = isf ? R.f : R.g;
+    if (lane == 0) s0 = tab[(x - 1) & 1][ring_slot(x - 1)].r;
+    const ff P0 = two_prod(a0, b0);
+    const ff rho = P0.h > 0.0f ? ff_mul(ff_mul_raw(P0, s0), s1) : ff_make(0.0f);
+    put_up<kGuard>(tab[x & 1], ring_slot(x), ffpair{rho, s1});
+}
 __device__ __forceinline__ void build_rings_next(CoefRing& R, int tb, int w, int l1, int c0, int lane)
 {
-    const int e = lane & 15;
-    {
-        const bool isf = lane >= 16;
-        const int x = isf ? ring_vlo(tb, w, c0) + 62 + e : ring_tlo(tb, w) + 62 + e;
-        // g: P(x) = x (2 l1 + 1 - x), P(x + 1) = (x + 1)(2 l1 - x)
-        // f: P(x) = (x - 2 l1)(x + 1), P(x + 1) = (x + 1 - 2 l1)(x + 2)
-        const float a0 = (float)(isf ? x - 2 * l1 : x), b0 = (float)(isf ? x + 1 : 2 * l1 + 1 - x);
-        const ff s1 = ff_rsqrt(two_prod(a0 + 1.0f, isf ? b0 + 1.0f : b0 - 1.0f));
-        ff s0{__shfl_up_sync(0xffffffffu, s1.h, 1, 16), __shfl_up_sync(0xffffffffu, s1.l, 1, 16)};
-        ffpair(*tab)[kRing + kGuard] = isf ? R.f : R.g;
-        if (e == 0) s0 = tab[(x - 1) & 1][ring_slot(x - 1)].r;
-        const ff P0 = two_prod(a0, b0);
-        const ff rho = P0.h > 0.0f ? ff_mul(ff_mul_raw(P0, s0), s1) : ff_make(0.0f);
-        put_up<kGuard>(tab[x & 1], ring_slot(x), ffpair{rho, s1});
-    }
-    if (lane < 16) {
-        const int x = ring_ulo(tb, w, c0) + e;  // Fb(x) = x (2 l1 + 1 + x)
-        const float a0 = (float)x, b0 = (float)(2 * l1 + 1 + x);
-        const ff s0 = ff_rsqrt(two_prod(a0, b0));
-        ff s1{__shfl_down_sync(0x0000ffffu, s0.h, 1, 16), __shfl_down_sync(0x0000ffffu, s0.l, 1, 16)};
-        if (e == 15) s1 = R.fb[(x + 1) & 1][kGuard + ring_slot(x + 1)].r;
-        const ff P1 = two_prod(a0 + 1.0f, b0 + 1.0f);
-        const ff rho = P1.h > 0.0f ? ff_mul(ff_mul_raw(P1, s1), s0) : ff_make(0.0f);
-        put_down<kGuard>(R.fb[x & 1], ring_slot(x), ffpair{rho, s0});
-    }
+    ring_gf_next(R, ring_tlo(tb, w) + 62 + lane, false, l1, lane);
+    ring_gf_next(R, ring_vlo(tb, w, c0) + 62 + lane, true, l1, lane);
+    const int x = ring_ulo(tb, w, c0) + lane;  // Fb(x) = x (2 l1 + 1 + x)
+    const float a0 = (float)x, b0 = (float)(2 * l1 + 1 + x);
+    const ff s0 = ff_rsqrt(two_prod(a0, b0));
+    ff s1{__shfl_down_sync(0xffffffffu, s0.h, 1), __shfl_down_sync(0xffffffffu, s0.l, 1)};
+    if (lane == 31) s1 = R.fb[(x + 1) & 1][kGuard + ring_slot(x + 1)].r;
+    const ff P1 = two_prod(a0 + 1.0f, b0 + 1.0f);
+    const ff rho = P1.h > 0.0f ? ff_mul(ff_mul_raw(P1, s1), s0) : ff_make(0.0f);
+    put_down<kGuard>(R.fb[x & 1], ring_slot(x), ffpair{rho, s0});
 }
 
 __device__ __forceinline__ float sq(const ff& f)
@@ -491,10 +501,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const bool runs = writes && (F00 || l1 >= 2);  // the (2 -2 0) family vanishes for l1 < 2
     const int T = runs ? l1 : 0;
     const int d = l2 - l1;
-    // block q covers the time steps q kK .. q kK + 15; the sweeps run for tau in [0, r0 + kRamp)
-    // ((2 -2 0)) or [0, floor((r0 + 1) / 2) + 34) ((0 0 0), two points per step)
+    // block q covers the time steps q kBlk .. q kBlk + 31; the sweeps run for tau in
+    // [0, r0 + kRamp) ((2 -2 0)) or [0, floor((r0 + 1) / 2) + 34) ((0 0 0), two points per step)
     const int ntau = F00 ? ((r0 + 1) >> 1) + 34 : r0 + kRamp;
-    const int nk = (ntau + kK - 1) / kK;  // 16-step blocks of the skewed sweeps (block-uniform)
+    const int nk = (ntau + kBlk - 1) / kBlk;  // 32-step blocks of the skewed sweeps (block-uniform)
     const int ncols = p.nslot + 1;
 
     if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
@@ -505,12 +515,9 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     umma::fence_after_sync();
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
-    fetch_B<F00>(p, sm, 0, 0, r0, c0, tid);
-    if (nk > 1) fetch_B<F00>(p, sm, 1, kK, r0, c0, tid);
-    build_B<F00>(p, sm, 0, 0, r0, c0, tid);
+    fetch_B<F00>(p, sm, 0, r0, c0, tid);
     if constexpr (F00) build_rings00_first(R, 0, warp, l1, c0, lane);
     else build_rings_first(R, 0, warp, l1, c0, lane);
-    __syncwarp();
 
     // sweep state: the (2 -2 0) family with its recurrence coefficient, or (f alone) the (0 0 0) family
     Sweep22 F, B;
@@ -567,12 +574,26 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     // From tau = 34 to floor((r0 + 1) / 2) + 1 every lane that runs is inside both sweeps.
     const int nx00 = (T + 1) / 2, ns00 = T / 2, steady00 = ((r0 + 1) >> 1) + 1;
     for (int q = 0; q < nk; ++q) {
-        const int buf = q & 1;
+        const int tb = q * kBlk;  // the block's first time step
+        // ---- block start: the A operand, B and D are single-buffered ----
+        if (q > 0) {
+            // the ring values of this block (no MMA reads them), then the MMAs of block q - 1
+            // (issued at its end): D into the totals; their A and B may be overwritten after
+            if constexpr (F00) build_rings00_next(R, tb, warp, l1, c0, lane);
+            else build_rings_next(R, tb, warp, l1, c0, lane);
+            flush(q - 1);
+        }
+        build_B<F00>(p, sm, q, tb, r0, c0, tid);
+        // the stage holds the next block's values from here on; each thread's copies go to the
+        // elements it has just read, after the warp's reads
+        __syncwarp();
+        if (q + 1 < nk) fetch_B<F00>(p, sm, tb + kBlk, r0, c0, tid);
+        __syncwarp();  // the ring values of the block, written by the warp's lanes
         // the ring indices of the block's first time step (first step pair)
         RingIdx00 ix00;
         RingIdx ix22;
-        if constexpr (F00) ix00 = ring00_idx(q * kK + fofs, q * kK + bofs, l2);
-        else ix22 = ring_idx(q * kK + fofs, q * kK + bofs, l2);
+        if constexpr (F00) ix00 = ring00_idx(tb + fofs, tb + bofs, l2);
+        else ix22 = ring_idx(tb + fofs, tb + bofs, l2);
         // One step pair of the block: the steps of both sweeps, then x into tensor memory.  In a
         // block whose steps all lie in the steady state, every lane that runs is inside both
         // sweeps, so both steps run unconditionally (their dependency chains interleave).  Lanes
@@ -581,7 +602,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         // The other blocks (the first few and the last) check every step.
         auto pair = [&](int s2, bool steady) {
             float xf[2], xb[2];
-            const int tau0 = q * kK + s2;
+            const int tau0 = tb + s2;
             if constexpr (F00) {
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
@@ -608,7 +629,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 const int k = s2 >> 1;  // the step pair of the block
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {  // e: the step parity (tau even, then odd)
-                    const int tf = tau0 + e + fofs, tb = tau0 + e + bofs;
+                    const int tf = tau0 + e + fofs, tbk = tau0 + e + bofs;
                     if (steady) {
                         xf[e] = sq(F.f);
                         xb[e] = sq(B.f);
@@ -621,7 +642,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                             xf[e] = sq(F.f);
                             fwd_step(F, R, e, ix22, k);
                         }
-                        if (tb >= 0 && tb < T) {
+                        if (tbk >= 0 && tbk < T) {
                             xb[e] = sq(B.f);
                             bwd_step(B, R, e, ix22, k);
                         }
@@ -632,46 +653,43 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             split3(xf[0], xf[1], wf);
             split3(xb[0], xb[1], wb);
             __syncwarp();  // the stores below are warp-collective (.sync.aligned)
+            const int h = s2 / kK, col = (s2 % kK) >> 1;  // MMA half, tensor-memory column in it
 #pragma unroll
             for (int pl = 0; pl < kPlanes; ++pl) {
-                umma::st_x1(tlane + a_col(buf, 0, pl) + (uint32_t)(s2 >> 1), wf[pl]);
-                umma::st_x1(tlane + a_col(buf, 1, pl) + (uint32_t)(s2 >> 1), wb[pl]);
+                umma::st_x1(tlane + a_col(h, 0, pl) + (uint32_t)col, wf[pl]);
+                umma::st_x1(tlane + a_col(h, 1, pl) + (uint32_t)col, wb[pl]);
             }
         };
-        const int t0 = q * kK, t1 = q * kK + kK - 1;  // the block's first and last time step
-        const bool steady = F00 ? (t0 >= 34 && t1 <= steady00) : (t0 >= kSteady && t1 <= r0 + kLead - 1);
+        const int t1 = tb + kBlk - 1;  // the block's last time step
+        const bool steady = F00 ? (tb >= 34 && t1 <= steady00) : (tb >= kSteady && t1 <= r0 + kLead - 1);
         if (steady) {
 #pragma unroll 2
-            for (int s2 = 0; s2 < kK; s2 += 2) pair(s2, true);
+            for (int s2 = 0; s2 < kBlk; s2 += 2) pair(s2, true);
         } else {
 #pragma unroll 1
-            for (int s2 = 0; s2 < kK; s2 += 2) pair(s2, false);
+            for (int s2 = 0; s2 < kBlk; s2 += 2) pair(s2, false);
         }
-        // ---- block boundary ----
-        if (q > 0) flush(q - 1);  // MMAs of block q - 1: done; their A buffer and B buffer are free
-        if (q + 1 < nk) {
-            build_B<F00>(p, sm, q + 1, (q + 1) * kK, r0, c0, tid);
-            if constexpr (F00) build_rings00_next(R, (q + 1) * kK, warp, l1, c0, lane);
-            else build_rings_next(R, (q + 1) * kK, warp, l1, c0, lane);
-        }
+        // ---- block end: A and B complete, one thread issues the block's 24 MMAs ----
         umma::wait_st();
         umma::fence_smem_async();
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
         if (tid == 0) {
+            // per sweep: the five small products of both halves first, hi x hi of both last; the
+            // first MMA starts D from zero
 #pragma unroll
             for (int s = 0; s < 2; ++s)
 #pragma unroll
-                for (int ps = 0; ps < 6; ++ps) {
-                    const uint64_t bd = umma::smem_desc(umma::smem_addr(&sm.B[buf][s][kPass[ps][1]][0]), 128u, 256u);
-                    umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(buf, s, kPass[ps][0]), bd, kIdesc,
-                                      ps > 0);
-                }
+                for (int ps = 0; ps < 6; ++ps)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const uint64_t bd = umma::smem_desc(umma::smem_addr(&sm.B[h][s][kPass[ps][1]][0]), 128u, 256u);
+                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(h, s, kPass[ps][0]), bd,
+                                          kIdesc, ps > 0 || h > 0);
+                    }
             umma::mma_commit(&sm.mbar);
         }
-        // stage[q & 1] was last read by build_B(q), before the barrier above
-        if (q + 2 < nk) fetch_B<F00>(p, sm, q + 2, (q + 2) * kK, r0, c0, tid);
     }
     flush(nk - 1);
     if (!ok) atomicExch(p.status, 1u);
