@@ -91,6 +91,7 @@ __device__ __forceinline__ uint32_t a_col(int half, int sweep, int plane)
 
 struct __align__(128) Smem {
     unsigned char B[2][2][kPlanes][kBPlane];  // [half][sweep][part]: K-major BF16, core matrices 8 x 16 B
+    unsigned char Bsh[2][kBPlane];            // [sweep]: the hi part of half 1 with column n at (n + 8) mod 16
     float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
     int grew[3][4];                           // per warp of build_B: some column's scale grew (slot q % 3)
     int2 stage[2][2][kMmaCols][kK];           // [half][sweep][column][step]: the next block's window values
@@ -169,8 +170,10 @@ __device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int tb, in
 
 // B of block q (both halves; all 128 threads: thread = sweep x column x 4 steps of each half),
 // from the values this thread fetched.  One scale per block, sweep and column: the two halves'
-// MMAs add into one D.
-template <bool F00>
+// MMAs add into one D.  With at most 8 columns in use (SHIFT), the hi part of half 1 is also
+// written with its columns moved up by 8 (the zero columns 8-15 moving down to 0-7), so that
+// its hi x hi product lands in D's spare columns 8-15.
+template <bool F00, bool SHIFT>
 __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
 {
     const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
@@ -219,6 +222,8 @@ __device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int
 #pragma unroll
         for (int pl = 0; pl < kPlanes; ++pl)
             *reinterpret_cast<uint2*>(&sm.B[h][s][pl][off]) = make_uint2(w01[pl], w23[pl]);
+        if (SHIFT && h == 1)
+            *reinterpret_cast<uint2*>(&sm.Bsh[s][b_off((n + 8) & (kMmaCols - 1), 4 * qd)]) = make_uint2(w01[0], w23[0]);
     }
 }
 
@@ -506,6 +511,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int ntau = F00 ? ((r0 + 1) >> 1) + 34 : r0 + kRamp;
     const int nk = (ntau + kBlk - 1) / kBlk;  // 32-step blocks of the skewed sweeps (block-uniform)
     const int ncols = p.nslot + 1;
+    // With at most 8 columns (NC == 8) D's columns 8-15 are spare: the hi x hi product of the
+    // block's second half goes there on its own (its B columns moved up by 8), and the fold adds
+    // the two column halves.  Each hi x hi product then takes its rounding toward zero at the
+    // scale of its own 16 steps, as with one D per 16 steps.
+    constexpr bool kShift = NC == 8;
 
     if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
     if (tid < 2 * kMmaCols) sm.ref[tid / kMmaCols][tid % kMmaCols] = kZeroExp;
@@ -553,6 +563,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                     }
                 }
             }
+            if (kShift) {
+#pragma unroll
+                for (int n = 0; n < NC; ++n) dv[n] = __fadd_rn(dv[n], dv[n + 8]);
+            }
 #pragma unroll
             for (int n = 0; n < NC; ++n)
                 if (n < ncols) tot[s][n].l = __fadd_rn(tot[s][n].l, dv[n]);
@@ -583,7 +597,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             else build_rings_next(R, tb, warp, l1, c0, lane);
             flush(q - 1);
         }
-        build_B<F00>(p, sm, q, tb, r0, c0, tid);
+        build_B<F00, kShift>(p, sm, q, tb, r0, c0, tid);
         // the stage holds the next block's values from here on; each thread's copies go to the
         // elements it has just read, after the warp's reads
         __syncwarp();
@@ -684,7 +698,8 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                 for (int ps = 0; ps < 6; ++ps)
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const uint64_t bd = umma::smem_desc(umma::smem_addr(&sm.B[h][s][kPass[ps][1]][0]), 128u, 256u);
+                        const unsigned char* bt = kShift && ps == 5 && h == 1 ? &sm.Bsh[s][0] : &sm.B[h][s][kPass[ps][1]][0];
+                        const uint64_t bd = umma::smem_desc(umma::smem_addr(bt), 128u, 256u);
                         umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(h, s, kPass[ps][0]), bd,
                                           kIdesc, ps > 0 || h > 0);
                     }
