@@ -127,8 +127,8 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * loop_cov*! call.  Here, in chosen mode, the Xi of all the blocks' windows
  * are computed grouped across the blocks by family product and parity, so
  * one family generation serves each group: the squared (0 0 0) windows by the
- * tensor-core kernel when there are 5 or more (up to 15 per launch), the
- * squared (2 -2 0) ones by the tensor-core kernel when there are more than 8,
+ * tensor-core kernel when there are 4 or more (up to 15 per launch), the
+ * squared (2 -2 0) ones by the tensor-core kernel when there are 5 or more,
  * the others by the CUDA-core kernel in groups of up to 8.  Each block is then
  * formed from its windows' Xi by the same per-element formula as the fused
  * kernel.  Plain FP64, or ps_set_tensor_cores(ctx, 0), runs the fused kernel
@@ -148,9 +148,9 @@ int ps_coupledcov_set_device(ps_ctx *ctx, int nblk, const int *kinds, const doub
  * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
-/* In chosen mode, the TT slots of a set when there are 5 or more of them,
- * and its ++ and -- slots when there are more than 8 of those (more than one
- * CUDA-core group holds), are computed by the tensor-core kernels: one
+/* In chosen mode, the TT slots of a set when there are 4 or more of them,
+ * and its ++ and -- slots when there are 5 or more of those, are computed by
+ * the tensor-core kernels: one
  * generation of the (0 0 0) or (2 -2 0) family for up to 15 windows,
  * contracted by BF16 tcgen05 MMAs in a three-part split with FP32
  * accumulators and float-float totals (same 1e-6 bar).  Their waits on
@@ -243,8 +243,8 @@ typedef struct ps_problem {
  * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
  * ps_batch_autotune() found, else defaults.  blocks_per_sm = -1 selects the
  * launch form instead: one chosen-kernel launch per window group.
- * A problem's TT slots when there are 5 or more, and its ++/-- slots when
- * there are more than 8, go to tensor-core launches instead, as in
+ * A problem's TT slots when there are 4 or more, and its ++/-- slots when
+ * there are 5 or more, go to tensor-core launches instead, as in
  * ps_mcm_set_device (unless ps_set_tensor_cores(ctx, 0)).
  * run() enqueues the window preparation, the tensor-core launches, then the
  * queue reset and ONE persistent kernel (or the per-group launches).  graph_launch() captures run()

@@ -446,17 +446,14 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 struct Slot {
     int k, s;
 };
-// Fewest slots of one kind for which a chosen-mode set takes a tensor-core kernel.
-// ++ and --: more than one CUDA-core group holds (ps::kMaxWin), so that one family generation
-// replaces two or more; on the lmax 8191 set 13 such slots take 487 ms in one tensor-core launch
-// against 944 ms in two CUDA-core groups, while up to 8 of them fit one CUDA-core group, which is
-// as fast or faster (at lmax 4095: 62 ms for 8 slots and 36 ms for 2, against 63-65 ms).
-// TT: the tensor-core kernel steps the (0 0 0) family two points at a time and costs about the
-// same for 1 to 15 windows (24 ms at lmax 4095), against 10.5, 16.7 and 19.4 ms for 1, 2 and 4
-// slots in the 4-slot CUDA-core kernel and 33-35 ms for 7-8 slots in the 8-slot one; at lmax 8191
-// 7 TT slots take 180 ms against 257 ms.  So TT sets of 5 or more slots take it.
-constexpr int kMmaMin22 = ps::kMaxWin + 1;
-constexpr int kMmaMin00 = 5;
+// Fewest slots of one kind for which a chosen-mode set takes a tensor-core kernel.  The
+// tensor-core kernels cost about the same for 1 to 15 windows (lmax 4095: 53 ms for ++/--, 18 ms
+// for TT); the CUDA-core groups grow with the slots: ++/-- 36, 42, 59 and 62 ms for 2, 4, 6 and 8
+// slots (up to 4 in the 4-slot kernel, then the 8-slot one, then two groups), TT 10.5, 16.7,
+// 18.0, 19.4 and 29.8 ms for 1 to 5.  On the lmax 8191 set 13 ++/-- slots take 405 ms on the
+// tensor cores against 944 ms in two CUDA-core groups, and 7 TT slots 132 ms against 257 ms.
+constexpr int kMmaMin22 = 5;
+constexpr int kMmaMin00 = 4;
 template <typename Used>
 static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {

@@ -1,6 +1,6 @@
 """The tensor-core coupling kernels (k_coupling_mma): the TT slots of a
-chosen-mode set when there are 5 or more, and its ++ / -- slots when there are
-more than 8; one (0 0 0) or (2 -2 0) family generation for up to 15 windows
+chosen-mode set when there are 4 or more, and its ++ / -- slots when there are
+5 or more; one (0 0 0) or (2 -2 0) family generation for up to 15 windows
 (the (0 0 0) sweeps two points per time step), the window contraction as BF16
 tcgen05 MMAs (three-part split, fresh FP32 accumulator per 16 steps,
 float-float totals).
@@ -121,7 +121,7 @@ def test_mma_matches_plain_fp64_full_size(ctx):
 
 def test_mma_agrees_with_cuda_core_path(ctx):
     """The same set with the tensor-core kernels switched off: both within 2e-6 of each other,
-    and the routing itself: the 10 ++/-- slots (more than 8) and the 5 TT slots take the
+    and the routing itself: the 10 ++/-- slots (5 or more) and the 5 TT slots take the
     tensor-core kernels, so their results differ from the CUDA-core kernels' in the last bits."""
     L = 700
     Ws = [_W(2 * L + 1, seed=80 + k, fsky=0.5 + 0.05 * k) for k in range(5)]
@@ -133,10 +133,10 @@ def test_mma_agrees_with_cuda_core_path(ctx):
         assert not np.array_equal(a[sl], b[sl]), sl
 
 
-@pytest.mark.parametrize("K,routed", [(4, False), (5, True)])
+@pytest.mark.parametrize("K,routed", [(3, False), (4, True)])
 def test_mma_tt_routing_threshold(ctx, K, routed):
-    """TT sets: 4 slots stay on the CUDA cores (the same bits with the tensor cores switched off),
-    5 take the tensor-core kernel (odd lmin and lmax, lmin > 0)."""
+    """TT sets: 3 slots stay on the CUDA cores (the same bits with the tensor cores switched off),
+    4 take the tensor-core kernel (odd lmin and lmax, lmin > 0)."""
     L = 333
     Ws = [_W(2 * L + 1, seed=120 + k, fsky=0.45 + 0.05 * k) for k in range(K)]
     slots = [(k, 0) for k in range(K)]
