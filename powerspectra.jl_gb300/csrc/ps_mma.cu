@@ -764,15 +764,32 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         for (int k = 0; k < NC - 1; ++k)
             if (k < p.nslot) Xi[k] = fma(lam2, BW[k], FW[k]) * inv;
     }
+    // Outputs (column-major, element (row, col) at row + col ldo).  M[l2, l1], the column l1 of
+    // the warp's row, is written directly: its lanes' rows step by 2, 16 bytes apart.  M[l1, l2]
+    // would put each lane in a different column; it goes through shared memory instead (the
+    // rings' space: every warp has passed its last step), and each warp writes 8 columns with the
+    // block's 4 rows of each in one store instruction, 4 words within 64 bytes of a column.
+    const bool mcm = p.epilogue == EPI_MCM;
+    double* so = reinterpret_cast<double*>(dyn);  // [slot][w][i]
     if (writes) {
         const long long ra = l1 - p.lmin, rb = l2 - p.lmin;
-        const bool mcm = p.epilogue == EPI_MCM;
 #pragma unroll
         for (int k = 0; k < kMmaMaxSlots; ++k) {
             if (k < p.nslot) {
-                p.out[k][ra + rb * p.ldo] = mcm ? (2.0 * l2 + 1.0) * Xi[k] : Xi[k];
+                so[(k * 4 + warp) * 32 + lane] = mcm ? (2.0 * l2 + 1.0) * Xi[k] : Xi[k];
                 p.out[k][rb + ra * p.ldo] = mcm ? (2.0 * l1 + 1.0) * Xi[k] : Xi[k];
             }
+        }
+    }
+    __syncthreads();
+    {
+        const int v = lane & 3, i = 8 * warp + (lane >> 2);  // row r0 + 2v, column c0 + 2i
+        const int l1v = r0 + 2 * v, l2i = c0 + 2 * i;
+        if (l1v >= p.lmin && l1v <= p.lmax && l2i >= l1v && l2i <= p.lmax) {
+            const long long off = (l1v - p.lmin) + (long long)(l2i - p.lmin) * p.ldo;
+#pragma unroll
+            for (int k = 0; k < kMmaMaxSlots; ++k)
+                if (k < p.nslot) p.out[k][off] = so[(k * 4 + v) * 32 + i];
         }
     }
     umma::fence_before_sync();
@@ -787,6 +804,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 constexpr int kBlockSmem = 48 * 1024;
 constexpr int kOccupancySmem = kBlockSmem - (int)sizeof(Smem);
 static_assert(4 * sizeof(CoefRing) <= kOccupancySmem, "the rings fit the block's dynamic shared memory");
+static_assert(kMmaMaxSlots * 128 * sizeof(double) <= kOccupancySmem, "the staged row halves fit the dynamic shared memory");
 static_assert(5 * (kBlockSmem + 1024) > 228 * 1024 && 4 * (kBlockSmem + 1024) <= 228 * 1024,
               "four blocks per SM (1 KB reserved per block)");
 
