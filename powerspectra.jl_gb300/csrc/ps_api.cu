@@ -623,6 +623,17 @@ uint64_t ps_launch_count(const ps_ctx* c) { return c ? (uint64_t)c->launches : 0
 // The device address of a page-locked host buffer that is mapped into the
 // device's address space (cudaHostAlloc / cudaHostRegister memory under unified
 // addressing), or nullptr for ordinary pageable memory.
+// Whether p (a host or device address) lies in host memory.
+static bool host_resident(const void* p)
+{
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 static double* mapped_host(double* h)
 {
     cudaPointerAttributes a;
@@ -1046,6 +1057,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                     mp.wW[i] = descs[q.k].wW;
                     mp.parity[i] = q.s == PS_SPIN_00 ? ps::PAR_ALL : (q.s == PS_SPIN_PP ? ps::PAR_EVEN : ps::PAR_ODD);
                     mp.out[i] = dM[4 * q.k + q.s];
+                    mp.stage_rows |= host_resident(mp.out[i]);
                 }
                 mp.ldo = ldm;
                 mp.wlen = wlen;
@@ -1209,6 +1221,7 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
                         mp.wW[q] = descs[sl.k].wW;
                         mp.parity[q] = sl.s == PS_SPIN_00 ? ps::PAR_ALL : (sl.s == PS_SPIN_PP ? ps::PAR_EVEN : ps::PAR_ODD);
                         mp.out[q] = P.M[4 * sl.k + sl.s];
+                        mp.stage_rows |= host_resident(mp.out[q]);
                     }
                     mp.ldo = P.ldm;
                     mp.wlen = wlen;

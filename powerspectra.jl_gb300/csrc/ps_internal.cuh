@@ -128,6 +128,7 @@ struct MmaParams {
     long long ldo;
     int wlen;
     int epilogue;                       // EPI_MCM or EPI_XI
+    int stage_rows;                     // 1: outputs in host memory, their scattered half staged
     const int2* tiles;                  // (r0, c0): rows r0 + 2w, columns c0 + 2i
     int ntiles;
     unsigned* status;                   // set to 1 when a bounded wait gives up

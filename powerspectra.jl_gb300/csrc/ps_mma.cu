@@ -491,8 +491,9 @@ __device__ __forceinline__ void renorm(ff (&t)[NC], int ncols)
 template <bool F00>
 using RingT = typename std::conditional<F00, Ring00, CoefRing>::type;
 
-// NC: columns folded into the totals (8 or 16; at least nslot + 1)
-template <bool F00, int NC>
+// NC: columns folded into the totals (8 or 16; at least nslot + 1).  STAGE: the outputs are
+// in host memory (MmaParams::stage_rows).
+template <bool F00, int NC, bool STAGE>
 __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 {
     __shared__ Smem sm;
@@ -766,9 +767,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     }
     // Outputs (column-major, element (row, col) at row + col ldo).  M[l2, l1], the column l1 of
     // the warp's row, is written directly: its lanes' rows step by 2, 16 bytes apart.  M[l1, l2]
-    // would put each lane in a different column; it goes through shared memory instead (the
-    // rings' space: every warp has passed its last step), and each warp writes 8 columns with the
-    // block's 4 rows of each in one store instruction, 4 words within 64 bytes of a column.
+    // puts each lane in a different column: written directly to device memory (L2 merges the
+    // words), but for outputs in host memory, where each such store crosses NVLink-C2C on its
+    // own, it goes through shared memory (the rings' space: every warp has passed its last step)
+    // and each warp writes 8 columns with the block's 4 rows of each in one store instruction,
+    // 4 words within 64 bytes of a column.
     const bool mcm = p.epilogue == EPI_MCM;
     double* so = reinterpret_cast<double*>(dyn);  // [slot][w][i]
     if (writes) {
@@ -776,13 +779,15 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll
         for (int k = 0; k < kMmaMaxSlots; ++k) {
             if (k < p.nslot) {
-                so[(k * 4 + warp) * 32 + lane] = mcm ? (2.0 * l2 + 1.0) * Xi[k] : Xi[k];
+                const double row = mcm ? (2.0 * l2 + 1.0) * Xi[k] : Xi[k];
+                if (STAGE) so[(k * 4 + warp) * 32 + lane] = row;
+                else p.out[k][ra + rb * p.ldo] = row;
                 p.out[k][rb + ra * p.ldo] = mcm ? (2.0 * l1 + 1.0) * Xi[k] : Xi[k];
             }
         }
     }
-    __syncthreads();
-    {
+    if (STAGE) {
+        __syncthreads();
         const int v = lane & 3, i = 8 * warp + (lane >> 2);  // row r0 + 2v, column c0 + 2i
         const int l1v = r0 + 2 * v, l2i = c0 + 2 * i;
         if (l1v >= p.lmin && l1v <= p.lmax && l2i >= l1v && l2i <= p.lmax) {
@@ -834,12 +839,14 @@ cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s)
     if (p.ntiles <= 0) return cudaSuccess;
     static_assert(sizeof(Smem) + kOccupancySmem <= 48 * 1024, "within the default shared memory limit");
     const unsigned grid = (unsigned)p.ntiles;
-    if (p.nslot + 1 <= 8) {
-        if (fam00) k_coupling_mma<true, 8><<<grid, 128, kOccupancySmem, s>>>(p);
-        else k_coupling_mma<false, 8><<<grid, 128, kOccupancySmem, s>>>(p);
+    auto go = [&](auto kernel) { kernel<<<grid, 128, kOccupancySmem, s>>>(p); };
+    const bool nc8 = p.nslot + 1 <= 8, stage = p.stage_rows != 0;
+    if (fam00) {
+        if (nc8) stage ? go(k_coupling_mma<true, 8, true>) : go(k_coupling_mma<true, 8, false>);
+        else stage ? go(k_coupling_mma<true, 16, true>) : go(k_coupling_mma<true, 16, false>);
     } else {
-        if (fam00) k_coupling_mma<true, 16><<<grid, 128, kOccupancySmem, s>>>(p);
-        else k_coupling_mma<false, 16><<<grid, 128, kOccupancySmem, s>>>(p);
+        if (nc8) stage ? go(k_coupling_mma<false, 8, true>) : go(k_coupling_mma<false, 8, false>);
+        else stage ? go(k_coupling_mma<false, 16, true>) : go(k_coupling_mma<false, 16, false>);
     }
     return cudaGetLastError();
 }
