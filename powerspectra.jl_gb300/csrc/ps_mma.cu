@@ -36,13 +36,14 @@
 // 24 bits) and D is formed from six products (all but the three smallest),
 // ordered so that the hi x hi products are added last: the tensor core rounds
 // its FP32 accumulation toward zero, so each block's D starts from zero and
-// takes one such rounding at full scale per 16 steps (the hi x hi of each of
-// its two MMA halves).  Each D is added to float-float totals on the CUDA
-// cores (into the low word; renormalised every fourth block).  B is scaled per
-// block by a running power of two (block floating point; windows span 1e-45),
-// the same role the slice exponents play in the chosen kernel.  The last
-// forward point, the match of the two sweeps, the normalisation and the
-// outputs are FP64.
+// takes such a rounding at full scale only for the hi x hi of each of its two
+// MMA halves: the second onto the first (at twice the scale) or, with at most
+// 8 columns, in D's spare columns on its own.  Each D is added to float-float
+// totals on the CUDA cores (into the low word; renormalised every fourth
+// block).  B is scaled per block by a running power of two (block floating
+// point; windows span 1e-45), the same role the slice exponents play in the
+// chosen kernel.  The last forward point, the match of the two sweeps, the
+// normalisation and the outputs are FP64.
 //
 // Pipeline per block q of 32 time steps: at its start the lanes build the
 // block's new ring values, wait (bounded) for the MMAs of block q - 1, add its
