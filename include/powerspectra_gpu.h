@@ -126,10 +126,10 @@ int ps_coupledcov_device(ps_ctx *ctx, int kind, const double *const *dS, const d
  * dR[b], dW[b], ..., dC[b]).  The reference computes one block per
  * loop_cov*! call.  Here, in chosen mode, the Xi of all the blocks' windows
  * are computed grouped across the blocks by family product and parity, so
- * one family generation serves each group: the squared (0 0 0) windows by the
- * tensor-core kernel when there are 4 or more (up to 15 per launch), the
- * squared (2 -2 0) ones by the tensor-core kernel when there are 5 or more,
- * the others by the CUDA-core kernel in groups of up to 8.  Each block is then
+ * one family generation serves each group: the squared (0 0 0) and squared
+ * (2 -2 0) windows by the tensor-core kernels when there are enough of them
+ * (the thresholds of ps_mcm_set_device; up to 15 per launch), the others by
+ * the CUDA-core kernel in groups of up to 8.  Each block is then
  * formed from its windows' Xi by the same per-element formula as the fused
  * kernel.  Plain FP64, or ps_set_tensor_cores(ctx, 0), runs the fused kernel
  * block by block.  Scratch: one n x n FP64 matrix per window (n = lmax - lmin
@@ -148,9 +148,10 @@ int ps_coupledcov_set_device(ps_ctx *ctx, int nblk, const int *kinds, const doub
  * Device pointers; enqueued on the context stream. */
 int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int K, int64_t nW, int lmin, int lmax,
                       int mode, double *const *dM, int64_t ldm);
-/* In chosen mode, the TT slots of a set when there are 4 or more of them,
- * and its ++ and -- slots when there are 5 or more of those, are computed by
- * the tensor-core kernels: one
+/* In chosen mode, the TT slots of a set and its ++ and -- slots, each kind
+ * when it has enough slots (TT: 4 or more at lmax >= 3072, 5 or more at
+ * lmax >= 768, else 9; ++/--: 5 or more at lmax >= 1536, else 9), are
+ * computed by the tensor-core kernels: one
  * generation of the (0 0 0) or (2 -2 0) family for up to 15 windows,
  * contracted by BF16 tcgen05 MMAs in a three-part split with FP32
  * accumulators and float-float totals (same 1e-6 bar).  Their waits on
@@ -243,9 +244,9 @@ typedef struct ps_problem {
  * uploads the tables; 0 for group_slots or blocks_per_sm picks the values
  * ps_batch_autotune() found, else defaults.  blocks_per_sm = -1 selects the
  * launch form instead: one chosen-kernel launch per window group.
- * A problem's TT slots when there are 4 or more, and its ++/-- slots when
- * there are 5 or more, go to tensor-core launches instead, as in
- * ps_mcm_set_device (unless ps_set_tensor_cores(ctx, 0)).
+ * A problem's TT slots and its ++/-- slots, when there are enough of them
+ * for its lmax, go to tensor-core launches instead, as in ps_mcm_set_device
+ * (unless ps_set_tensor_cores(ctx, 0)).
  * run() enqueues the window preparation, the tensor-core launches, then the
  * queue reset and ONE persistent kernel (or the per-group launches).  graph_launch() captures run()
  * into a CUDA graph on first use and replays it afterwards.  The problems'

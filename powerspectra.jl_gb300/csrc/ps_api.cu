@@ -84,8 +84,8 @@ struct ps_ctx {
         bool launches = false;
         std::vector<ps::CouplingParams> host_groups;
         int2* d_tasks = nullptr;
-        // tensor-core launches (the problems' TT slots when there are kMmaMin00 or more, their
-        // ++/-- slots when there are kMmaMin22 or more), enqueued before the CUDA-core part,
+        // tensor-core launches (the problems' TT slots and ++/-- slots when there are
+        // mma_min_slots of them), enqueued before the CUDA-core part,
         // with the block lists of every distinct (lmin, lmax) in d_mtiles
         std::vector<ps::MmaParams> host_mma;
         std::vector<char> host_mma00;
@@ -446,14 +446,25 @@ static int dev_upload(ps_ctx* c, T** dst, const std::vector<T>& v)
 struct Slot {
     int k, s;
 };
-// Fewest slots of one kind for which a chosen-mode set takes a tensor-core kernel.  The
-// tensor-core kernels cost about the same for 1 to 15 windows (lmax 4095: 53 ms for ++/--, 18 ms
-// for TT); the CUDA-core groups grow with the slots: ++/-- 36, 42, 59 and 62 ms for 2, 4, 6 and 8
-// slots (up to 4 in the 4-slot kernel, then the 8-slot one, then two groups), TT 10.5, 16.7,
-// 18.0, 19.4 and 29.8 ms for 1 to 5.  On the lmax 8191 set 13 ++/-- slots take 405 ms on the
-// tensor cores against 944 ms in two CUDA-core groups, and 7 TT slots 132 ms against 257 ms.
-constexpr int kMmaMin22 = 5;
-constexpr int kMmaMin00 = 4;
+// Fewest slots of one kind for which a chosen-mode set takes a tensor-core kernel, by lmax.
+// The tensor-core kernels cost about the same for 1 to 15 windows; the CUDA-core groups grow
+// with the slots, and win for small grids, where the tensor-core kernel's ramps and block
+// boundaries weigh more.  Measured (ms, tensor-core against CUDA-core):
+//   ++/--  lmax  511:  8 slots 0.24 / 0.17, 12 slots 0.26 / 0.31
+//          lmax 1023:  8 slots 1.18 / 1.12, 12 slots 1.22 / 1.84
+//          lmax 2047:  4 slots 7.4 / 5.4,   6 slots 7.4 / 7.7
+//          lmax 4095:  4 slots 53 / 42,     6 slots 53 / 59
+//   TT     lmax  511:  8 slots 0.138 / 0.127
+//          lmax 1023:  4 slots 0.47 / 0.38, 6 slots 0.49 / 0.67
+//          lmax 2047:  4 slots 2.69 / 2.54, 6 slots 2.75 / 4.21
+//          lmax 4095:  3 slots 18.1 / 18.0, 4 slots 18.2 / 19.4
+// On the lmax 8191 set 13 ++/-- slots take 405 ms on the tensor cores against 944 ms in two
+// CUDA-core groups, and 7 TT slots 132 ms against 257 ms.
+static int mma_min_slots(bool fam00, int lmax)
+{
+    if (fam00) return lmax >= 3072 ? 4 : (lmax >= 768 ? 5 : ps::kMaxWin + 1);
+    return lmax >= 1536 ? 5 : ps::kMaxWin + 1;
+}
 template <typename Used>
 static std::vector<std::vector<Slot>> group_slots(unsigned cases, int K, int gs, Used used)
 {
@@ -878,9 +889,9 @@ int ps_coupledcov_set_device(ps_ctx* c, int nblk, const int* kinds, const double
     }
     // Chosen mode with the tensor cores: the Xi of every window of every block, grouped across
     // the blocks by family product and parity, so that one family generation serves each group:
-    // the squared (0 0 0) windows by the (0 0 0) tensor-core kernel when there are kMmaMin00 or
-    // more, the squared (2 -2 0) ones by the (2 -2 0) tensor-core kernel when there are kMmaMin22
-    // or more, and the others by the CUDA-core kernel in groups of up to kMaxWin.  Then each block
+    // the squared (0 0 0) windows by the (0 0 0) tensor-core kernel and the squared (2 -2 0) ones
+    // by the (2 -2 0) tensor-core kernel when there are mma_min_slots of them or more, and the
+    // others by the CUDA-core kernel in groups of up to kMaxWin.  Then each block
     // is formed from its windows' Xi.
     struct XWin {
         int b, k, prod, par;
@@ -912,8 +923,8 @@ int ps_coupledcov_set_device(ps_ctx* c, int nblk, const int* kinds, const double
         for (int j = 0; j < nx; ++j)
             if (xw[j].prod == cl[0] && xw[j].par == cl[1]) js.push_back(j);
         if (js.empty()) continue;
-        const bool mma00 = cl[0] == ps::PROD_00_00 && (int)js.size() >= kMmaMin00;
-        const bool mma22 = cl[0] == ps::PROD_22_22 && (int)js.size() >= kMmaMin22;
+        const bool mma00 = cl[0] == ps::PROD_00_00 && (int)js.size() >= mma_min_slots(true, lmax);
+        const bool mma22 = cl[0] == ps::PROD_22_22 && (int)js.size() >= mma_min_slots(false, lmax);
         if (mma00 || mma22) {
             if ((st = ensure_mtiles(c, lmin, lmax)) || (st = arm_status(c, c->stream))) return st;
             for (size_t i0 = 0; i0 < js.size(); i0 += ps::kMmaMaxSlots) {
@@ -1023,7 +1034,7 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
         }
         base.wlen = wlen;
         // chosen mode: the TT slots (00 family) and the ++ / -- slots (22 family) of a set, each
-        // kind with at least kMmaMin00 / kMmaMin22 slots, go to the tensor-core kernels, up to kMmaMaxSlots
+        // kind with at least mma_min_slots slots, go to the tensor-core kernels, up to kMmaMaxSlots
         // windows per launch; the rest go to the CUDA-core kernels in groups of up to 8
         std::vector<Slot> mma00, mma22;
         if (mode == PS_MODE_CHOSEN && c->tensor_cores)
@@ -1031,8 +1042,8 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                 for (int s = 0; s < 4; ++s)
                     if ((cases & (1u << s)) && dM[4 * k + s] && s != PS_SPIN_02)
                         (s == PS_SPIN_00 ? mma00 : mma22).push_back(Slot{k, s});
-        if ((int)mma00.size() < kMmaMin00) mma00.clear();
-        if ((int)mma22.size() < kMmaMin22) mma22.clear();
+        if ((int)mma00.size() < mma_min_slots(true, lmax)) mma00.clear();
+        if ((int)mma22.size() < mma_min_slots(false, lmax)) mma22.clear();
         const int gs = ps::kMaxWin;  // one generation of the families serves up to 8 slots
         const auto groups = group_slots(cases, K, gs, [&](int k, int s) {
             if (!dM[4 * k + s]) return false;
@@ -1192,9 +1203,9 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
             for (int k = 0; k < P.K; ++k)
                 for (int s = 0; s < 4; ++s)
                     if ((P.cases & (1u << s)) && s != PS_SPIN_02) (s == PS_SPIN_00 ? m00 : m22).push_back(Slot{k, s});
-            if ((int)m00.size() >= kMmaMin00) cases_cc &= ~(1u << PS_SPIN_00);
+            if ((int)m00.size() >= mma_min_slots(true, P.lmax)) cases_cc &= ~(1u << PS_SPIN_00);
             else m00.clear();
-            if ((int)m22.size() >= kMmaMin22) cases_cc &= ~((1u << PS_SPIN_PP) | (1u << PS_SPIN_MM));
+            if ((int)m22.size() >= mma_min_slots(false, P.lmax)) cases_cc &= ~((1u << PS_SPIN_PP) | (1u << PS_SPIN_MM));
             else m22.clear();
         }
         if (!m00.empty() || !m22.empty()) {

@@ -151,9 +151,9 @@ def test_mcm_set_host(ctx, cases):
 
 
 def _routed_problems():
-    """Problems whose TT slots (4 or more) or ++/-- slots (5 or more) take the tensor-core
+    """Problems whose TT slots or ++/-- slots (9 or more at these sizes) take the tensor-core
     kernels, next to ones that stay on the CUDA cores."""
-    specs = [(97, 0, 0x1, 6), (130, 3, 0xC, 3), (64, 0, 0xF, 5), (77, 2, 0x1, 3), (50, 0, 0x3, 4)]
+    specs = [(97, 0, 0x1, 9), (130, 3, 0xC, 5), (64, 0, 0xF, 5), (77, 2, 0x1, 3), (50, 0, 0x3, 4)]
     probs, refs = [], []
     for i, (L, lmin, cases, K) in enumerate(specs):
         n = L - lmin + 1
@@ -170,15 +170,16 @@ def _routed_problems():
 
 @pytest.mark.parametrize("bps,graph", [(0, False), (-1, False), (0, True), (-1, True)])
 def test_batch_tensor_core_routing(ctx, bps, graph):
-    """The batch routes each problem's TT slots (4 or more) and ++/-- slots (5 or more) to the
-    tensor-core kernels, like ps_mcm_set_device: every output against the oracle (NaN sentinels),
+    """The batch routes each problem's TT slots and ++/-- slots to the tensor-core kernels when
+    there are enough for its lmax, like ps_mcm_set_device: every output against the oracle (NaN sentinels),
     in the persistent and the launch form, directly and from a CUDA graph; with the tensor cores
-    switched off the routed slots change in their last bits, and problem 3 (3 TT slots, grouped
-    the same either way) not at all.  The TE slots of problems 2 and 4 stay on the CUDA cores but
-    in other groups (a TE-only body instead of a mixed one), so only their tolerance is checked."""
+    switched off the routed slots change in their last bits, and problems 3 and 4 (TT and TE
+    slots on the CUDA cores, grouped the same either way) not at all.  Problem 2's TT and TE slots
+    stay on the CUDA cores but in other groups once its ++/-- slots leave, so only their tolerance
+    is checked."""
     probs, refs = _routed_problems()
-    routed = {(0, 0), (1, 2), (1, 3), (2, 0), (2, 2), (2, 3), (4, 0)}  # (problem, spin case)
-    same_groups = {(3, 0)}
+    routed = {(0, 0), (1, 2), (1, 3), (2, 2), (2, 3)}  # (problem, spin case)
+    same_groups = {(3, 0), (4, 0), (4, 1)}
     ctx.set_stream(torch.cuda.current_stream().cuda_stream)
     try:
         outs = {}

@@ -2,8 +2,8 @@
 
 In chosen mode the Xi of all the blocks' windows are computed grouped across
 the blocks by family product and parity (the squared (0 0 0) windows by the
-tensor-core kernel when there are 4 or more, the squared (2 -2 0) ones when
-there are 5 or more, the rest by the CUDA-core kernel in groups of up to 8),
+tensor-core kernel, and the squared (2 -2 0) ones, when there are enough of them
+for the lmax, the rest by the CUDA-core kernel in groups of up to 8),
 and each block is formed from its windows' Xi.  Plain FP64, or the tensor cores
 switched off, runs the fused covariance kernel block by block.
 """
@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 SET6 = ["TTTT", "EEEE", "TETE", "TTTE", "TTEE", "TEEE"]
-ROUTED = {"TTTT", "TTTE", "TTEE", "EEEE"}  # all their windows on the tensor-core kernels
+ROUTED = {"TTTT", "TTTE", "TTEE"}  # at lmax 180 all their 15 windows on the tensor-core kernel
 
 
 def _inputs(L, kinds, seed=0):
@@ -108,8 +108,8 @@ def test_cov_set_plain_fp64(ctx):
 
 
 def test_cov_set_below_the_thresholds(ctx):
-    """TTEE's 2 squared (0 0 0) windows (fewer than 4) and TEEE_PLANCK's 4 squared (2 -2 0) ones
-    (fewer than 5) take the CUDA-core kernel for their Xi: the same arithmetic as the fused kernel,
+    """TTEE's 2 squared (0 0 0) windows and TEEE_PLANCK's 4 squared (2 -2 0) ones (fewer than
+    the 9 needed at lmax 120) take the CUDA-core kernel for their Xi: the same arithmetic as the fused kernel,
     so the blocks agree with it to FP64 rounding of the final formula."""
     L = 120
     blocks = _inputs(L, ["TTEE", "TEEE_PLANCK"], seed=3)
