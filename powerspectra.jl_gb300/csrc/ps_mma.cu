@@ -105,6 +105,11 @@ __device__ __forceinline__ float pow2f_or_zero(int d)  // 2^d for d <= 0, 0 belo
 {
     return d < -126 ? 0.0f : __int_as_float((d + 127) << 23);
 }
+// 2^e as a double for e <= 1023, 0 below the normal range (the totals' scales, |e| < 300)
+__device__ __forceinline__ double pow2d_or_zero(int e)
+{
+    return e < -1022 ? 0.0 : __longlong_as_double((long long)(e + 1023) << 52);
+}
 
 // Byte offset of element (column n, step k) in a B plane: K-major core matrices,
 // 128 B between the two along K (LBO), 256 B between 8-column groups (SBO).
@@ -721,8 +726,8 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         for (int n = 0; n < NC; ++n) {
             FW[n] = BW[n] = 0.0;
             if (n < ncols) {
-                FW[n] = ldexp((double)tot[0][n].h + (double)tot[0][n].l, sm.ref[0][n]);
-                BW[n] = ldexp((double)tot[1][n].h + (double)tot[1][n].l, sm.ref[1][n]);
+                FW[n] = ((double)tot[0][n].h + (double)tot[0][n].l) * pow2d_or_zero(sm.ref[0][n]);
+                BW[n] = ((double)tot[1][n].h + (double)tot[1][n].l) * pow2d_or_zero(sm.ref[1][n]);
             }
         }
         const int jm = l2;  // jmin + T: the last forward point, in FP64; its parity is that of T
