@@ -83,11 +83,12 @@ constexpr uint32_t kIdesc = umma::idesc_bf16(128, kMmaCols);
 // (A part, B part)
 __device__ constexpr int kPass[6][2] = {{2, 0}, {1, 1}, {0, 2}, {1, 0}, {0, 1}, {0, 0}};
 
-// tensor memory columns: D forward [0, 16), D backward [16, 32), then A[half][sweep][plane], 8
-// columns each (a block's 32 steps: two MMA halves of 16, two steps per column)
-__device__ __forceinline__ uint32_t a_col(int half, int sweep, int plane)
+// tensor memory columns: D forward [0, 16), D backward [16, 32), then A[sweep][plane][half], 8
+// columns per half: a block's 32 steps of one sweep and plane in 16 consecutive columns, two
+// steps per column (step pair k of the block in column a_col(s, p) + k)
+__device__ __forceinline__ uint32_t a_col(int sweep, int plane, int half = 0)
 {
-    return 2u * kMmaCols + (uint32_t)(((half * 2 + sweep) * kPlanes + plane) * (kK / 2));
+    return 2u * kMmaCols + (uint32_t)(((sweep * kPlanes + plane) * 2 + half) * (kK / 2));
 }
 
 struct __align__(128) Smem {
@@ -674,11 +675,11 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             split3(xf[0], xf[1], wf);
             split3(xb[0], xb[1], wb);
             __syncwarp();  // the stores below are warp-collective (.sync.aligned)
-            const int h = s2 / kK, col = (s2 % kK) >> 1;  // MMA half, tensor-memory column in it
+            const uint32_t k = (uint32_t)(s2 >> 1);  // the step pair of the block
 #pragma unroll
             for (int pl = 0; pl < kPlanes; ++pl) {
-                umma::st_x1(tlane + a_col(h, 0, pl) + (uint32_t)col, wf[pl]);
-                umma::st_x1(tlane + a_col(h, 1, pl) + (uint32_t)col, wb[pl]);
+                umma::st_x1(tlane + a_col(0, pl) + k, wf[pl]);
+                umma::st_x1(tlane + a_col(1, pl) + k, wb[pl]);
             }
         };
         const int t1 = tb + kBlk - 1;  // the block's last time step
@@ -707,7 +708,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                     for (int h = 0; h < 2; ++h) {
                         const unsigned char* bt = kShift && ps == 5 && h == 1 ? &sm.Bsh[s][0] : &sm.B[h][s][kPass[ps][1]][0];
                         const uint64_t bd = umma::smem_desc(umma::smem_addr(bt), 128u, 256u);
-                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(h, s, kPass[ps][0]), bd,
+                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h), bd,
                                           kIdesc, ps > 0 || h > 0);
                     }
             umma::mma_commit(&sm.mbar);
