@@ -90,12 +90,15 @@ struct ps_ctx {
         std::vector<ps::MmaParams> host_mma;
         std::vector<char> host_mma00;
         int2* d_mtiles = nullptr;
+        unsigned char* d_btab = nullptr;  // the tensor-core launches' table of B tiles (one at a time)
     } batch;
     int tuned_group_slots = 0, tuned_blocks_per_sm = 0;
     // tensor-core kernels: their block list for the current (lmin, lmax) and the status of their bounded waits
     int2* d_mtiles = nullptr;
     size_t mtiles_cap = 0;
     int nmtiles = 0, mtile_lmin = -1, mtile_lmax = -1;
+    unsigned char* d_btab = nullptr;  // their table of B tiles (mma_table_bytes), one launch at a time
+    size_t btab_cap = 0;
     unsigned* d_status = nullptr;
     bool status_pending = false;  // a tensor-core launch whose status is not yet checked
     bool tensor_cores = true;
@@ -229,8 +232,12 @@ namespace ps {
 void mma_tile_list(int lmin, int lmax, std::vector<int2>& t);  // ps_mma.cu
 }
 
+static int ensure_bytes(ps_ctx* c, unsigned char** p, size_t* cap, size_t need);
+
+// The tensor-core kernels' block list for (lmin, lmax) and the scratch of their table of B tiles.
 static int ensure_mtiles(ps_ctx* c, int lmin, int lmax)
 {
+    if (int st = ensure_bytes(c, &c->d_btab, &c->btab_cap, ps::mma_table_bytes(lmax))) return st;
     if (c->mtile_lmin == lmin && c->mtile_lmax == lmax && c->d_mtiles) return PS_OK;
     std::vector<int2> t;
     ps::mma_tile_list(lmin, lmax, t);
@@ -352,6 +359,22 @@ static int run_coupling(ps_ctx* c, ps::CouplingParams& p, int mode, bool first =
     return PS_OK;
 }
 
+static int ensure_bytes(ps_ctx* c, unsigned char** p, size_t* cap, size_t need)
+{
+    if (need <= *cap) return PS_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)p, need);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_err(c, PS_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", need, cudaGetErrorString(e));
+    }
+    *cap = need;
+    return PS_OK;
+}
+
 static int ensure_int2(ps_ctx* c, int2** p, size_t* cap, size_t need)
 {
     if (need <= *cap) return PS_OK;
@@ -417,6 +440,7 @@ static void batch_release(ps_ctx* c)
     cudaFree(b.d_bf);
     cudaFree(b.d_tasks);
     cudaFree(b.d_mtiles);
+    cudaFree(b.d_btab);
     b = ps_ctx::Batch();
 }
 
@@ -584,6 +608,7 @@ void ps_destroy(ps_ctx* c)
     cudaFree(c->d_part);
     cudaFree(c->d_qp);
     cudaFree(c->d_mtiles);
+    cudaFree(c->d_btab);
     cudaFree(c->d_status);
     cudaFreeHost(c->h_pack);
     batch_release(c);
@@ -946,8 +971,9 @@ int ps_coupledcov_set_device(ps_ctx* c, int nblk, const int* kinds, const double
                 mp.tiles = c->d_mtiles;
                 mp.ntiles = c->nmtiles;
                 mp.status = c->d_status;
+                mp.tab = c->d_btab;
                 PS_CUDA(c, ps::launch_mma(mp, mma00, c->stream));
-                c->launches++;
+                c->launches += 2;
             }
         } else {
             for (size_t i0 = 0; i0 < js.size(); i0 += ps::kMaxWin) {
@@ -1076,8 +1102,9 @@ int ps_mcm_set_device(ps_ctx* c, unsigned cases, const double* const* dW, int K,
                 mp.tiles = c->d_mtiles;
                 mp.ntiles = c->nmtiles;
                 mp.status = c->d_status;
+                mp.tab = c->d_btab;
                 PS_CUDA(c, ps::launch_mma(mp, list == &mma00, c->stream));
-                c->launches++;
+                c->launches += 2;
             }
         }
         for (size_t g = 0; g < groups.size(); ++g) {
@@ -1314,9 +1341,19 @@ int ps_batch_prepare(ps_ctx* c, const ps_problem* probs, int nprob, int gs, int 
         batch_release(c);
         return st;
     }
+    if (!b.host_mma.empty()) {  // one table for the launches in turn: the size of the largest lmax
+        int tab_lmax = 0;
+        for (const auto& mp : b.host_mma) tab_lmax = std::max(tab_lmax, mp.lmax);
+        size_t cap = 0;
+        if ((st = ensure_bytes(c, &b.d_btab, &cap, ps::mma_table_bytes(tab_lmax)))) {
+            batch_release(c);
+            return st;
+        }
+    }
     for (size_t m = 0; m < b.host_mma.size(); ++m) {
         b.host_mma[m].tiles = b.d_mtiles + mma_tile_off[m];
         b.host_mma[m].status = c->d_status;
+        b.host_mma[m].tab = b.d_btab;
     }
     b.host_groups = groups;
     for (auto& g : b.host_groups) {
@@ -1370,7 +1407,7 @@ static int batch_enqueue(ps_ctx* c, cudaStream_t s)
 // kernels one run of the batch launches (window preparation included)
 static size_t batch_kernel_count(const ps_ctx::Batch& b)
 {
-    return 1 + b.host_mma.size() + (b.launches ? b.host_groups.size() : (b.nitems > 0 ? 1 : 0));
+    return 1 + 2 * b.host_mma.size() + (b.launches ? b.host_groups.size() : (b.nitems > 0 ? 1 : 0));
 }
 
 int ps_batch_run(ps_ctx* c)

@@ -132,9 +132,15 @@ struct MmaParams {
     const int2* tiles;                  // (r0, c0): rows r0 + 2w, columns c0 + 2i
     int ntiles;
     unsigned* status;                   // set to 1 when a bounded wait gives up
+    // scratch of mma_table_bytes(lmax) bytes (256-byte aligned) for the launch's table of B
+    // tiles; launch_mma fills it, and the entry ranges below, on the stream before the kernel
+    unsigned char* tab;
+    int tab_fmin, tab_nf, tab_bmin, tab_nb;  // forward entries l3 = fmin .. fmin + nf - 1, then backward ones
 };
-// fam00: the (0 0 0) family (every slot PAR_ALL); otherwise the (2 -2 0) family
+// fam00: the (0 0 0) family (every slot PAR_ALL); otherwise the (2 -2 0) family.  Two
+// launches: the table of B tiles, then the coupling kernel.
 cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s);
+size_t mma_table_bytes(int lmax);
 
 // A covariance block from its Xi matrices (ps_cov_combine.cu): C[l1, l2] =
 // cov_combine(kind, S, R, {X_k[l1, l2]}, l1, l2) over the whole n x n block.

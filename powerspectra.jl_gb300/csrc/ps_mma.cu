@@ -40,23 +40,34 @@
 // MMA halves: the second onto the first (at twice the scale) or, with at most
 // 8 columns, in D's spare columns on its own.  Each D is added to float-float
 // totals on the CUDA cores (into the low word; renormalised every fourth
-// block).  B is scaled per block by a running power of two (block floating
-// point; windows span 1e-45), the same role the slice exponents play in the
-// chosen kernel.  The last forward point, the match of the two sweeps, the
+// block).  B holds each column scaled by the largest power of two of its values
+// in the block (block floating point; windows span 1e-45), the same role the
+// slice exponents play in the chosen kernel; the fold brings D to the totals'
+// running exponent.  The last forward point, the match of the two sweeps, the
 // normalisation and the outputs are FP64.
 //
+// B tiles.  B of one block and sweep depends on the block's position only
+// through o, the l3 of its first time step: its step k holds the windows at
+// l3 = o + k (forward) or o - k (backward), o + 2k and o - 2k for the (0 0 0)
+// sweeps, with the slots' parities by the parity of k.  So a table kernel
+// builds, before the coupling kernel, one B tile per o that the launch's blocks
+// use, and a block takes its two tiles with two bulk copies.
+//
 // Pipeline per block q of 32 time steps: at its start the lanes build the
-// block's new ring values, wait (bounded) for the MMAs of block q - 1, add its
-// D into the totals, and build B of block q in shared memory from window
-// values fetched (cp.async) during block q - 1; then they write x (three
-// planes, two steps per 32-bit column, two MMA halves) into tensor memory, and
-// at the block end one thread issues the 24 MMAs of q (12 per sweep) and
-// commits them to an mbarrier.  A, B and D are single-buffered: 128 tensor
-// memory columns per block.  A wait that gives up sets *p.status.
+// block's new ring values, wait (bounded) for the MMAs of block q - 1 and add
+// its D into the totals; one thread starts the copies of block q + 1's tiles
+// into the buffer that those MMAs have released, and the first warp takes block
+// q's column scales from its tiles (copied a block ahead).  Then the lanes
+// write x (three planes, two steps per 32-bit column, two MMA halves) into
+// tensor memory, and at the block end one thread issues the 24 MMAs of q (12
+// per sweep) and commits them to an mbarrier.  A and D are single-buffered (128
+// tensor memory columns per block), B double-buffered in shared memory.  A wait
+// that gives up sets *p.status.
 #include "ps_internal.cuh"
 #include "ps_epilogue.cuh"
 #include "ps_ff.cuh"
 #include "ps_umma.cuh"
+#include "ps_mma_tiles.h"
 
 #include <cuda_bf16.h>
 #include <algorithm>
@@ -67,7 +78,8 @@ namespace ps {
 namespace {
 
 constexpr int kK = 16;            // time steps per MMA (BF16 K)
-constexpr int kBlk = 2 * kK;      // time steps per block: two MMA halves, one D, one barrier
+constexpr int kBlk = ps_mma_tiles::kBlk;  // time steps per block: two MMA halves, one D, one barrier
+static_assert(kBlk == 2 * kK, "a block is two MMA halves");
 constexpr int kPlanes = 3;        // hi, mid, lo BF16 parts
 constexpr int kLead = 6;          // forward skew offset: tF = tau - kLead - 2i + 2w
 constexpr int kRamp = 68;         // extra time steps of a block beyond r0 (both sweeps)
@@ -91,14 +103,27 @@ __device__ __forceinline__ uint32_t a_col(int sweep, int plane, int half = 0)
     return 2u * kMmaCols + (uint32_t)(((sweep * kPlanes + plane) * 2 + half) * (kK / 2));
 }
 
+// B of one block and sweep, as the table holds it and a block's shared memory receives it: the
+// block's 32 time steps of every column, in units of 2^E[column].
+struct __align__(16) BTile {
+    unsigned char B[2][kPlanes][kBPlane];  // [half][part]: K-major BF16, core matrices 8 x 16 B
+    int E[kMmaCols];                       // the largest exponent of the column's values (kZeroExp: all zero)
+    unsigned char Bsh[kBPlane];            // the hi part of half 1 with column n at (n + 8) mod 16
+};
+static_assert(sizeof(BTile) == 2 * kPlanes * kBPlane + 64 + kBPlane && sizeof(BTile) % 16 == 0,
+              "tiles are whole 16-byte units");
+// the bytes a block copies per tile: Bsh only with at most 8 columns in use
+constexpr uint32_t kTileBytesShift = (uint32_t)sizeof(BTile);
+constexpr uint32_t kTileBytes = (uint32_t)(2 * kPlanes * kBPlane + 64);
+
 struct __align__(128) Smem {
-    unsigned char B[2][2][kPlanes][kBPlane];  // [half][sweep][part]: K-major BF16, core matrices 8 x 16 B
-    unsigned char Bsh[2][kBPlane];            // [sweep]: the hi part of half 1 with column n at (n + 8) mod 16
-    float rescale[3][2][kMmaCols];            // factor for the totals before adding block q's D (slot q % 3)
-    int grew[3][4];                           // per warp of build_B: some column's scale grew (slot q % 3)
-    int2 stage[2][2][kMmaCols][kK];           // [half][sweep][column][step]: the next block's window values
-    int ref[2][kMmaCols];                     // running exponent of B's scale per sweep and column
-    uint64_t mbar;
+    BTile b[2][2];                  // [buffer][sweep]: block q's tiles in buffer q % 2
+    float rescale[3][2][kMmaCols];  // factor for the totals before adding block q's D (slot q % 3)
+    float dscale[3][2][kMmaCols];   // factor for block q's D: 2^(its exponent - the running one)
+    int grew[3][2];                 // per sweep: some column's running exponent grew at block q
+    int ref[2][kMmaCols];           // running exponent per sweep and column
+    uint64_t mbar;                  // the MMAs of a block
+    uint64_t bbar[2];               // the copies into buffer 0 / 1
     uint32_t tmem;
 };
 
@@ -137,100 +162,92 @@ __device__ __forceinline__ void split3(float a, float b, uint32_t (&w)[kPlanes])
 template <bool F00>
 __device__ __forceinline__ int l3_of(int s, int tau, int r0, int c0)
 {
-    if (F00) return s ? r0 + c0 + 68 - 2 * tau : c0 - r0 - 6 + 2 * tau;
-    return s ? r0 + c0 + kRamp - tau : c0 - r0 - kLead + tau;
+    return ps_mma_tiles::l3_at(F00, s, tau, r0, c0);
 }
+static_assert(ps_mma_tiles::l3_at(false, 0, 0, 0, 0) == -kLead && ps_mma_tiles::l3_at(false, 1, 0, 0, 0) == kRamp,
+              "the skew of the (2 -2 0) sweeps");
 
-// Whether B's element (sweep s, column n, time step tau) is a window value, and its l3.  The
-// (0 0 0) sweeps visit only points where l1 + l2 + l3 is even.
+// ---- the table of B tiles ---------------------------------------------------------
+// Entry e < nf is the forward tile of o = fmin + e, entry nf + e the backward tile of o = bmin + e
+// (ps_mma_tiles::table_geom: the ranges every block of a launch stays in).
+using ps_mma_tiles::TableGeom;
+using ps_mma_tiles::table_geom;
+
+// One tile per block of 128 threads: thread = column n (16) x 4 consecutive steps k (8).  The
+// (0 0 0) sweeps visit only points where l1 + l2 + l3 is even; a (2 -2 0) slot of one parity
+// takes the steps of that parity (l1 + l2 + l3 has the parity of the time step, whose blocks
+// start at even steps).  Column nslot is the normalisation, 2 l3 + 1.  With at most 8 columns
+// in use, the hi part of half 1 is also written with its columns moved up by 8 (the zero
+// columns 8-15 moving down to 0-7), so that its hi x hi product lands in D's spare columns.
 template <bool F00>
-__device__ __forceinline__ bool b_window(const MmaParams& p, int s, int n, int tau, int r0, int c0, int& l3)
+__global__ void __launch_bounds__(128) k_mma_table(const MmaParams p)
 {
-    l3 = l3_of<F00>(s, tau, r0, c0);
-    if (l3 < 0 || l3 >= p.wlen || n >= p.nslot) return false;
-    const int par = p.parity[n];
-    if (F00) return par != PAR_ODD;
-    return par == PAR_ALL || (par == PAR_EVEN) == ((tau & 1) == 0);
-}
-
-// A block covers the time steps tb .. tb + 31 (two halves of 16).
-// Start the copies of a block's window values that this thread's part of build_B needs (4 steps
-// of each half, one sweep and column, 8 bytes each) into the stage, a block ahead, so their
-// latency is hidden behind a block of steps.
-template <bool F00>
-__device__ __forceinline__ void fetch_B(const MmaParams& p, Smem& sm, int tb, int r0, int c0, int tid)
-{
-    const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3;
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            int l3;
-            if (b_window<F00>(p, s, n, tb + kK * h + 4 * qd + u, r0, c0, l3))
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(
-                                 umma::smem_addr(&sm.stage[h][s][n][4 * qd + u])),
-                             "l"(p.bf[n] + l3)
-                             : "memory");
-        }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-
-// B of block q (both halves; all 128 threads: thread = sweep x column x 4 steps of each half),
-// from the values this thread fetched.  One scale per block, sweep and column: the two halves'
-// MMAs add into one D.  With at most 8 columns in use (SHIFT), the hi part of half 1 is also
-// written with its columns moved up by 8 (the zero columns 8-15 moving down to 0-7), so that
-// its hi x hi product lands in D's spare columns 8-15.
-template <bool F00, bool SHIFT>
-__device__ __forceinline__ void build_B(const MmaParams& p, Smem& sm, int q, int tb, int r0, int c0, int tid)
-{
-    const int s = tid >> 6, n = (tid >> 2) & (kMmaCols - 1), qd = tid & 3, lane = tid & 31;
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    float m[8];
-    int e[8];
+    const int e = blockIdx.x, tid = threadIdx.x;
+    const int s = e < p.tab_nf ? 0 : 1;
+    const int o = s ? p.tab_bmin + (e - p.tab_nf) : p.tab_fmin + e;
+    const int n = tid >> 3, kq = tid & 7;
+    const int step = F00 ? 2 : 1;
+    float m[4];
+    int ex[4];
     int emax = kZeroExp;
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = 4 * h + u, tau = tb + kK * h + 4 * qd + u;
-            int l3;
-            m[i] = 0.0f;
-            e[i] = kZeroExp;
-            if (b_window<F00>(p, s, n, tau, r0, c0, l3)) {
-                const int2 v = sm.stage[h][s][n][4 * qd + u];
-                m[i] = __int_as_float(v.x);
-                e[i] = v.y;
-            } else if (n == p.nslot && l3 >= 0 && l3 < p.wlen) {  // the normalisation column: 2 l3 + 1
-                m[i] = frexpf((float)(2 * l3 + 1), &e[i]);
+    for (int u = 0; u < 4; ++u) {
+        const int k = 4 * kq + u, l3 = s ? o - step * k : o + step * k;
+        m[u] = 0.0f;
+        ex[u] = kZeroExp;
+        if (l3 >= 0 && l3 < p.wlen) {
+            if (n < p.nslot) {
+                const int par = p.parity[n];
+                if (F00 ? par != PAR_ODD : (par == PAR_ALL || (par == PAR_EVEN) == ((k & 1) == 0))) {
+                    const int2 v = __ldg(p.bf[n] + l3);
+                    m[u] = __int_as_float(v.x);
+                    ex[u] = v.y;
+                }
+            } else if (n == p.nslot) {
+                m[u] = frexpf((float)(2 * l3 + 1), &ex[u]);
             }
-            emax = max(emax, e[i]);
         }
+        emax = max(emax, ex[u]);
+    }
+    // the column's 8 threads are consecutive lanes
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 2));
-    int rold = qd == 0 ? sm.ref[s][n] : 0;
-    rold = __shfl_sync(0xffffffffu, rold, lane & ~3);
-    const int rnew = max(rold, emax);
-    if (qd == 0) {
-        sm.ref[s][n] = rnew;
-        sm.rescale[q % 3][s][n] = rold == rnew ? 1.0f : pow2f_or_zero(rold - rnew);
-    }
-    // warps 0, 1 build sweep 0 and warps 2, 3 sweep 1: the flush reads two flags, not 16 factors
-    const unsigned grew = __ballot_sync(0xffffffffu, qd == 0 && rold != rnew);
-    if (lane == 0) sm.grew[q % 3][tid >> 5] = grew != 0u;
-    const int off = b_off(n, 4 * qd);
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 4));
+    BTile& T = reinterpret_cast<BTile*>(p.tab)[e];
+    if (kq == 0) T.E[n] = emax;
+    float v[4];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float v[4];
+    for (int u = 0; u < 4; ++u) v[u] = m[u] * pow2f_or_zero(ex[u] - emax);
+    uint32_t w01[kPlanes], w23[kPlanes];
+    split3(v[0], v[1], w01);
+    split3(v[2], v[3], w23);
+    const int h = kq >> 2, kk = 4 * (kq & 3);
+    const int off = b_off(n, kk);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = m[4 * h + u] * pow2f_or_zero(e[4 * h + u] - rnew);
-        uint32_t w01[kPlanes], w23[kPlanes];
-        split3(v[0], v[1], w01);
-        split3(v[2], v[3], w23);
+    for (int pl = 0; pl < kPlanes; ++pl) *reinterpret_cast<uint2*>(&T.B[h][pl][off]) = make_uint2(w01[pl], w23[pl]);
+    if (p.nslot + 1 <= 8 && h == 1)
+        *reinterpret_cast<uint2*>(&T.Bsh[b_off((n + 8) & (kMmaCols - 1), kk)]) = make_uint2(w01[0], w23[0]);
+}
+
+// One thread starts the copies of block q's two tiles (time steps q kBlk ..) into buffer q % 2.
+// An entry outside the table (which the ranges above exclude) is replaced by the first entry of
+// its sweep and reported through ok.
+template <bool F00>
+__device__ __forceinline__ void copy_tiles(const MmaParams& p, Smem& sm, int q, int r0, int c0, uint32_t bytes,
+                                           bool& ok)
+{
+    const int tb = q * kBlk, buf = q & 1;
+    umma::mbar_expect_tx(&sm.bbar[buf], 2u * bytes);
 #pragma unroll
-        for (int pl = 0; pl < kPlanes; ++pl)
-            *reinterpret_cast<uint2*>(&sm.B[h][s][pl][off]) = make_uint2(w01[pl], w23[pl]);
-        if (SHIFT && h == 1)
-            *reinterpret_cast<uint2*>(&sm.Bsh[s][b_off((n + 8) & (kMmaCols - 1), 4 * qd)]) = make_uint2(w01[0], w23[0]);
+    for (int s = 0; s < 2; ++s) {
+        const int o = l3_of<F00>(s, tb, r0, c0);
+        int e = s ? o - p.tab_bmin : o - p.tab_fmin;
+        if (e < 0 || e >= (s ? p.tab_nb : p.tab_nf)) {
+            ok = false;
+            e = 0;
+        }
+        if (s) e += p.tab_nf;
+        umma::bulk_g2s(&sm.b[buf][s], p.tab + (size_t)e * sizeof(BTile), bytes, &sm.bbar[buf]);
     }
 }
 
@@ -516,7 +533,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int d = l2 - l1;
     // block q covers the time steps q kBlk .. q kBlk + 31; the sweeps run for tau in
     // [0, r0 + kRamp) ((2 -2 0)) or [0, floor((r0 + 1) / 2) + 34) ((0 0 0), two points per step)
-    const int ntau = F00 ? ((r0 + 1) >> 1) + 34 : r0 + kRamp;
+    const int ntau = ps_mma_tiles::nsteps(F00, r0);
     const int nk = (ntau + kBlk - 1) / kBlk;  // 32-step blocks of the skewed sweeps (block-uniform)
     const int ncols = p.nslot + 1;
     // With at most 8 columns (NC == 8) D's columns 8-15 are spare: the hi x hi product of the
@@ -525,15 +542,25 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     // scale of its own 16 steps, as with one D per 16 steps.
     constexpr bool kShift = NC == 8;
 
+    constexpr uint32_t kBytes = kShift ? kTileBytesShift : kTileBytes;
+    bool ok = true;
+
     if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
     if (tid < 2 * kMmaCols) sm.ref[tid / kMmaCols][tid % kMmaCols] = kZeroExp;
-    if (tid == 0) umma::mbar_init(&sm.mbar);
+    if (tid == 0) {
+        umma::mbar_init(&sm.mbar);
+        umma::mbar_init(&sm.bbar[0]);
+        umma::mbar_init(&sm.bbar[1]);
+    }
     umma::fence_before_sync();
     __syncthreads();
     umma::fence_after_sync();
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
-    fetch_B<F00>(p, sm, 0, r0, c0, tid);
+    if (tid == 0) {  // the tiles of blocks 0 and 1 (both buffers are free)
+        copy_tiles<F00>(p, sm, 0, r0, c0, kBytes, ok);
+        if (nk > 1) copy_tiles<F00>(p, sm, 1, r0, c0, kBytes, ok);
+    }
     if constexpr (F00) build_rings00_first(R, 0, warp, l1, c0, lane);
     else build_rings_first(R, 0, warp, l1, c0, lane);
 
@@ -546,7 +573,36 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     for (int s = 0; s < 2; ++s)
 #pragma unroll
         for (int n = 0; n < NC; ++n) tot[s][n] = ff_make(0.0f);
-    bool ok = true;
+
+    // The first warp, lane = sweep (lane / 16) x column (lane % 16), once block q's tiles have
+    // arrived: the column's running exponent (in a register and in sm.ref) and the factors that
+    // the fold of block q applies, to the totals where the running exponent grows and to D.
+    int ref = kZeroExp;
+    auto scales = [&](int q) {
+        const int s = lane >> 4, n = lane & (kMmaCols - 1);
+        ok &= umma::mbar_wait(&sm.bbar[q & 1], (uint32_t)((q >> 1) & 1), kWaitLimit);
+        const int E = sm.b[q & 1][s].E[n];
+        float dsc = 0.0f, rsc = 1.0f;
+        bool grew = false;
+        if (E != kZeroExp) {
+            if (E > ref) {
+                rsc = pow2f_or_zero(ref - E);
+                dsc = 1.0f;
+                ref = E;
+                sm.ref[s][n] = E;
+                grew = true;
+            } else {
+                dsc = pow2f_or_zero(E - ref);
+            }
+        }
+        sm.dscale[q % 3][s][n] = dsc;
+        sm.rescale[q % 3][s][n] = rsc;
+        const unsigned g = __ballot_sync(0xffffffffu, grew);
+        if (lane == 0) {
+            sm.grew[q % 3][0] = (g & 0xffffu) != 0u;
+            sm.grew[q % 3][1] = (g >> 16) != 0u;
+        }
+    };
 
     auto flush = [&](int q) {
         ok &= umma::mbar_wait(&sm.mbar, (uint32_t)(q & 1), kWaitLimit);
@@ -556,9 +612,9 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         for (int s = 0; s < 2; ++s) {
             float dv[kMmaCols];
             umma::ld_x16(tlane + (uint32_t)(s * kMmaCols), dv);
-            // the totals move to block q's scale where its exponent grew (the same for every
-            // thread: a uniform branch, taken only when some window's scale changed)
-            if (sm.grew[q % 3][2 * s] | sm.grew[q % 3][2 * s + 1]) {
+            // the totals move to the new running exponent where it grew (the same for every
+            // thread: a uniform branch, taken only when some window's exponent grew)
+            if (sm.grew[q % 3][s]) {
                 const float4* rs = reinterpret_cast<const float4*>(&sm.rescale[q % 3][s][0]);
 #pragma unroll
                 for (int v = 0; v < NC / 4; ++v) {
@@ -575,9 +631,16 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll
                 for (int n = 0; n < NC; ++n) dv[n] = __fadd_rn(dv[n], dv[n + 8]);
             }
+            // D in units of 2^(block exponent), brought to the running exponent (an exact power of two)
+            const float4* ds = reinterpret_cast<const float4*>(&sm.dscale[q % 3][s][0]);
 #pragma unroll
-            for (int n = 0; n < NC; ++n)
-                if (n < ncols) tot[s][n].l = __fadd_rn(tot[s][n].l, dv[n]);
+            for (int v = 0; v < NC / 4; ++v) {
+                const float4 d4 = ds[v];
+                const float dw[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (4 * v + j < ncols) tot[s][4 * v + j].l = __fmaf_rn(dv[4 * v + j], dw[j], tot[s][4 * v + j].l);
+            }
             switch (q & 3) {
                 case 0: renorm<0>(tot[s], ncols); break;
                 case 1: renorm<1>(tot[s], ncols); break;
@@ -597,19 +660,17 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     const int nx00 = (T + 1) / 2, ns00 = T / 2, steady00 = ((r0 + 1) >> 1) + 1;
     for (int q = 0; q < nk; ++q) {
         const int tb = q * kBlk;  // the block's first time step
-        // ---- block start: the A operand, B and D are single-buffered ----
+        // ---- block start: the A operand and D are single-buffered, B double-buffered ----
         if (q > 0) {
             // the ring values of this block (no MMA reads them), then the MMAs of block q - 1
-            // (issued at its end): D into the totals; their A and B may be overwritten after
+            // (issued at its end): D into the totals; A and the B buffer of q - 1 may be
+            // overwritten after, the latter by block q + 1's tiles
             if constexpr (F00) build_rings00_next(R, tb, warp, l1, c0, lane);
             else build_rings_next(R, tb, warp, l1, c0, lane);
             flush(q - 1);
+            if (tid == 0 && q + 1 < nk) copy_tiles<F00>(p, sm, q + 1, r0, c0, kBytes, ok);
         }
-        build_B<F00, kShift>(p, sm, q, tb, r0, c0, tid);
-        // the stage holds the next block's values from here on; each thread's copies go to the
-        // elements it has just read, after the warp's reads
-        __syncwarp();
-        if (q + 1 < nk) fetch_B<F00>(p, sm, tb + kBlk, r0, c0, tid);
+        if (warp == 0) scales(q);
         __syncwarp();  // the ring values of the block, written by the warp's lanes
         // the ring indices of the block's first time step (first step pair)
         RingIdx00 ix00;
@@ -691,22 +752,23 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll 1
             for (int s2 = 0; s2 < kBlk; s2 += 2) pair(s2, false);
         }
-        // ---- block end: A and B complete, one thread issues the block's 24 MMAs ----
+        // ---- block end: A complete (B arrived before the first warp's scales), one thread
+        // issues the block's 24 MMAs ----
         umma::wait_st();
-        umma::fence_smem_async();
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
         if (tid == 0) {
             // per sweep: the five small products of both halves first, hi x hi of both last; the
             // first MMA starts D from zero
+            const BTile* bq = sm.b[q & 1];
 #pragma unroll
             for (int s = 0; s < 2; ++s)
 #pragma unroll
                 for (int ps = 0; ps < 6; ++ps)
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const unsigned char* bt = kShift && ps == 5 && h == 1 ? &sm.Bsh[s][0] : &sm.B[h][s][kPass[ps][1]][0];
+                        const unsigned char* bt = kShift && ps == 5 && h == 1 ? &bq[s].Bsh[0] : &bq[s].B[h][kPass[ps][1]][0];
                         const uint64_t bd = umma::smem_desc(umma::smem_addr(bt), 128u, 256u);
                         umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h), bd,
                                           kIdesc, ps > 0 || h > 0);
@@ -826,25 +888,32 @@ static_assert(5 * (kBlockSmem + 1024) > 228 * 1024 && 4 * (kBlockSmem + 1024) <=
 // in four classes of (row parity, column parity), heaviest (largest r0) first.
 void mma_tile_list(int lmin, int lmax, std::vector<int2>& t)
 {
-    t.clear();
-    for (int pr = 0; pr < 2; ++pr) {
-        const int rmax = lmax - ((lmax - pr) & 1);
-        for (int r0 = rmax - 6; r0 + 6 >= lmin; r0 -= 8) {
-            int lo = r0;  // lowest row of the tile that exists
-            while (lo < lmin || lo < 0) lo += 2;
-            for (int pc = 0; pc < 2; ++pc) {
-                const int cmax = lmax - ((lmax - pc) & 1);
-                for (int c0 = cmax - 62; c0 + 62 >= lo; c0 -= 64) t.push_back(make_int2(r0, c0));
-            }
-        }
-    }
-    std::stable_sort(t.begin(), t.end(), [](int2 a, int2 b) { return a.x > b.x; });
+    std::vector<std::pair<int, int>> b;
+    ps_mma_tiles::block_list(lmin, lmax, b);
+    t.resize(b.size());
+    for (size_t i = 0; i < b.size(); ++i) t[i] = make_int2(b[i].first, b[i].second);
 }
 
-cudaError_t launch_mma(const MmaParams& p, bool fam00, cudaStream_t s)
+size_t mma_table_bytes(int lmax)
 {
-    if (p.ntiles <= 0) return cudaSuccess;
+    const TableGeom g = table_geom(lmax < 0 ? 0 : lmax);
+    return (size_t)(g.nf + g.nb) * sizeof(BTile);
+}
+
+cudaError_t launch_mma(const MmaParams& p0, bool fam00, cudaStream_t s)
+{
+    if (p0.ntiles <= 0) return cudaSuccess;
+    if (!p0.tab || ((uintptr_t)p0.tab & 15u) || p0.lmax < 0) return cudaErrorInvalidValue;
     static_assert(sizeof(Smem) + kOccupancySmem <= 48 * 1024, "within the default shared memory limit");
+    MmaParams p = p0;
+    const TableGeom g = table_geom(p.lmax);
+    p.tab_fmin = g.fmin;
+    p.tab_nf = g.nf;
+    p.tab_bmin = g.bmin;
+    p.tab_nb = g.nb;
+    if (fam00) k_mma_table<true><<<(unsigned)(g.nf + g.nb), 128, 0, s>>>(p);
+    else k_mma_table<false><<<(unsigned)(g.nf + g.nb), 128, 0, s>>>(p);
+    if (cudaError_t e = cudaGetLastError()) return e;
     const unsigned grid = (unsigned)p.ntiles;
     auto go = [&](auto kernel) { kernel<<<grid, 128, kOccupancySmem, s>>>(p); };
     const bool nc8 = p.nslot + 1 <= 8, stage = p.stage_rows != 0;

@@ -1,7 +1,8 @@
 // ps_umma.cuh -- inline-PTX wrappers for the 5th-generation tensor core
 // (tcgen05) as the coupling kernels use it: tensor-memory allocation, BF16
 // MMAs with FP32 accumulators in tensor memory, loads and stores of tensor
-// memory, and the mbarrier that an MMA commit arrives on.
+// memory, the mbarrier that an MMA commit arrives on, and bulk copies from
+// global to shared memory that complete on an mbarrier.
 //
 // Layouts (one CTA of 128 threads, M = 128 rows = TMEM lanes 0..127; warp w
 // reaches lanes 32w .. 32w + 31):
@@ -76,6 +77,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int li
         if (done) return true;
     }
     return false;
+}
+
+// One arrival on the mbarrier that also expects `bytes` more bytes of bulk copies in this phase.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from global memory to
+// this block's shared memory; its bytes complete the mbarrier's expected transaction.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
 }
 
 // D (tensor memory) = A (tensor memory) x B (shared memory) [+ D when acc]; issued by one thread.
