@@ -557,6 +557,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     umma::fence_after_sync();
     const uint32_t tbase = sm.tmem;
     const uint32_t tlane = tbase + ((uint32_t)(32 * warp) << 16);
+    const uint64_t bdesc0 = umma::smem_desc(umma::smem_addr(&sm.b[0][0]), 128u, 256u);  // B[0] of buffer 0, sweep 0
     if (tid == 0) {  // the tiles of blocks 0 and 1 (both buffers are free)
         copy_tiles<F00>(p, sm, 0, r0, c0, kBytes, ok);
         if (nk > 1) copy_tiles<F00>(p, sm, 1, r0, c0, kBytes, ok);
@@ -677,13 +678,13 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         RingIdx ix22;
         if constexpr (F00) ix00 = ring00_idx(tb + fofs, tb + bofs, l2);
         else ix22 = ring_idx(tb + fofs, tb + bofs, l2);
-        // One step pair of the block: the steps of both sweeps, then x into tensor memory.  In a
-        // block whose steps all lie in the steady state, every lane that runs is inside both
+        // One step pair of the block: the steps of both sweeps, and x of both as split words.  In
+        // a block whose steps all lie in the steady state, every lane that runs is inside both
         // sweeps, so both steps run unconditionally (their dependency chains interleave).  Lanes
         // that do not run compute values that may not be finite: they reach only their own rows
         // of the MMAs (row m of D is row m of A times B) and their own totals, never written.
         // The other blocks (the first few and the last) check every step.
-        auto pair = [&](int s2, bool steady) {
+        auto pair = [&](int s2, bool steady, uint32_t (&wf)[kPlanes], uint32_t (&wb)[kPlanes]) {
             float xf[2], xb[2];
             const int tau0 = tb + s2;
             if constexpr (F00) {
@@ -732,25 +733,31 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
                     }
                 }
             }
-            uint32_t wf[kPlanes], wb[kPlanes];
             split3(xf[0], xf[1], wf);
             split3(xb[0], xb[1], wb);
+        };
+        // Two step pairs (s2 .. s2 + 3), then their x into tensor memory: step pairs k and k + 1
+        // of the block in two consecutive columns of each sweep and plane, one store each.
+        auto two_pairs = [&](int s2, bool steady) {
+            uint32_t wf0[kPlanes], wb0[kPlanes], wf1[kPlanes], wb1[kPlanes];
+            pair(s2, steady, wf0, wb0);
+            pair(s2 + 2, steady, wf1, wb1);
             __syncwarp();  // the stores below are warp-collective (.sync.aligned)
-            const uint32_t k = (uint32_t)(s2 >> 1);  // the step pair of the block
+            const uint32_t k = (uint32_t)(s2 >> 1);  // the first step pair
 #pragma unroll
             for (int pl = 0; pl < kPlanes; ++pl) {
-                umma::st_x1(tlane + a_col(0, pl) + k, wf[pl]);
-                umma::st_x1(tlane + a_col(1, pl) + k, wb[pl]);
+                umma::st_x2(tlane + a_col(0, pl) + k, wf0[pl], wf1[pl]);
+                umma::st_x2(tlane + a_col(1, pl) + k, wb0[pl], wb1[pl]);
             }
         };
         const int t1 = tb + kBlk - 1;  // the block's last time step
         const bool steady = F00 ? (tb >= 34 && t1 <= steady00) : (tb >= kSteady && t1 <= r0 + kLead - 1);
         if (steady) {
-#pragma unroll 2
-            for (int s2 = 0; s2 < kBlk; s2 += 2) pair(s2, true);
+#pragma unroll 1
+            for (int s2 = 0; s2 < kBlk; s2 += 4) two_pairs(s2, true);
         } else {
 #pragma unroll 1
-            for (int s2 = 0; s2 < kBlk; s2 += 2) pair(s2, false);
+            for (int s2 = 0; s2 < kBlk; s2 += 4) two_pairs(s2, false);
         }
         // ---- block end: A complete (B arrived before the first warp's scales), one thread
         // issues the block's 24 MMAs ----
@@ -761,17 +768,20 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
         if (tid == 0) {
             // per sweep: the five small products of both halves first, hi x hi of both last; the
             // first MMA starts D from zero
-            const BTile* bq = sm.b[q & 1];
+            // descriptors of buffer q % 2: the first one's plus the planes' offsets (in 16-byte
+            // units, within the 14-bit address field: shared memory lies below 256 KB)
+            const uint64_t bq = bdesc0 + (uint64_t)((q & 1) * (2 * sizeof(BTile) / 16));
 #pragma unroll
             for (int s = 0; s < 2; ++s)
 #pragma unroll
                 for (int ps = 0; ps < 6; ++ps)
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const unsigned char* bt = kShift && ps == 5 && h == 1 ? &bq[s].Bsh[0] : &bq[s].B[h][kPass[ps][1]][0];
-                        const uint64_t bd = umma::smem_desc(umma::smem_addr(bt), 128u, 256u);
-                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h), bd,
-                                          kIdesc, ps > 0 || h > 0);
+                        const uint32_t off = (uint32_t)(s * sizeof(BTile)) +
+                                             (kShift && ps == 5 && h == 1 ? (uint32_t)offsetof(BTile, Bsh)
+                                                                          : (uint32_t)((h * kPlanes + kPass[ps][1]) * kBPlane));
+                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h),
+                                          bq + (off >> 4), kIdesc, ps > 0 || h > 0);
                     }
             umma::mma_commit(&sm.mbar);
         }

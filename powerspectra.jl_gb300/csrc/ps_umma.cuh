@@ -115,6 +115,11 @@ __device__ __forceinline__ void st_x1(uint32_t taddr, uint32_t v)
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};\n" ::"r"(taddr), "r"(v) : "memory");
 }
+// Two consecutive 32-bit columns of this warp's lanes (v0 in the first).
+__device__ __forceinline__ void st_x2(uint32_t taddr, uint32_t v0, uint32_t v1)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};\n" ::"r"(taddr), "r"(v0), "r"(v1) : "memory");
+}
 __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory"); }
 
 // 16 consecutive 32-bit columns of this warp's lanes (one value per column per
