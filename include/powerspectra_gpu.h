@@ -154,9 +154,12 @@ int ps_mcm_set_device(ps_ctx *ctx, unsigned cases, const double *const *dW, int 
  * computed by the tensor-core kernels: one
  * generation of the (0 0 0) or (2 -2 0) family for up to 15 windows,
  * contracted by BF16 tcgen05 MMAs in a three-part split with FP32
- * accumulators and float-float totals (same 1e-6 bar).  Their waits on
- * the tensor core are bounded: a wait that gives up is reported as
- * PS_ERR_TIMEOUT by the next ps_synchronize or host-pointer call. */
+ * accumulators and float-float totals (same 1e-6 bar).  Each such launch
+ * first builds its table of window tiles in a context-owned device buffer of
+ * (3 lmax + 160) x 3648 bytes (90 MB at lmax 8191), grown on demand.  Their
+ * waits on the tensor core and on the tile copies are bounded: a wait that
+ * gives up is reported as PS_ERR_TIMEOUT by the next ps_synchronize or
+ * host-pointer call. */
 /* The same with host spectra and host matrices: returns when every M is
  * filled (page-locked matrices are written by the kernel in place). */
 int ps_mcm_set(ps_ctx *ctx, unsigned cases, const double *const *W, int K, int64_t nW, int lmin, int lmax, int mode,
