@@ -56,13 +56,14 @@
 // Pipeline per block q of 32 time steps: at its start the lanes build the
 // block's new ring values, wait (bounded) for the MMAs of block q - 1 and add
 // its D into the totals; one thread starts the copies of block q + 1's tiles
-// into the buffer that those MMAs have released, and the first warp takes block
+// into the buffer that those MMAs have released, and the last warp takes block
 // q's column scales from its tiles (copied a block ahead).  Then the lanes
 // write x (three planes, two steps per 32-bit column, two MMA halves) into
-// tensor memory, and at the block end one thread issues the 24 MMAs of q (12
-// per sweep) and commits them to an mbarrier.  A and D are single-buffered (128
-// tensor memory columns per block), B double-buffered in shared memory.  A wait
-// that gives up sets *p.status.
+// tensor memory, and at the block end two threads (one per sweep, in
+// different warps) issue the 24 MMAs of q, 12 each, and commit them to one
+// mbarrier.  A and D are single-buffered (128 tensor memory columns per
+// block), B double-buffered in shared memory.  A wait that gives up sets
+// *p.status.
 #include "ps_internal.cuh"
 #include "ps_epilogue.cuh"
 #include "ps_ff.cuh"
@@ -548,7 +549,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
     if (warp == 0) umma::tmem_alloc(&sm.tmem, kTmemCols);
     if (tid < 2 * kMmaCols) sm.ref[tid / kMmaCols][tid % kMmaCols] = kZeroExp;
     if (tid == 0) {
-        umma::mbar_init(&sm.mbar);
+        umma::mbar_init(&sm.mbar, 2);  // one commit per sweep
         umma::mbar_init(&sm.bbar[0]);
         umma::mbar_init(&sm.bbar[1]);
     }
@@ -575,9 +576,10 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll
         for (int n = 0; n < NC; ++n) tot[s][n] = ff_make(0.0f);
 
-    // The first warp, lane = sweep (lane / 16) x column (lane % 16), once block q's tiles have
+    // The last warp, lane = sweep (lane / 16) x column (lane % 16), once block q's tiles have
     // arrived: the column's running exponent (in a register and in sm.ref) and the factors that
     // the fold of block q applies, to the totals where the running exponent grows and to D.
+    // (The first warp starts the copies, the first two issue the MMAs.)
     int ref = kZeroExp;
     auto scales = [&](int q) {
         const int s = lane >> 4, n = lane & (kMmaCols - 1);
@@ -671,7 +673,7 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
             flush(q - 1);
             if (tid == 0 && q + 1 < nk) copy_tiles<F00>(p, sm, q + 1, r0, c0, kBytes, ok);
         }
-        if (warp == 0) scales(q);
+        if (warp == 3) scales(q);
         __syncwarp();  // the ring values of the block, written by the warp's lanes
         // the ring indices of the block's first time step (first step pair)
         RingIdx00 ix00;
@@ -759,32 +761,33 @@ __global__ void __launch_bounds__(128) k_coupling_mma(const MmaParams p)
 #pragma unroll 1
             for (int s2 = 0; s2 < kBlk; s2 += 4) two_pairs(s2, false);
         }
-        // ---- block end: A complete (B arrived before the first warp's scales), one thread
-        // issues the block's 24 MMAs ----
+        // ---- block end: A complete; lane 0 of warp s issues sweep s's 12 MMAs once it has seen
+        // the block's tiles arrive, and commits them (the barrier's phase needs both commits) ----
         umma::wait_st();
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
-        if (tid == 0) {
-            // per sweep: the five small products of both halves first, hi x hi of both last; the
-            // first MMA starts D from zero
-            // descriptors of buffer q % 2: the first one's plus the planes' offsets (in 16-byte
-            // units, within the 14-bit address field: shared memory lies below 256 KB)
-            const uint64_t bq = bdesc0 + (uint64_t)((q & 1) * (2 * sizeof(BTile) / 16));
+        // the five small products of both halves first, hi x hi of both last; the first MMA
+        // starts D from zero.  Descriptors of buffer q % 2: the first one's plus the planes'
+        // offsets (in 16-byte units, within the 14-bit address field: shared memory lies below
+        // 256 KB)
+        auto issue = [&](auto sweep) {
+            constexpr int s = decltype(sweep)::value;
+            ok &= umma::mbar_wait(&sm.bbar[q & 1], (uint32_t)((q >> 1) & 1), kWaitLimit);
+            const uint64_t bq = bdesc0 + (uint64_t)((q & 1) * (2 * sizeof(BTile) / 16) + s * (sizeof(BTile) / 16));
 #pragma unroll
-            for (int s = 0; s < 2; ++s)
+            for (int ps = 0; ps < 6; ++ps)
 #pragma unroll
-                for (int ps = 0; ps < 6; ++ps)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const uint32_t off = (uint32_t)(s * sizeof(BTile)) +
-                                             (kShift && ps == 5 && h == 1 ? (uint32_t)offsetof(BTile, Bsh)
-                                                                          : (uint32_t)((h * kPlanes + kPass[ps][1]) * kBPlane));
-                        umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h),
-                                          bq + (off >> 4), kIdesc, ps > 0 || h > 0);
-                    }
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t off = kShift && ps == 5 && h == 1 ? (uint32_t)offsetof(BTile, Bsh)
+                                                                     : (uint32_t)((h * kPlanes + kPass[ps][1]) * kBPlane);
+                    umma::mma_bf16_ts(tbase + (uint32_t)(s * kMmaCols), tbase + a_col(s, kPass[ps][0], h),
+                                      bq + (off >> 4), kIdesc, ps > 0 || h > 0);
+                }
             umma::mma_commit(&sm.mbar);
-        }
+        };
+        if (tid == 0) issue(std::integral_constant<int, 0>{});
+        else if (tid == 32) issue(std::integral_constant<int, 1>{});
     }
     flush(nk - 1);
     if (!ok) atomicExch(p.status, 1u);

@@ -58,9 +58,10 @@ __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence
 // generic-proxy shared-memory writes made visible to the tensor core (async proxy)
 __device__ __forceinline__ void fence_smem_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
-__device__ __forceinline__ void mbar_init(uint64_t* bar)
+// An mbarrier whose phases complete after `count` arrivals.
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count = 1)
 {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 // Bounded wait for the completion of phase `parity`; false when it gave up.
